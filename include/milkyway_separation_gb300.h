@@ -1,0 +1,309 @@
+/*
+ * milkyway_separation_gb300.h -- C ABI of the GB300 (sm_103a) separation
+ * likelihood library, libmwsep_gb300.so.
+ *
+ * The library is a drop-in for the evaluator slot of the Milkyway@Home
+ * separation client: the reference registers an evaluator of type
+ *
+ *     typedef double (*EvalFunc)(double*, ASTRONOMY_PARAMETERS*,
+ *                                EVALUATION_STATE*, STAR_POINTS*);
+ *
+ * (milkyway_separation/cpu/simple_evaluator.h:26) and calls it once from
+ * worker() (src/milkyway_client_app.c:263-278).  mwsep_evaluate() below has
+ * that signature and fills EVALUATION_STATE the way cpu_evaluate does.
+ *
+ * The problem structs are layout-compatible with the reference's
+ * (cpu/parameters.h:27-71, cpu/star_points.h:27-31,
+ * cpu/evaluation_state.h:30-58).  They are defined here under the reference
+ * headers' own include guards, so a translation unit may include either the
+ * reference headers or this one first; whichever comes first defines them.
+ *
+ * Every function except the EvalFunc-shaped ones returns an int status
+ * (MWSEP_OK == 0).  The library never calls exit(); the EvalFunc-shaped
+ * entry points return NaN on failure and record the status, readable with
+ * mwsep_last_error().  All device work runs on one GPU.  There is no CPU
+ * fallback: without a usable sm_103a device every call fails with
+ * MWSEP_ERR_CUDA.
+ */
+#ifndef MILKYWAY_SEPARATION_GB300_H
+#define MILKYWAY_SEPARATION_GB300_H
+
+#include <stddef.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Reference problem structs (layout-compatible)                       */
+/* ------------------------------------------------------------------ */
+
+#ifndef ASTRONOMY_PARAMETERS_H
+#define ASTRONOMY_PARAMETERS_H
+/* cpu/parameters.h:27-35 */
+typedef struct
+{
+    double r_min, r_max, r_step_size;
+    double nu_min, nu_max, nu_step_size;
+    double mu_min, mu_max, mu_step_size;
+    int r_steps, nu_steps, mu_steps;
+
+    long min_calculation, max_calculation;
+} INTEGRAL;
+
+/* cpu/parameters.h:37-71 */
+typedef struct
+{
+    double parameters_version;
+
+    int number_background_parameters;
+    double background_weight;
+    double* background_parameters;
+    double* background_step;
+    double* background_min;
+    double* background_max;
+    int* background_optimize;
+
+    int number_streams;
+    int number_stream_parameters;
+
+    double* stream_weights;
+    double* stream_weight_step;
+    double* stream_weight_min;
+    double* stream_weight_max;
+    int* stream_weight_optimize;
+
+    double** stream_parameters;
+    double** stream_step;
+    double** stream_min;
+    double** stream_max;
+    int** stream_optimize;
+
+    int convolve;
+    int sgr_coordinates;
+    int aux_bg_profile;
+    int wedge;
+
+    int number_integrals;
+    INTEGRAL** integral;
+} ASTRONOMY_PARAMETERS;
+#endif
+
+#ifndef _STAR_POINTS_H_
+#define _STAR_POINTS_H_
+/* cpu/star_points.h:27-31: stars[i] = {l (deg), b (deg), r (kpc)} */
+typedef struct star_points
+{
+    int number_stars;
+    double** stars;
+} STAR_POINTS;
+#endif
+
+#ifndef _EVALUATION_STATE_H_
+#define _EVALUATION_STATE_H_
+/* cpu/evaluation_state.h:30-41 */
+typedef struct integral_area
+{
+    int mu_steps, nu_steps, r_steps;
+    double mu_min, nu_min, r_min;
+    double mu_max, nu_max, r_max;
+    double mu_step_size, nu_step_size, r_step_size;
+
+    long min_calculation, max_calculation, current_calculation;
+
+    int number_streams;
+    double background_integral, *stream_integrals;
+} INTEGRAL_AREA;
+
+/* cpu/evaluation_state.h:43-58 */
+typedef struct evaluation_state
+{
+    INTEGRAL_AREA** integral;
+    int current_integral, number_streams, number_integrals;
+
+    double background_integral;
+    double* stream_integrals;
+
+    int current_star_point, total_stars;
+    int num_zero;
+    int bad_jacobians;
+    double prob_sum;
+} EVALUATION_STATE;
+#endif
+
+#ifndef _SIMPLE_EVALUATOR_H_
+/* cpu/simple_evaluator.h:26 */
+typedef double (*EvalFunc)(double*, ASTRONOMY_PARAMETERS*, EVALUATION_STATE*, STAR_POINTS*);
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes and limits                                             */
+/* ------------------------------------------------------------------ */
+
+enum
+{
+    MWSEP_OK = 0,
+    MWSEP_ERR_ARG = 1,        /* NULL pointer, bad size, bad enum          */
+    MWSEP_ERR_IO = 2,         /* file missing or unparsable                */
+    MWSEP_ERR_PARAM_COUNT = 3,/* theta length != optimised-parameter count */
+    MWSEP_ERR_UNSUPPORTED = 4,/* outside MWSEP_MAX_* limits                */
+    MWSEP_ERR_CUDA = 5,       /* CUDA runtime error / no sm_103a device    */
+    MWSEP_ERR_NOMEM = 6,      /* host or device allocation failed          */
+    MWSEP_ERR_BUDGET = 7,     /* request exceeds the context HBM budget    */
+    MWSEP_ERR_TIMEOUT = 8,    /* a bounded wait ran out                    */
+    MWSEP_ERR_CANCELLED = 9,  /* serving request cancelled before launch   */
+    MWSEP_ERR_STATE = 10      /* call out of order (no problem / no stars) */
+};
+
+#define MWSEP_MAX_STREAMS 8
+#define MWSEP_MAX_AREAS 8
+#define MWSEP_MAX_CONVOLVE 512
+#define MWSEP_MAX_BG_PARAMS 8
+#define MWSEP_MAX_STREAM_PARAMS 8
+
+/* Arithmetic of one evaluation. */
+enum
+{
+    /* FP64 end to end, the reference's cell and convolution order.  The
+     * drop-in form: within 1e-12 relative of the reference on each
+     * integral and 1e-12 absolute on the log-likelihood. */
+    MWSEP_PLAIN_F64 = 0,
+    /* Densities and exp in FP32 (SFU) with compensated per-thread sums;
+     * geometry, tables, cross-block sums, normalisation and the
+     * log-likelihood in FP64.  Within 1e-7 absolute on the log-likelihood. */
+    MWSEP_MIXED_F32 = 1
+};
+
+const char* mwsep_status_string(int status);
+/* Status of the most recent failing call on this thread (0 if none). */
+int mwsep_last_error(void);
+/* Library build/version string. */
+const char* mwsep_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Problem I/O, same file formats and semantics as the reference        */
+/* ------------------------------------------------------------------ */
+
+/* Replaces read_astronomy_parameters (cpu/parameters.c:61-91) and
+ * fread_astronomy_parameters (:107-228).  Fills *ap with heap arrays; free
+ * them with mwsep_free_parameters. */
+int mwsep_read_astronomy_parameters(const char* path, ASTRONOMY_PARAMETERS* ap);
+/* Replaces write_astronomy_parameters (cpu/parameters.c:93-105, 230-305). */
+int mwsep_write_astronomy_parameters(const char* path, const ASTRONOMY_PARAMETERS* ap);
+/* Replaces free_parameters (cpu/parameters.c:27-59). */
+void mwsep_free_parameters(ASTRONOMY_PARAMETERS* ap);
+/* Replaces get_optimized_parameter_count (cpu/parameters.c:307-330). */
+int mwsep_get_optimized_parameter_count(const ASTRONOMY_PARAMETERS* ap);
+/* Replaces set_astronomy_parameters (cpu/parameters.c:332-363). */
+int mwsep_set_astronomy_parameters(ASTRONOMY_PARAMETERS* ap, const double* parameters);
+/* Replaces get_search_parameters (cpu/parameters.c:365-397); out holds
+ * get_optimized_parameter_count doubles. */
+int mwsep_get_search_parameters(const ASTRONOMY_PARAMETERS* ap, double* out);
+/* Replaces split_astronomy_parameters (cpu/parameters.c:502-522), without
+ * its printf. */
+int mwsep_split_astronomy_parameters(ASTRONOMY_PARAMETERS* ap, int rank, int max_rank);
+
+/* Replaces read_star_points (cpu/star_points.c:26-52, 69-81). */
+int mwsep_read_star_points(const char* path, STAR_POINTS* sp);
+/* Replaces write_star_points (cpu/star_points.c:54-67, 83-93). */
+int mwsep_write_star_points(const char* path, const STAR_POINTS* sp);
+/* Replaces free_star_points (cpu/star_points.c:95-103). */
+void mwsep_free_star_points(STAR_POINTS* sp);
+/* Replaces split_star_points (cpu/star_points.c:105-131). */
+int mwsep_split_star_points(STAR_POINTS* sp, int rank, int max_rank);
+
+/* Replaces initialize_state (cpu/evaluation_state.c:153-176). */
+int mwsep_initialize_state(const ASTRONOMY_PARAMETERS* ap, const STAR_POINTS* sp, EVALUATION_STATE* es);
+/* Replaces free_state (cpu/evaluation_state.c:201-211). */
+void mwsep_free_state(EVALUATION_STATE* es);
+
+/* ------------------------------------------------------------------ */
+/* EvalFunc drop-ins                                                    */
+/* ------------------------------------------------------------------ */
+
+/* Plain FP64 evaluation on the GPU.  Replaces cpu_evaluate
+ * (cpu/evaluation_optimized.c:756-784) and cuda_evaluate
+ * (cuda/evaluation_gpu6.cu:1058-1106, cuda/evaluation_gpu.h:34-37).
+ * Applies parameters to *ap (set_astronomy_parameters), evaluates every
+ * integral area and every star, writes es->integral[i]->*_integral,
+ * es->background_integral, es->stream_integrals[], es->prob_sum,
+ * es->num_zero, and returns prob_sum / number_stars.  The caller subtracts
+ * 3.0 as worker() does (src/milkyway_client_app.c:278).  Does not need
+ * init_constants.  Each call uploads the catalogue and rebuilds the wedge
+ * tables (no state kept between calls besides device buffers).  Returns NaN
+ * on failure (see mwsep_last_error). */
+double mwsep_evaluate(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
+
+/* Same contract in the compensated-FP32 form (MWSEP_MIXED_F32).  Replaces
+ * the same reference entry points for callers that accept 1e-7 on the
+ * log-likelihood. */
+double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
+
+/* ------------------------------------------------------------------ */
+/* Context API: resident wedges and catalogues, batches                 */
+/* ------------------------------------------------------------------ */
+
+typedef struct mwsep_ctx mwsep_ctx;
+
+/* One evaluation's results.  likelihood = prob_sum/N - 3.0 (the value the
+ * reference client prints as <search_likelihood>). */
+typedef struct
+{
+    double likelihood;
+    double prob_sum;
+    int num_zero;
+    int number_streams;
+    int number_integrals;
+    int status;
+    double background_integral;
+    double stream_integrals[MWSEP_MAX_STREAMS];
+    double area_integrals[MWSEP_MAX_AREAS][1 + MWSEP_MAX_STREAMS];
+    /* <background_only_likelihood>, <stream_only_likelihood> diagnostics
+     * (cpu/evaluation_optimized.c:719-733), already minus 3.0 */
+    double background_only_likelihood;
+    double stream_only_likelihood[MWSEP_MAX_STREAMS];
+} mwsep_result;
+
+/* Create a context on CUDA device `device` (one stream, one GPU). */
+int mwsep_ctx_create(int device, mwsep_ctx** out);
+int mwsep_ctx_destroy(mwsep_ctx* ctx);
+
+/* Make the wedge description of *ap resident: integral areas, convolve,
+ * coordinate system, wedge, aux profile and the theta layout (optimize
+ * flags).  Builds the per-(mu,nu) geometry and r-bin tables on the device.
+ * Replaces any previous problem. */
+int mwsep_ctx_set_problem(mwsep_ctx* ctx, const ASTRONOMY_PARAMETERS* ap);
+/* Make a catalogue resident (rows {l, b, r_kpc}) and build its per-star
+ * convolution tables on the device. */
+int mwsep_ctx_set_stars(mwsep_ctx* ctx, const STAR_POINTS* sp);
+int mwsep_ctx_set_stars_soa(mwsep_ctx* ctx, int n, const double* l, const double* b, const double* r);
+
+/* Number of theta values the resident problem expects. */
+int mwsep_ctx_theta_count(const mwsep_ctx* ctx);
+
+/* One evaluation of theta (mwsep_ctx_theta_count doubles) in `precision`. */
+int mwsep_ctx_evaluate(mwsep_ctx* ctx, const double* theta, int precision, mwsep_result* out);
+
+/* A population: n_theta vectors, row-major [n_theta][theta_count], evaluated
+ * together (one batched launch per phase).  out[n_theta].  Each result is
+ * the same as that theta evaluated alone. */
+int mwsep_ctx_evaluate_batch(mwsep_ctx* ctx, int n_theta, const double* thetas, int precision, mwsep_result* out);
+
+/* Bytes of device memory the context holds (tables, catalogue, scratch). */
+int mwsep_ctx_device_bytes(const mwsep_ctx* ctx, size_t* out);
+
+/* Per-phase device time of the last evaluate/evaluate_batch call, measured
+ * with CUDA events on the context stream, in milliseconds:
+ * out[0] integral kernels, out[1] integral reduction, out[2] likelihood
+ * kernels, out[3] likelihood reduction, out[4] whole call. */
+int mwsep_ctx_last_timings(const mwsep_ctx* ctx, double* out5);
+
+/* Number of kernel launches issued by the last evaluate/evaluate_batch. */
+int mwsep_ctx_last_launches(const mwsep_ctx* ctx, int* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MILKYWAY_SEPARATION_GB300_H */

@@ -1,0 +1,13 @@
+"""GB300-native (sm_103a) separation likelihood for Milkyway@Home.
+
+The compute path is libmwsep_gb300.so (hand-written CUDA kernels behind a C
+ABI, include/milkyway_separation_gb300.h); this package holds its sources,
+its in-tree build and a Python mirror of the reference client's evaluation
+interface.
+"""
+from .native import (MWSEP_MIXED_F32, MWSEP_PLAIN_F64, MwsepError)  # noqa: F401
+from .separation import (AstronomyParameters, Context, EvaluationState, Result,  # noqa: F401
+                         StarPoints, evaluate, evaluate_mixed)
+
+__all__ = ["AstronomyParameters", "StarPoints", "EvaluationState", "Context", "Result",
+           "evaluate", "evaluate_mixed", "MWSEP_PLAIN_F64", "MWSEP_MIXED_F32", "MwsepError"]

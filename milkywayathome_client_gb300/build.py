@@ -1,0 +1,94 @@
+"""In-tree build of libmwsep_gb300.so (CUDA kernels + C ABI) for sm_103a.
+
+Translation units are compiled in parallel and linked with nvcc; nothing is
+installed outside the package directory.  The FP64 files are compiled with
+``-fmad=false`` so no product or sum is fused (the reference CPU path
+evaluates every operation separately); the compensated-FP32 file keeps FMA
+contraction on.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(REPO_DIR, "include")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_DIR = os.path.join(PKG_DIR, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libmwsep_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
+
+# (source, extra nvcc flags)
+UNITS = [
+    ("mwsep_host.cu", ["-fmad=false"]),
+    ("mwsep_geometry.cu", ["-fmad=false"]),
+    ("mwsep_f64.cu", ["-fmad=false"]),
+    ("mwsep_reduce.cu", ["-fmad=false"]),
+    ("mwsep_f32.cu", ["-fmad=true"]),
+    ("mwsep_io.cpp", []),
+]
+
+
+def nvcc() -> str:
+    cand = [os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"]
+    for c in cand:
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libmwsep_gb300")
+
+
+def _sources_newer_than(target: str) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(unit, extra, verbose):
+    src = os.path.join(CSRC, unit)
+    obj = os.path.join(BUILD_DIR, unit + ".o")
+    cmd = [nvcc(), "-c", src, "-o", obj, "-std=c++17", "-O3", "-lineinfo", *ARCH,
+           "-I" + INCLUDE, "-I" + CSRC, "-Xcompiler", ",".join(HOST_FLAGS), *extra]
+    if unit.endswith(".cpp"):
+        cmd += ["-x", "c++"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compiling {unit} failed:\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout + r.stderr, flush=True)
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every translation unit and link the shared library."""
+    if not force and not _sources_newer_than(LIB_PATH):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda u: _compile(u[0], u[1], verbose), UNITS))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lpthread"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"linking libmwsep_gb300.so failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

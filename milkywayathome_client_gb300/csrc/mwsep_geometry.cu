@@ -1,0 +1,105 @@
+/* mwsep_geometry.cu -- parameter-independent device tables.
+ *
+ *  - per-(mu, nu) column of a wedge: Galactic (l, b) of the column centre
+ *    and the four sines/cosines the density loop uses;
+ *  - per-star convolution tables (the per-star set_probability_constants).
+ *
+ * Compiled with -fmad=false; transcendentals are CUDA's double-precision
+ * libm (<= 2 ulp), so these tables agree with the reference's host tables
+ * to a few ulp rather than bit for bit; the tests bound that.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include "mwsep_internal.h"
+#include "mwsep_geometry.cuh"
+
+namespace {
+
+/* One (mu, nu) column: cpu/evaluation_optimized.c:463 and :480-491, then
+ * the per-point sines/cosines of calculate_probabilities :205-208. */
+__global__ void geometry_kernel(double mu_min, double mu_step, int mu_steps, const double* __restrict__ nus,
+                                int nu_steps, int sgr, int wedge, double* __restrict__ geom)
+{
+    const int n = mu_steps * nu_steps;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
+    {
+        const int i = idx / nu_steps;
+        const int j = idx - i * nu_steps;
+        const double mu = mu_min + (i * mu_step);
+        const double nu = nus[j];
+        double l, b;
+        mwsep::wedge_point_lb(sgr, wedge, mu + 0.5 * mu_step, nu, l, b);
+        double* g = geom + 4 * (size_t)idx;
+        g[0] = sin(b / MW_DEG);
+        g[1] = cos(b / MW_DEG);
+        g[2] = sin(l / MW_DEG);
+        g[3] = cos(l / MW_DEG);
+    }
+}
+
+/* Per-star tables: cpu/evaluation_optimized.c:159-188 applied to the
+ * star's distance, plus its sines/cosines (:205-208).  Tables are [C][N]. */
+__global__ void star_tables_kernel(int n, const double* __restrict__ l, const double* __restrict__ b,
+                                   const double* __restrict__ r, int C, const double* __restrict__ dx,
+                                   const double* __restrict__ gl_w, double coeff, double* __restrict__ geom,
+                                   double* __restrict__ r_point, double* __restrict__ qw,
+                                   double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
+                                   double* __restrict__ reff, float* __restrict__ r_hi, float* __restrict__ r_lo,
+                                   float* __restrict__ qwv, float* __restrict__ gmag)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        double gPrime, rf;
+        mwsep::prob_consts_head(r[s], gPrime, rf);
+        reff[s] = rf;
+        for (int i = 0; i < C; ++i)
+        {
+            double g, rp, q;
+            mwsep::prob_consts_point(gPrime, dx[i], gl_w[i], coeff, g, rp, q);
+            const size_t o = (size_t)i * n + s;
+            r_in_mag[o] = g;
+            r_in_mag2[o] = g * g;
+            r_point[o] = rp;
+            qw[o] = q;
+            const float hi = (float)rp;
+            r_hi[o] = hi;
+            r_lo[o] = (float)(rp - (double)hi);
+            qwv[o] = (float)(q * rf);
+            gmag[o] = (float)g;
+        }
+        double* gg = geom + 4 * (size_t)s;
+        gg[0] = sin(b[s] / MW_DEG);
+        gg[1] = cos(b[s] / MW_DEG);
+        gg[2] = sin(l[s] / MW_DEG);
+        gg[3] = cos(l[s] / MW_DEG);
+    }
+}
+
+} // namespace
+
+extern "C" int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps, const double* nus, int nu_steps,
+                                     int sgr, int wedge, double* geom_out, void* stream)
+{
+    const int n = mu_steps * nu_steps;
+    if (n <= 0) return 0;
+    int grid = (n + 255) / 256;
+    if (grid > 152 * 32) grid = 152 * 32;
+    geometry_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(mu_min, mu_step, mu_steps, nus,
+                                                            nu_steps, sgr, wedge, geom_out);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
+                                        const double* dx, const double* gl_w, double coeff, double* geom,
+                                        double* r_point, double* qw, double* r_in_mag, double* r_in_mag2,
+                                        double* reff, float* r_hi, float* r_lo, float* qwv, float* gmag,
+                                        void* stream)
+{
+    if (n <= 0) return 0;
+    int grid = (n + 127) / 128;
+    if (grid > 152 * 32) grid = 152 * 32;
+    star_tables_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(n, l, b, r, convolve, dx, gl_w, coeff, geom,
+                                                               r_point, qw, r_in_mag, r_in_mag2, reff, r_hi,
+                                                               r_lo, qwv, gmag);
+    return (int)cudaGetLastError();
+}

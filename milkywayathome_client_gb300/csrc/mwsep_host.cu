@@ -1,0 +1,953 @@
+/* mwsep_host.cu -- host orchestration of libmwsep_gb300.
+ *
+ * Owns the device context (one GPU, one stream), builds the resident wedge
+ * and catalogue tables, computes the per-evaluation constants and issues the
+ * kernel sequence of one evaluation or one batch:
+ *
+ *   H2D theta constants -> integral kernel per area -> integral reduction
+ *   -> likelihood kernel -> likelihood reduction -> one D2H of the results.
+ *
+ * The integrals stay on the device between the two phases (the reference's
+ * GPU backend copied per-cell partials back and summed on the host,
+ * cuda/evaluation_gpu6.cu:639-767).
+ *
+ * Host-side formulas (r-bin tables, theta constants) are the reference's
+ * (cpu/evaluation_optimized.c) evaluated with glibc libm, compiled with
+ * -ffp-contract=off, so they equal the reference's doubles bit for bit.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "milkyway_separation_gb300.h"
+#include "mwsep_geometry.cuh"
+#include "mwsep_internal.h"
+#include "mwsep_status.h"
+
+/* ---------------------------------------------------------------- status */
+
+static thread_local int tl_last_error = 0;
+
+extern "C" int mwsep_fail(int status)
+{
+    if (status != MWSEP_OK) tl_last_error = status;
+    return status;
+}
+
+extern "C" int mwsep_last_error(void) { return tl_last_error; }
+
+extern "C" const char* mwsep_status_string(int s)
+{
+    switch (s)
+    {
+    case MWSEP_OK: return "ok";
+    case MWSEP_ERR_ARG: return "invalid argument";
+    case MWSEP_ERR_IO: return "file missing or unparsable";
+    case MWSEP_ERR_PARAM_COUNT: return "parameter vector length does not match the optimised-parameter count";
+    case MWSEP_ERR_UNSUPPORTED: return "problem outside the library limits";
+    case MWSEP_ERR_CUDA: return "CUDA error or no sm_103 device";
+    case MWSEP_ERR_NOMEM: return "out of memory";
+    case MWSEP_ERR_BUDGET: return "request exceeds the device-memory budget";
+    case MWSEP_ERR_TIMEOUT: return "bounded wait ran out";
+    case MWSEP_ERR_CANCELLED: return "request cancelled";
+    case MWSEP_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char* mwsep_version(void) { return "libmwsep_gb300 1.0 (sm_103a)"; }
+
+#define CU(call)                                                                                           \
+    do                                                                                                     \
+    {                                                                                                      \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+        {                                                                                                  \
+            if (getenv("MWSEP_DEBUG"))                                                                     \
+                fprintf(stderr, "mwsep: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                         \
+            return mwsep_fail(MWSEP_ERR_CUDA);                                                             \
+        }                                                                                                  \
+    } while (0)
+
+#define CK(expr)                                                                                           \
+    do                                                                                                     \
+    {                                                                                                      \
+        int s_ = (expr);                                                                                   \
+        if (s_ != 0)                                                                                       \
+        {                                                                                                  \
+            if (getenv("MWSEP_DEBUG"))                                                                     \
+                fprintf(stderr, "mwsep: %s failed: %d (%s:%d)\n", #expr, s_, __FILE__, __LINE__);          \
+            return mwsep_fail(MWSEP_ERR_CUDA);                                                             \
+        }                                                                                                  \
+    } while (0)
+
+/* --------------------------------------------------------- device memory */
+
+namespace {
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want, size_t& total)
+    {
+        if (want <= bytes) return MWSEP_OK;
+        if (p)
+        {
+            cudaFree(p);
+            total -= bytes;
+            p = nullptr;
+            bytes = 0;
+        }
+        if (want == 0) return MWSEP_OK;
+        if (cudaMalloc(&p, want) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return MWSEP_ERR_NOMEM;
+        }
+        bytes = want;
+        total += bytes;
+        return MWSEP_OK;
+    }
+    void release(size_t& total)
+    {
+        if (p)
+        {
+            cudaFree(p);
+            total -= bytes;
+        }
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return (T*)p; }
+};
+
+struct HostPinned
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want)
+    {
+        if (want <= bytes) return MWSEP_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMallocHost(&p, want) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return MWSEP_ERR_NOMEM;
+        }
+        bytes = want;
+        return MWSEP_OK;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return (T*)p; }
+};
+
+/* numericalIntegration.c:67-104 (Numerical Recipes gauleg on [-1, 1]). */
+void gauss_legendre(int n, double* x, double* w)
+{
+    const double x1 = -1.0, x2 = 1.0, eps = 3.0e-11;
+    const int m = (n + 1) / 2;
+    const double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+    for (int i = 1; i <= m; ++i)
+    {
+        double z = cos(MW_PI * (i - 0.25) / (n + 0.5)), z1, pp, p1, p2, p3;
+        int guard = 0;
+        do
+        {
+            p1 = 1.0;
+            p2 = 0.0;
+            for (int j = 1; j <= n; ++j)
+            {
+                p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            z1 = z;
+            z = z1 - p1 / pp;
+        } while (fabs(z - z1) > eps && ++guard < 1000);
+        x[i - 1] = xm - xl * z;
+        x[n - i] = xm + xl * z;
+        w[i - 1] = 2.0 * xl / ((1.0 - z * z) * pp * pp);
+        w[n - i] = w[i - 1];
+    }
+}
+
+/* Host description of one integral area. */
+struct AreaHost
+{
+    int mu_steps, nu_steps, r_steps;
+    double mu_min, mu_max, nu_min, nu_max, r_min, r_max;
+    double mu_step, nu_step, r_step;
+};
+
+struct AreaDev
+{
+    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, r_hi, r_lo, qwv, gmag;
+    mwsep_area_dev view{};
+};
+
+/* The theta layout and the fixed values of the problem (a private copy of
+ * the reference struct's values). */
+struct ProblemHost
+{
+    int n_bg = 0, n_streams = 0, n_sparams = 0;
+    double bg_weight = 0.0;
+    double bg[MWSEP_MAX_BG_PARAMS] = {};
+    int bg_opt[MWSEP_MAX_BG_PARAMS] = {};
+    double st_weight[MWSEP_MAX_STREAMS] = {};
+    int st_weight_opt[MWSEP_MAX_STREAMS] = {};
+    double st[MWSEP_MAX_STREAMS][MWSEP_MAX_STREAM_PARAMS] = {};
+    int st_opt[MWSEP_MAX_STREAMS][MWSEP_MAX_STREAM_PARAMS] = {};
+    int convolve = 0, sgr = 0, aux = 0, wedge = 0;
+    int n_areas = 0;
+    AreaHost area[MWSEP_MAX_AREAS];
+    int n_theta = 0;
+};
+
+/* Launch tuning of one precision. */
+struct Tune
+{
+    int block = 256;
+    int grid = 0;
+    int k_chunk = 0;
+    int lk_block = 256;
+    int lk_grid = 0;
+};
+
+} // namespace
+
+struct mwsep_ctx
+{
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    size_t dev_bytes = 0;
+
+    bool has_problem = false;
+    ProblemHost prob;
+    std::vector<double> gl_x, gl_w, dx;
+    double coeff = 0.0;
+    AreaDev areas[MWSEP_MAX_AREAS];
+    DevBuf d_dx, d_glw;
+
+    bool has_stars = false;
+    int n_stars = 0;
+    DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_r_hi, s_r_lo, s_qwv,
+        s_gmag;
+    mwsep_stars_dev stars_view{};
+    HostPinned h_stars;
+
+    DevBuf d_theta, d_partials, d_lkpartials, d_out;
+    HostPinned h_theta, h_out;
+
+    Tune tune[2];
+    double last_ms[5] = {};
+    int last_launches = 0;
+};
+
+namespace {
+
+int check_problem(const ASTRONOMY_PARAMETERS* ap)
+{
+    if (!ap) return MWSEP_ERR_ARG;
+    if (ap->number_streams < 0 || ap->number_streams > MWSEP_MAX_STREAMS) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->number_integrals < 1 || ap->number_integrals > MWSEP_MAX_AREAS) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->convolve < 1 || ap->convolve > MWSEP_MAX_CONVOLVE) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->number_background_parameters < 4 || ap->number_background_parameters > MWSEP_MAX_BG_PARAMS)
+        return MWSEP_ERR_UNSUPPORTED;
+    if (ap->aux_bg_profile != 0 && ap->aux_bg_profile != 1) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->aux_bg_profile == 1 && ap->number_background_parameters < 7) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->sgr_coordinates != 0 && ap->sgr_coordinates != 1) return MWSEP_ERR_UNSUPPORTED;
+    if (ap->number_streams > 0 &&
+        (ap->number_stream_parameters < 5 || ap->number_stream_parameters > MWSEP_MAX_STREAM_PARAMS))
+        return MWSEP_ERR_UNSUPPORTED;
+    for (int i = 0; i < ap->number_integrals; ++i)
+    {
+        const INTEGRAL* in = ap->integral[i];
+        if (!in || in->mu_steps < 1 || in->nu_steps < 1 || in->r_steps < 1) return MWSEP_ERR_ARG;
+        if ((long long)in->mu_steps * in->nu_steps > (1LL << 30)) return MWSEP_ERR_UNSUPPORTED;
+    }
+    return MWSEP_OK;
+}
+
+/* Copy the reference struct's values into the context's private copy. */
+void copy_problem(const ASTRONOMY_PARAMETERS* ap, ProblemHost& p)
+{
+    p = ProblemHost();
+    p.n_bg = ap->number_background_parameters;
+    p.n_streams = ap->number_streams;
+    p.n_sparams = ap->number_stream_parameters;
+    p.bg_weight = ap->background_weight;
+    for (int i = 0; i < p.n_bg; ++i)
+    {
+        p.bg[i] = ap->background_parameters[i];
+        p.bg_opt[i] = ap->background_optimize[i];
+    }
+    for (int s = 0; s < p.n_streams; ++s)
+    {
+        p.st_weight[s] = ap->stream_weights[s];
+        p.st_weight_opt[s] = ap->stream_weight_optimize[s];
+        for (int j = 0; j < p.n_sparams; ++j)
+        {
+            p.st[s][j] = ap->stream_parameters[s][j];
+            p.st_opt[s][j] = ap->stream_optimize[s][j];
+        }
+    }
+    p.convolve = ap->convolve;
+    p.sgr = ap->sgr_coordinates;
+    p.aux = ap->aux_bg_profile;
+    p.wedge = ap->wedge;
+    p.n_areas = ap->number_integrals;
+    for (int a = 0; a < p.n_areas; ++a)
+    {
+        const INTEGRAL* in = ap->integral[a];
+        AreaHost& A = p.area[a];
+        A.mu_steps = in->mu_steps;
+        A.nu_steps = in->nu_steps;
+        A.r_steps = in->r_steps;
+        A.mu_min = in->mu_min;
+        A.mu_max = in->mu_max;
+        A.nu_min = in->nu_min;
+        A.nu_max = in->nu_max;
+        A.r_min = in->r_min;
+        A.r_max = in->r_max;
+        /* INTEGRAL_AREA step sizes (cpu/evaluation_state.c:247-249) */
+        A.mu_step = (A.mu_max - A.mu_min) / A.mu_steps;
+        A.nu_step = (A.nu_max - A.nu_min) / A.nu_steps;
+        A.r_step = (A.r_max - A.r_min) / A.r_steps;
+    }
+    int n = 0;
+    for (int i = 0; i < p.n_bg; ++i) n += p.bg_opt[i] ? 1 : 0;
+    for (int s = 0; s < p.n_streams; ++s)
+    {
+        n += p.st_weight_opt[s] ? 1 : 0;
+        for (int j = 0; j < p.n_sparams; ++j) n += p.st_opt[s][j] ? 1 : 0;
+    }
+    p.n_theta = n;
+}
+
+/* theta -> constants: set_astronomy_parameters (cpu/parameters.c:332-363),
+ * init_constants (cpu/evaluation_optimized.c:54-133) and the likelihood
+ * weights (:639-646). */
+void theta_consts(const ProblemHost& base, const double* theta, mwsep_theta_consts& th)
+{
+    ProblemHost p = base;
+    int k = 0;
+    for (int i = 0; i < p.n_bg; ++i)
+        if (p.bg_opt[i]) p.bg[i] = theta[k++];
+    for (int s = 0; s < p.n_streams; ++s)
+    {
+        if (p.st_weight_opt[s]) p.st_weight[s] = theta[k++];
+        for (int j = 0; j < p.n_sparams; ++j)
+            if (p.st_opt[s][j]) p.st[s][j] = theta[k++];
+    }
+    memset(&th, 0, sizeof(th));
+    th.alpha = p.bg[0];
+    th.q = p.bg[1];
+    th.r0 = p.bg[2];
+    th.delta = p.bg[3];
+    if (p.aux == 1)
+    {
+        th.bg_a = p.bg[4];
+        th.bg_b = p.bg[5];
+        th.bg_c = p.bg[6];
+    }
+    th.aux = p.aux;
+    th.alpha_delta3 = 3 - th.alpha + th.delta;
+    th.bg_mode = (th.q == 0) ? 2 : ((th.alpha == 1 && th.delta == 1) ? 0 : 1);
+    th.n_streams = p.n_streams;
+    for (int s = 0; s < p.n_streams; ++s)
+    {
+        const double sigma = p.st[s][4];
+        th.sigma_sq2[s] = 2.0 * sigma * sigma;
+        th.stream_on[s] = !(sigma > -0.0001 && sigma < 0.0001);
+        double l, b;
+        mwsep::wedge_point_lb(p.sgr, p.wedge, p.st[s][0], 0, l, b);
+        mwsep::lbr_to_xyz(l, b, p.st[s][1], th.c[s]);
+        th.a[s][0] = sin(p.st[s][2]) * cos(p.st[s][3]);
+        th.a[s][1] = sin(p.st[s][2]) * sin(p.st[s][3]);
+        th.a[s][2] = cos(p.st[s][2]);
+    }
+    th.exp_bg_weight = exp(p.bg_weight);
+    double sum = th.exp_bg_weight;
+    for (int s = 0; s < p.n_streams; ++s)
+    {
+        th.exp_stream_weight[s] = exp(p.st_weight[s]);
+        sum += exp(p.st_weight[s]);
+    }
+    th.sum_exp_weights = sum * 0.001;
+}
+
+int occupancy_grid(mwsep_ctx* c, int block, long long items)
+{
+    long long g = (items + block - 1) / block;
+    const long long cap = (long long)c->sm_count * (2048 / block);
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+/* Default launch shapes for the resident problem.  The shape depends only
+ * on the problem, never on the batch, so a theta gives the same bits alone
+ * and inside any batch. */
+void default_tune(mwsep_ctx* c)
+{
+    const ProblemHost& p = c->prob;
+    long long max_cols = 0;
+    int max_r = 1;
+    for (int a = 0; a < p.n_areas; ++a)
+    {
+        max_cols = std::max<long long>(max_cols, (long long)p.area[a].mu_steps * p.area[a].nu_steps);
+        max_r = std::max(max_r, p.area[a].r_steps);
+    }
+    for (int prec = 0; prec < 2; ++prec)
+    {
+        Tune& t = c->tune[prec];
+        t.block = 256;
+        /* enough items for ~32 per thread of a full-occupancy grid */
+        const long long want_items = (long long)c->sm_count * 2048 * 32;
+        long long chunks = (want_items + max_cols - 1) / std::max<long long>(max_cols, 1);
+        if (chunks < 1) chunks = 1;
+        if (chunks > max_r) chunks = max_r;
+        t.k_chunk = (int)((max_r + chunks - 1) / chunks);
+        long long items = max_cols * ((max_r + t.k_chunk - 1) / t.k_chunk);
+        t.grid = occupancy_grid(c, t.block, items);
+        t.lk_block = 256;
+        t.lk_grid = occupancy_grid(c, t.lk_block, std::max(c->n_stars, 1));
+    }
+}
+
+int build_area(mwsep_ctx* c, int a)
+{
+    const ProblemHost& p = c->prob;
+    const AreaHost& A = p.area[a];
+    AreaDev& D = c->areas[a];
+    const int R = A.r_steps, C = p.convolve, NU = A.nu_steps;
+    const size_t RC = (size_t)R * C;
+
+    /* cpu__r_constants (cpu/evaluation_optimized.c:360-422) on the host */
+    std::vector<double> irv(R), reff(R), rp(RC), qw(RC), gm(RC), gm2(RC), ids(NU), nus(NU);
+    std::vector<float> rhi(RC), rlo(RC), qwv(RC), gmf(RC);
+    for (int i = 0; i < R; ++i)
+    {
+        const double log_r = A.r_min + (i * A.r_step);
+        const double r = pow(10.0, (log_r - 14.2) / 5.0);
+        const double next_r = pow(10.0, (log_r + A.r_step - 14.2) / 5.0);
+        irv[i] = (((next_r * next_r * next_r) - (r * r * r)) / 3.0) * A.mu_step / MW_DEG;
+        const double rPrime = (next_r + r) / 2.0;
+        double gPrime;
+        mwsep::prob_consts_head(rPrime, gPrime, reff[i]);
+        for (int n = 0; n < C; ++n)
+        {
+            const size_t o = (size_t)i * C + n;
+            double g;
+            mwsep::prob_consts_point(gPrime, c->dx[n], c->gl_w[n], c->coeff, g, rp[o], qw[o]);
+            gm[o] = g;
+            gm2[o] = g * g;
+            const float hi = (float)rp[o];
+            rhi[o] = hi;
+            rlo[o] = (float)(rp[o] - (double)hi);
+            qwv[o] = (float)(qw[o] * (reff[i] * irv[i]));
+            gmf[o] = (float)g;
+        }
+    }
+    for (int j = 0; j < NU; ++j)
+    {
+        nus[j] = A.nu_min + (j * A.nu_step);
+        ids[j] = cos((90 - nus[j] - A.nu_step) / MW_DEG) - cos((90 - nus[j]) / MW_DEG);
+        nus[j] += 0.5 * A.nu_step;
+    }
+
+    const size_t cols = (size_t)A.mu_steps * NU;
+    size_t& tot = c->dev_bytes;
+    int rc = 0;
+    rc |= D.geom.ensure(cols * 4 * sizeof(double), tot);
+    rc |= D.r_point.ensure(RC * 8, tot);
+    rc |= D.qw.ensure(RC * 8, tot);
+    rc |= D.r_in_mag.ensure(RC * 8, tot);
+    rc |= D.r_in_mag2.ensure(RC * 8, tot);
+    rc |= D.reff.ensure(R * 8, tot);
+    rc |= D.irv.ensure(R * 8, tot);
+    rc |= D.ids.ensure(NU * 8, tot);
+    rc |= D.nus.ensure(NU * 8, tot);
+    rc |= D.r_hi.ensure(RC * 4, tot);
+    rc |= D.r_lo.ensure(RC * 4, tot);
+    rc |= D.qwv.ensure(RC * 4, tot);
+    rc |= D.gmag.ensure(RC * 4, tot);
+    if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
+
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(D.r_point.p, rp.data(), RC * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.qw.p, qw.data(), RC * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.r_in_mag.p, gm.data(), RC * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.r_in_mag2.p, gm2.data(), RC * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.reff.p, reff.data(), R * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.irv.p, irv.data(), R * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.ids.p, ids.data(), NU * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.nus.p, nus.data(), NU * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.r_hi.p, rhi.data(), RC * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.r_lo.p, rlo.data(), RC * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.qwv.p, qwv.data(), RC * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(D.gmag.p, gmf.data(), RC * 4, cudaMemcpyHostToDevice, st));
+    CK(mwsep_launch_geometry(A.mu_min, A.mu_step, A.mu_steps, D.nus.as<double>(), NU, p.sgr, p.wedge,
+                             D.geom.as<double>(), st));
+    /* the host vectors die with this frame: wait for the copies */
+    CU(cudaStreamSynchronize(st));
+
+    mwsep_area_dev& v = D.view;
+    v.mu_steps = A.mu_steps;
+    v.nu_steps = NU;
+    v.r_steps = R;
+    v.convolve = C;
+    v.n_cols = (int)cols;
+    v.geom = D.geom.as<double>();
+    v.r_point = D.r_point.as<double>();
+    v.qw = D.qw.as<double>();
+    v.r_in_mag = D.r_in_mag.as<double>();
+    v.r_in_mag2 = D.r_in_mag2.as<double>();
+    v.reff = D.reff.as<double>();
+    v.irv = D.irv.as<double>();
+    v.ids = D.ids.as<double>();
+    v.r_hi = D.r_hi.as<float>();
+    v.r_lo = D.r_lo.as<float>();
+    v.qwv = D.qwv.as<float>();
+    v.gmag = D.gmag.as<float>();
+    return MWSEP_OK;
+}
+
+void set_chunking(mwsep_area_dev& v, int k_chunk)
+{
+    v.k_chunk = std::max(1, std::min(k_chunk, v.r_steps));
+    v.n_kchunks = (v.r_steps + v.k_chunk - 1) / v.k_chunk;
+    v.n_items = (long long)v.n_cols * v.n_kchunks;
+}
+
+int upload_stars(mwsep_ctx* c, int n, const double* l, const double* b, const double* r)
+{
+    if (!c->has_problem) return mwsep_fail(MWSEP_ERR_STATE);
+    if (n < 1) return mwsep_fail(MWSEP_ERR_ARG);
+    const int C = c->prob.convolve;
+    const size_t NC = (size_t)n * C;
+    size_t& tot = c->dev_bytes;
+    int rc = 0;
+    rc |= c->s_l.ensure((size_t)n * 8, tot);
+    rc |= c->s_b.ensure((size_t)n * 8, tot);
+    rc |= c->s_r.ensure((size_t)n * 8, tot);
+    rc |= c->s_geom.ensure((size_t)n * 32, tot);
+    rc |= c->s_r_point.ensure(NC * 8, tot);
+    rc |= c->s_qw.ensure(NC * 8, tot);
+    rc |= c->s_r_in_mag.ensure(NC * 8, tot);
+    rc |= c->s_r_in_mag2.ensure(NC * 8, tot);
+    rc |= c->s_reff.ensure((size_t)n * 8, tot);
+    rc |= c->s_r_hi.ensure(NC * 4, tot);
+    rc |= c->s_r_lo.ensure(NC * 4, tot);
+    rc |= c->s_qwv.ensure(NC * 4, tot);
+    rc |= c->s_gmag.ensure(NC * 4, tot);
+    if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(c->s_l.p, l, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(c->s_b.p, b, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(c->s_r.p, r, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    CK(mwsep_launch_star_tables(n, c->s_l.as<double>(), c->s_b.as<double>(), c->s_r.as<double>(), C,
+                                c->d_dx.as<double>(), c->d_glw.as<double>(), c->coeff, c->s_geom.as<double>(),
+                                c->s_r_point.as<double>(), c->s_qw.as<double>(), c->s_r_in_mag.as<double>(),
+                                c->s_r_in_mag2.as<double>(), c->s_reff.as<double>(), c->s_r_hi.as<float>(),
+                                c->s_r_lo.as<float>(), c->s_qwv.as<float>(), c->s_gmag.as<float>(), st));
+    mwsep_stars_dev& v = c->stars_view;
+    v.n_stars = n;
+    v.convolve = C;
+    v.geom = c->s_geom.as<double>();
+    v.r_point = c->s_r_point.as<double>();
+    v.qw = c->s_qw.as<double>();
+    v.r_in_mag = c->s_r_in_mag.as<double>();
+    v.r_in_mag2 = c->s_r_in_mag2.as<double>();
+    v.reff = c->s_reff.as<double>();
+    v.r_hi = c->s_r_hi.as<float>();
+    v.r_lo = c->s_r_lo.as<float>();
+    v.qwv = c->s_qwv.as<float>();
+    v.gmag = c->s_gmag.as<float>();
+    c->n_stars = n;
+    c->has_stars = true;
+    for (int prec = 0; prec < 2; ++prec)
+        c->tune[prec].lk_grid = occupancy_grid(c, c->tune[prec].lk_block, n);
+    return MWSEP_OK;
+}
+
+int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out)
+{
+    if (!c->has_problem || !c->has_stars) return mwsep_fail(MWSEP_ERR_STATE);
+    if (B < 1 || B > 65535 || !thetas || !out) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
+    const ProblemHost& p = c->prob;
+    const int S = p.n_streams, A = p.n_areas, P = p.n_theta;
+    const Tune& t = c->tune[precision];
+    const int ncomp = 1 + S, nslots = 3 + S;
+
+    size_t& tot = c->dev_bytes;
+    const size_t th_bytes = sizeof(mwsep_theta_consts) * (size_t)B;
+    const size_t part_bytes = sizeof(double2) * (size_t)B * A * t.grid * ncomp;
+    const size_t lkpart_bytes = sizeof(double2) * (size_t)B * t.lk_grid * nslots;
+    const size_t out_doubles = (size_t)B * (A * ncomp + ncomp + nslots);
+    int rc = 0;
+    rc |= c->d_theta.ensure(th_bytes, tot);
+    rc |= c->d_partials.ensure(part_bytes, tot);
+    rc |= c->d_lkpartials.ensure(lkpart_bytes, tot);
+    rc |= c->d_out.ensure(out_doubles * 8, tot);
+    rc |= c->h_theta.ensure(th_bytes);
+    rc |= c->h_out.ensure(out_doubles * 8);
+    if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
+
+    mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
+    for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
+
+    double* d_areas = c->d_out.as<double>();
+    double* d_ints = d_areas + (size_t)B * A * ncomp;
+    double* d_lk = d_ints + (size_t)B * ncomp;
+
+    cudaStream_t st = c->stream;
+    int launches = 0;
+    CU(cudaEventRecord(c->ev[0], st));
+    CU(cudaMemcpyAsync(c->d_theta.p, hth, th_bytes, cudaMemcpyHostToDevice, st));
+    CU(cudaEventRecord(c->ev[1], st));
+    mwsep_launch_shape sh;
+    sh.n_theta = B;
+    sh.n_streams = S;
+    sh.n_areas = A;
+    sh.block = t.block;
+    sh.grid = t.grid;
+    for (int a = 0; a < A; ++a)
+    {
+        mwsep_area_dev v = c->areas[a].view;
+        set_chunking(v, t.k_chunk);
+        sh.area_index = a;
+        if (precision == MWSEP_PLAIN_F64)
+            CK(mwsep_launch_integral_f64(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                         c->d_partials.as<double2>(), st));
+        else
+            CK(mwsep_launch_integral_f32(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                         c->d_partials.as<double2>(), st));
+        ++launches;
+    }
+    CU(cudaEventRecord(c->ev[2], st));
+    CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
+    ++launches;
+    CU(cudaEventRecord(c->ev[3], st));
+    mwsep_launch_shape lk = sh;
+    lk.block = t.lk_block;
+    lk.grid = t.lk_grid;
+    lk.area_index = 0;
+    if (precision == MWSEP_PLAIN_F64)
+        CK(mwsep_launch_likelihood_f64(&c->stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                       c->d_lkpartials.as<double2>(), st));
+    else
+        CK(mwsep_launch_likelihood_f32(&c->stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                       c->d_lkpartials.as<double2>(), st));
+    ++launches;
+    CU(cudaEventRecord(c->ev[4], st));
+    CK(mwsep_launch_reduce_likelihood(c->d_lkpartials.as<double2>(), &lk, d_lk, st));
+    ++launches;
+    CU(cudaMemcpyAsync(c->h_out.p, c->d_out.p, out_doubles * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaEventRecord(c->ev[5], st));
+    CU(cudaStreamSynchronize(st));
+
+    float ms;
+    cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+    c->last_ms[0] = ms;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    c->last_ms[1] = ms;
+    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
+    c->last_ms[2] = ms;
+    cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+    c->last_ms[3] = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[5]);
+    c->last_ms[4] = ms;
+    c->last_launches = launches;
+
+    const double* h_areas = c->h_out.as<double>();
+    const double* h_ints = h_areas + (size_t)B * A * ncomp;
+    const double* h_lk = h_ints + (size_t)B * ncomp;
+    const double N = (double)c->n_stars;
+    for (int i = 0; i < B; ++i)
+    {
+        mwsep_result& r = out[i];
+        memset(&r, 0, sizeof(r));
+        r.number_streams = S;
+        r.number_integrals = A;
+        for (int a = 0; a < A; ++a)
+            for (int k = 0; k < ncomp; ++k) r.area_integrals[a][k] = h_areas[((size_t)i * A + a) * ncomp + k];
+        r.background_integral = h_ints[(size_t)i * ncomp];
+        for (int s = 0; s < S; ++s) r.stream_integrals[s] = h_ints[(size_t)i * ncomp + 1 + s];
+        const double* lkv = h_lk + (size_t)i * nslots;
+        r.prob_sum = lkv[0];
+        r.num_zero = (int)llround(lkv[1]);
+        /* cpu_evaluate returns prob_sum/(N - bad_jacobians) (:783); the app
+         * subtracts 3.0 (src/milkyway_client_app.c:278) */
+        r.likelihood = lkv[0] / N - 3.0;
+        r.background_only_likelihood = lkv[2] / N - 3.0;
+        for (int s = 0; s < S; ++s) r.stream_only_likelihood[s] = lkv[3 + s] / N - 3.0;
+        r.status = MWSEP_OK;
+    }
+    return MWSEP_OK;
+}
+
+} // namespace
+
+/* ------------------------------------------------------------ public API */
+
+extern "C" int mwsep_ctx_create(int device, mwsep_ctx** out)
+{
+    if (!out) return mwsep_fail(MWSEP_ERR_ARG);
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    {
+        cudaGetLastError();
+        return mwsep_fail(MWSEP_ERR_CUDA);
+    }
+    if (device < 0 || device >= ndev) return mwsep_fail(MWSEP_ERR_ARG);
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, device));
+    /* the kernels are built for sm_103a only */
+    if (prop.major != 10 || prop.minor != 3) return mwsep_fail(MWSEP_ERR_CUDA);
+    CU(cudaSetDevice(device));
+    mwsep_ctx* c = new (std::nothrow) mwsep_ctx();
+    if (!c) return mwsep_fail(MWSEP_ERR_NOMEM);
+    c->device = device;
+    c->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete c;
+        return mwsep_fail(MWSEP_ERR_CUDA);
+    }
+    for (int i = 0; i < 6; ++i)
+    {
+        if (cudaEventCreate(&c->ev[i]) != cudaSuccess)
+        {
+            mwsep_ctx_destroy(c);
+            return mwsep_fail(MWSEP_ERR_CUDA);
+        }
+    }
+    *out = c;
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
+{
+    if (!c) return mwsep_fail(MWSEP_ERR_ARG);
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    size_t& t = c->dev_bytes;
+    for (int a = 0; a < MWSEP_MAX_AREAS; ++a)
+    {
+        AreaDev& D = c->areas[a];
+        DevBuf* bufs[] = {&D.geom, &D.r_point, &D.qw, &D.r_in_mag, &D.r_in_mag2, &D.reff, &D.irv,
+                          &D.ids, &D.nus, &D.r_hi, &D.r_lo, &D.qwv, &D.gmag};
+        for (DevBuf* b : bufs) b->release(t);
+    }
+    DevBuf* bufs[] = {&c->d_dx, &c->d_glw, &c->s_l, &c->s_b, &c->s_r, &c->s_geom, &c->s_r_point, &c->s_qw,
+                      &c->s_r_in_mag, &c->s_r_in_mag2, &c->s_reff, &c->s_r_hi, &c->s_r_lo, &c->s_qwv,
+                      &c->s_gmag, &c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out};
+    for (DevBuf* b : bufs) b->release(t);
+    c->h_stars.release();
+    c->h_theta.release();
+    c->h_out.release();
+    for (int i = 0; i < 6; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_set_problem(mwsep_ctx* c, const ASTRONOMY_PARAMETERS* ap)
+{
+    if (!c || !ap) return mwsep_fail(MWSEP_ERR_ARG);
+    int rc = check_problem(ap);
+    if (rc) return mwsep_fail(rc);
+    CU(cudaSetDevice(c->device));
+    const int old_convolve = c->has_problem ? c->prob.convolve : -1;
+    copy_problem(ap, c->prob);
+    c->has_problem = false;
+    const int C = c->prob.convolve;
+    c->gl_x.assign(C, 0.0);
+    c->gl_w.assign(C, 0.0);
+    c->dx.assign(C, 0.0);
+    gauss_legendre(C, c->gl_x.data(), c->gl_w.data());
+    for (int i = 0; i < C; ++i) c->dx[i] = 3 * MW_STDEV * c->gl_x[i]; /* :131 */
+    c->coeff = 1 / (MW_STDEV * sqrt(2 * MW_PI));                     /* :84 */
+    if (c->d_dx.ensure((size_t)C * 8, c->dev_bytes) || c->d_glw.ensure((size_t)C * 8, c->dev_bytes))
+        return mwsep_fail(MWSEP_ERR_NOMEM);
+    CU(cudaMemcpyAsync(c->d_dx.p, c->dx.data(), (size_t)C * 8, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->d_glw.p, c->gl_w.data(), (size_t)C * 8, cudaMemcpyHostToDevice, c->stream));
+    for (int a = 0; a < c->prob.n_areas; ++a)
+    {
+        rc = build_area(c, a);
+        if (rc) return rc;
+    }
+    /* a catalogue built for another convolve count is stale */
+    if (old_convolve != C) c->has_stars = false;
+    c->has_problem = true;
+    default_tune(c);
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_set_stars_soa(mwsep_ctx* c, int n, const double* l, const double* b, const double* r)
+{
+    if (!c || !l || !b || !r) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    int rc = upload_stars(c, n, l, b, r);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_set_stars(mwsep_ctx* c, const STAR_POINTS* sp)
+{
+    if (!c || !sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    const int n = sp->number_stars;
+    if (c->h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
+    double* l = c->h_stars.as<double>();
+    double* b = l + n;
+    double* r = b + n;
+    for (int i = 0; i < n; ++i)
+    {
+        const double* row = sp->stars[i];
+        if (!row) return mwsep_fail(MWSEP_ERR_ARG);
+        l[i] = row[0];
+        b[i] = row[1];
+        r[i] = row[2];
+    }
+    int rc = upload_stars(c, n, l, b, r);
+    if (rc) return rc;
+    /* the pinned staging buffer is reused: wait for the copies */
+    CU(cudaStreamSynchronize(c->stream));
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_theta_count(const mwsep_ctx* c)
+{
+    if (!c || !c->has_problem) return -mwsep_fail(MWSEP_ERR_STATE);
+    return c->prob.n_theta;
+}
+
+extern "C" int mwsep_ctx_evaluate(mwsep_ctx* c, const double* theta, int precision, mwsep_result* out)
+{
+    if (!c) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    return evaluate_impl(c, 1, theta, precision, out);
+}
+
+extern "C" int mwsep_ctx_evaluate_batch(mwsep_ctx* c, int n_theta, const double* thetas, int precision,
+                                        mwsep_result* out)
+{
+    if (!c) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    return evaluate_impl(c, n_theta, thetas, precision, out);
+}
+
+extern "C" int mwsep_ctx_device_bytes(const mwsep_ctx* c, size_t* out)
+{
+    if (!c || !out) return mwsep_fail(MWSEP_ERR_ARG);
+    *out = c->dev_bytes;
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_last_timings(const mwsep_ctx* c, double* out5)
+{
+    if (!c || !out5) return mwsep_fail(MWSEP_ERR_ARG);
+    for (int i = 0; i < 5; ++i) out5[i] = c->last_ms[i];
+    return MWSEP_OK;
+}
+
+extern "C" int mwsep_ctx_last_launches(const mwsep_ctx* c, int* out)
+{
+    if (!c || !out) return mwsep_fail(MWSEP_ERR_ARG);
+    *out = c->last_launches;
+    return MWSEP_OK;
+}
+
+/* --------------------------------------------------------- EvalFunc path */
+
+namespace {
+
+std::mutex g_default_mu;
+mwsep_ctx* g_default = nullptr;
+
+double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp,
+                     int precision)
+{
+    const double nan = NAN;
+    if (!parameters || !ap || !es || !sp)
+    {
+        mwsep_fail(MWSEP_ERR_ARG);
+        return nan;
+    }
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if (!g_default)
+    {
+        int dev = 0;
+        if (const char* e = getenv("MWSEP_DEVICE")) dev = atoi(e);
+        if (mwsep_ctx_create(dev, &g_default) != MWSEP_OK) return nan;
+    }
+    /* cpu_evaluate: set_astronomy_parameters (:763), then integrals and
+     * likelihood. */
+    if (mwsep_set_astronomy_parameters(ap, parameters) != MWSEP_OK) return nan;
+    if (mwsep_ctx_set_problem(g_default, ap) != MWSEP_OK) return nan;
+    if (mwsep_ctx_set_stars(g_default, sp) != MWSEP_OK) return nan;
+    if (es->number_integrals != ap->number_integrals || es->number_streams != ap->number_streams || !es->integral)
+    {
+        mwsep_fail(MWSEP_ERR_STATE);
+        return nan;
+    }
+    mwsep_result r;
+    if (mwsep_ctx_evaluate(g_default, parameters, precision, &r) != MWSEP_OK) return nan;
+
+    const int S = ap->number_streams;
+    for (int a = 0; a < ap->number_integrals; ++a)
+    {
+        INTEGRAL_AREA* ia = es->integral[a];
+        ia->background_integral = r.area_integrals[a][0];
+        for (int s = 0; s < S; ++s) ia->stream_integrals[s] = r.area_integrals[a][1 + s];
+        ia->current_calculation = ia->max_calculation;
+    }
+    es->current_integral = ap->number_integrals;
+    es->background_integral = r.background_integral;
+    for (int s = 0; s < S; ++s) es->stream_integrals[s] = r.stream_integrals[s];
+    es->current_star_point = sp->number_stars;
+    es->total_stars = sp->number_stars;
+    es->num_zero = r.num_zero;
+    es->bad_jacobians = 0;
+    es->prob_sum = r.prob_sum;
+    return es->prob_sum / (sp->number_stars - es->bad_jacobians);
+}
+
+} // namespace
+
+extern "C" double mwsep_evaluate(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                                 STAR_POINTS* sp)
+{
+    return evalfunc_impl(parameters, ap, es, sp, MWSEP_PLAIN_F64);
+}
+
+extern "C" double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                                       STAR_POINTS* sp)
+{
+    return evalfunc_impl(parameters, ap, es, sp, MWSEP_MIXED_F32);
+}

@@ -1,0 +1,142 @@
+/* mwsep_internal.h -- shared between the host orchestration and the CUDA
+ * kernels of libmwsep_gb300.  Not part of the public ABI. */
+#ifndef MWSEP_INTERNAL_H
+#define MWSEP_INTERNAL_H
+
+#include <stdint.h>
+#include "milkyway_separation_gb300.h"
+
+#ifdef __CUDACC__
+#define MWSEP_HD __host__ __device__
+#else
+#define MWSEP_HD
+#endif
+
+/* include/milkyway.h:46-52 (pi is M_PI on glibc; deg = 180/pi) and the
+ * density-model constants of cpu/evaluation_optimized.c:41-46. */
+#define MW_PI 3.1415926535897932384626433832795028841971693993751
+#define MW_DEG (180.0 / MW_PI)
+#define MW_D2PI 6.2831853071795864769252867665590057683943387987502
+#define MW_STDEV 0.6
+#define MW_LBR_R 8.5
+#define MW_ABSM 4.2
+#define MW_SIG0 0.9402
+#define MW_SIG1 1.6171
+#define MW_SIG2 23.5877
+
+/* Kernels are specialised on an upper bound of the stream count. */
+#define MWSEP_KMAX_STREAMS 8
+
+/* Parameter-dependent constants of one evaluation, computed on the host in
+ * FP64 with the reference's formulas (init_constants,
+ * cpu/evaluation_optimized.c:54-133, and the weights of
+ * calculate_likelihood :639-646). */
+typedef struct
+{
+    double alpha, q, r0, delta;
+    double bg_a, bg_b, bg_c;
+    double alpha_delta3;
+    int n_streams;
+    int bg_mode;   /* 0: alpha=delta=1; 1: general pow branch; 2: q==0 */
+    int aux;       /* aux_bg_profile (0/1) */
+    int pad0;
+    double sigma_sq2[MWSEP_KMAX_STREAMS];
+    int stream_on[MWSEP_KMAX_STREAMS]; /* 0 when |sigma| < 1e-4 (:279-280) */
+    double a[MWSEP_KMAX_STREAMS][3];
+    double c[MWSEP_KMAX_STREAMS][3];
+    double exp_bg_weight;
+    double exp_stream_weight[MWSEP_KMAX_STREAMS];
+    double sum_exp_weights;           /* already * 0.001 */
+} mwsep_theta_consts;
+
+/* One integral area on the device. */
+typedef struct
+{
+    int mu_steps, nu_steps, r_steps, convolve;
+    int n_cols;          /* mu_steps * nu_steps */
+    int k_chunk;         /* r-bins per thread */
+    int n_kchunks;       /* ceil(r_steps / k_chunk) */
+    int pad0;
+    long long n_items;   /* n_cols * n_kchunks */
+    const double* geom;      /* [mu][nu] x 4: bsin, bcos, lsin, lcos */
+    const double* r_point;   /* [R][C] */
+    const double* qw;        /* [R][C]  qw_r3_N */
+    const double* r_in_mag;  /* [R][C] */
+    const double* r_in_mag2; /* [R][C] */
+    const double* reff;      /* [R] reff_xr_rp3 */
+    const double* irv;       /* [R] */
+    const double* ids;       /* [NU] */
+    /* compensated-FP32 tables */
+    const float* r_hi;       /* [R][C] */
+    const float* r_lo;       /* [R][C] */
+    const float* qwv;        /* [R][C]  qw * reff * irv, rounded once */
+    const float* gmag;       /* [R][C]  r_in_mag (aux only) */
+} mwsep_area_dev;
+
+/* A resident catalogue on the device (tables are [C][N], star-minor). */
+typedef struct
+{
+    int n_stars, convolve;
+    const double* geom;      /* [N] x 4: bsin, bcos, lsin, lcos */
+    const double* r_point;   /* [C][N] */
+    const double* qw;        /* [C][N] */
+    const double* r_in_mag;  /* [C][N] */
+    const double* r_in_mag2; /* [C][N] */
+    const double* reff;      /* [N] */
+    const float* r_hi;       /* [C][N] */
+    const float* r_lo;       /* [C][N] */
+    const float* qwv;        /* [C][N]  qw * reff */
+    const float* gmag;       /* [C][N] */
+} mwsep_stars_dev;
+
+/* Per-evaluation likelihood sums written by the reduction kernels:
+ * [0] sum of log10 p (prob_sum), [1] zero-probability count, [2] bg-only
+ * sum, [3..3+S) stream-only sums. */
+#define MWSEP_LK_SLOTS (3 + MWSEP_KMAX_STREAMS)
+
+/* Shape of one batched launch.  Partials are laid out
+ * [theta][area][grid][ncomp] for integrals (ncomp = 1+S) and
+ * [theta][grid][nslots] for the likelihood (nslots = 3+S). */
+typedef struct
+{
+    int n_theta;     /* gridDim.y */
+    int n_streams;   /* S, the same for every theta of a batch */
+    int n_areas;     /* integral areas of the problem */
+    int area_index;  /* which area this launch covers */
+    int block;       /* threads per block */
+    int grid;        /* blocks per theta (gridDim.x) */
+} mwsep_launch_shape;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* Launchers (defined in the .cu files).  All return cudaError_t as int. */
+int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps, const double* nus, int nu_steps,
+                          int sgr, int wedge, double* geom_out, void* stream);
+int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
+                             const double* dx, const double* gl_w, double coeff, double* geom,
+                             double* r_point, double* qw, double* r_in_mag, double* r_in_mag2,
+                             double* reff, float* r_hi, float* r_lo, float* qwv, float* gmag, void* stream);
+int mwsep_launch_integral_f64(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                              const mwsep_launch_shape* shape, double2* partials, void* stream);
+int mwsep_launch_likelihood_f64(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
+                                const mwsep_launch_shape* shape, const double* integrals,
+                                double2* partials, void* stream);
+int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                              const mwsep_launch_shape* shape, double2* partials, void* stream);
+int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
+                                const mwsep_launch_shape* shape, const double* integrals,
+                                double2* partials, void* stream);
+/* Reduce per-block compensated partials of every area into area integrals
+ * and subtract the cut areas (cpu/evaluation_optimized.c:584-593):
+ * out_areas [n_theta][n_areas][1+S], out_integrals [n_theta][1+S]. */
+int mwsep_launch_reduce_integrals(const double2* partials, const mwsep_launch_shape* shape,
+                                  double* out_areas, double* out_integrals, void* stream);
+/* Reduce likelihood partials into out [n_theta][3+S]. */
+int mwsep_launch_reduce_likelihood(const double2* partials, const mwsep_launch_shape* shape,
+                                   double* out, void* stream);
+#ifdef __cplusplus
+}
+#endif
+
+#endif

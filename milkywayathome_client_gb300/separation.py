@@ -1,0 +1,351 @@
+"""Python mirror of the reference separation client's evaluation interface.
+
+The call sequence reads like worker() in the reference
+(src/milkyway_client_app.c:197-288)::
+
+    ap = AstronomyParameters.read("astronomy_parameters.txt")   # read_astronomy_parameters
+    sp = StarPoints.read("stars.txt")                          # read_star_points
+    es = EvaluationState(ap, sp)                               # initialize_state
+    assert len(theta) == ap.optimized_parameter_count          # :244-259
+    likelihood = evaluate(theta, ap, es, sp) - 3.0             # :278
+
+``evaluate`` is the plain FP64 GPU evaluator (``mwsep_evaluate``, an
+EvalFunc); ``evaluate_mixed`` is the compensated-FP32 one.  ``Context``
+exposes the resident-data API for many evaluations of one wedge.
+
+Every compute call goes through libmwsep_gb300.so; there is no Python or CPU
+implementation of the likelihood here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import native as N
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class AstronomyParameters:
+    """An ASTRONOMY_PARAMETERS owned by the library (cpu/parameters.h:37-71)."""
+
+    def __init__(self):
+        self._s = N.ASTRONOMY_PARAMETERS()
+        self._owned = False
+
+    @classmethod
+    def read(cls, path: str) -> "AstronomyParameters":
+        ap = cls()
+        N.check(N.lib().mwsep_read_astronomy_parameters(str(path).encode(), C.byref(ap._s)),
+                f"reading {path}")
+        ap._owned = True
+        return ap
+
+    def write(self, path: str) -> None:
+        N.check(N.lib().mwsep_write_astronomy_parameters(str(path).encode(), C.byref(self._s)),
+                f"writing {path}")
+
+    def close(self) -> None:
+        if self._owned:
+            N.lib().mwsep_free_parameters(C.byref(self._s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def struct(self):
+        return self._s
+
+    @property
+    def optimized_parameter_count(self) -> int:
+        return N.lib().mwsep_get_optimized_parameter_count(C.byref(self._s))
+
+    @property
+    def number_streams(self) -> int:
+        return self._s.number_streams
+
+    @property
+    def number_integrals(self) -> int:
+        return self._s.number_integrals
+
+    @property
+    def convolve(self) -> int:
+        return self._s.convolve
+
+    def set_parameters(self, theta: Sequence[float]) -> None:
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        if t.size != self.optimized_parameter_count:
+            raise ValueError(f"theta has {t.size} values, {self.optimized_parameter_count} expected")
+        N.check(N.lib().mwsep_set_astronomy_parameters(C.byref(self._s), _dptr(t)))
+
+    def search_parameters(self) -> np.ndarray:
+        out = np.zeros(self.optimized_parameter_count)
+        N.check(N.lib().mwsep_get_search_parameters(C.byref(self._s), _dptr(out)))
+        return out
+
+    def split(self, rank: int, max_rank: int) -> None:
+        N.check(N.lib().mwsep_split_astronomy_parameters(C.byref(self._s), rank, max_rank))
+
+    def area(self, i: int) -> dict:
+        a = self._s.integral[i].contents
+        return {k: getattr(a, k) for k, _ in N.INTEGRAL._fields_}
+
+
+class StarPoints:
+    """A STAR_POINTS catalogue (cpu/star_points.h:27-31), rows (l, b, r_kpc)."""
+
+    def __init__(self):
+        self._s = N.STAR_POINTS()
+        self._owned = False
+        self._keep = None
+
+    @classmethod
+    def read(cls, path: str) -> "StarPoints":
+        sp = cls()
+        N.check(N.lib().mwsep_read_star_points(str(path).encode(), C.byref(sp._s)), f"reading {path}")
+        sp._owned = True
+        return sp
+
+    @classmethod
+    def from_array(cls, lbr: np.ndarray) -> "StarPoints":
+        """Wrap an (N, 3) array without copying rows into C allocations."""
+        a = np.ascontiguousarray(lbr, dtype=np.float64)
+        if a.ndim != 2 or a.shape[1] != 3:
+            raise ValueError("expected an (N, 3) array of l, b, r")
+        n = a.shape[0]
+        rows = (C.POINTER(C.c_double) * max(n, 1))()
+        base = a.ctypes.data
+        for i in range(n):
+            rows[i] = C.cast(base + 24 * i, C.POINTER(C.c_double))
+        sp = cls()
+        sp._s.number_stars = n
+        sp._s.stars = C.cast(rows, C.POINTER(C.POINTER(C.c_double)))
+        sp._keep = (a, rows)
+        return sp
+
+    def write(self, path: str) -> None:
+        N.check(N.lib().mwsep_write_star_points(str(path).encode(), C.byref(self._s)), f"writing {path}")
+
+    def to_array(self) -> np.ndarray:
+        n = self._s.number_stars
+        out = np.empty((n, 3))
+        for i in range(n):
+            row = self._s.stars[i]
+            out[i] = (row[0], row[1], row[2])
+        return out
+
+    def split(self, rank: int, max_rank: int) -> None:
+        """Keep this rank's slice (split_star_points, cpu/star_points.c:105-131)."""
+        if self._owned:
+            N.check(N.lib().mwsep_split_star_points(C.byref(self._s), rank, max_rank))
+            return
+        if rank == 0 and max_rank == 0:
+            return
+        n = self.number_stars
+        first = int(float(n) * (float(rank) / float(max_rank)))
+        last = int(float(n) * ((float(rank) + 1.0) / float(max_rank)))
+        other = StarPoints.from_array(self.to_array()[first:last])
+        self._s, self._keep = other._s, other._keep
+        other._keep = None
+
+    def close(self) -> None:
+        if self._owned:
+            N.lib().mwsep_free_star_points(C.byref(self._s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def struct(self):
+        return self._s
+
+    @property
+    def number_stars(self) -> int:
+        return self._s.number_stars
+
+
+class EvaluationState:
+    """An EVALUATION_STATE (cpu/evaluation_state.h:43-58)."""
+
+    def __init__(self, ap: AstronomyParameters, sp: StarPoints):
+        self._s = N.EVALUATION_STATE()
+        N.check(N.lib().mwsep_initialize_state(C.byref(ap.struct), C.byref(sp.struct), C.byref(self._s)))
+        self._owned = True
+
+    def close(self):
+        if self._owned:
+            N.lib().mwsep_free_state(C.byref(self._s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def struct(self):
+        return self._s
+
+    @property
+    def background_integral(self) -> float:
+        return self._s.background_integral
+
+    @property
+    def stream_integrals(self) -> List[float]:
+        return [self._s.stream_integrals[i] for i in range(self._s.number_streams)]
+
+    @property
+    def area_integrals(self) -> List[List[float]]:
+        out = []
+        for a in range(self._s.number_integrals):
+            ia = self._s.integral[a].contents
+            out.append([ia.background_integral] + [ia.stream_integrals[i] for i in range(ia.number_streams)])
+        return out
+
+    @property
+    def prob_sum(self) -> float:
+        return self._s.prob_sum
+
+    @property
+    def num_zero(self) -> int:
+        return self._s.num_zero
+
+
+def _evalfunc(fn, theta, ap, es, sp) -> float:
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    if t.size != ap.optimized_parameter_count:
+        raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "evaluate")
+    v = fn(_dptr(t), C.byref(ap.struct), C.byref(es.struct), C.byref(sp.struct))
+    if v != v:  # NaN: the library recorded why
+        raise N.MwsepError(N.lib().mwsep_last_error(), "evaluate")
+    return v
+
+
+def evaluate(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> float:
+    """Plain FP64 GPU evaluation; returns prob_sum/N like cpu_evaluate
+    (cpu/evaluation_optimized.c:756-784).  Subtract 3.0 for the likelihood."""
+    return _evalfunc(N.lib().mwsep_evaluate, theta, ap, es, sp)
+
+
+def evaluate_mixed(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> float:
+    """Compensated-FP32 GPU evaluation with the same contract as evaluate."""
+    return _evalfunc(N.lib().mwsep_evaluate_mixed, theta, ap, es, sp)
+
+
+@dataclass
+class Result:
+    likelihood: float
+    prob_sum: float
+    num_zero: int
+    background_integral: float
+    stream_integrals: List[float]
+    area_integrals: List[List[float]]
+    background_only_likelihood: float
+    stream_only_likelihood: List[float]
+
+    @classmethod
+    def from_c(cls, r: N.mwsep_result) -> "Result":
+        S, A = r.number_streams, r.number_integrals
+        return cls(
+            likelihood=r.likelihood, prob_sum=r.prob_sum, num_zero=r.num_zero,
+            background_integral=r.background_integral,
+            stream_integrals=[r.stream_integrals[i] for i in range(S)],
+            area_integrals=[[r.area_integrals[a][k] for k in range(1 + S)] for a in range(A)],
+            background_only_likelihood=r.background_only_likelihood,
+            stream_only_likelihood=[r.stream_only_likelihood[i] for i in range(S)],
+        )
+
+    @property
+    def integrals(self) -> List[float]:
+        return [self.background_integral] + list(self.stream_integrals)
+
+
+class Context:
+    """A device context with a resident wedge and catalogue (mwsep_ctx_*)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        N.check(N.lib().mwsep_ctx_create(device, C.byref(self._h)), "mwsep_ctx_create")
+
+    def close(self):
+        if self._h:
+            N.lib().mwsep_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_problem(self, ap: AstronomyParameters) -> None:
+        N.check(N.lib().mwsep_ctx_set_problem(self._h, C.byref(ap.struct)), "set_problem")
+
+    def set_stars(self, sp) -> None:
+        if isinstance(sp, StarPoints):
+            N.check(N.lib().mwsep_ctx_set_stars(self._h, C.byref(sp.struct)), "set_stars")
+        else:
+            a = np.asarray(sp, dtype=np.float64)
+            l = np.ascontiguousarray(a[:, 0])
+            b = np.ascontiguousarray(a[:, 1])
+            r = np.ascontiguousarray(a[:, 2])
+            N.check(N.lib().mwsep_ctx_set_stars_soa(self._h, a.shape[0], _dptr(l), _dptr(b), _dptr(r)),
+                    "set_stars")
+
+    @property
+    def theta_count(self) -> int:
+        return N.lib().mwsep_ctx_theta_count(self._h)
+
+    def evaluate(self, theta, precision: int = N.MWSEP_PLAIN_F64) -> Result:
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        if t.size != self.theta_count:
+            raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "evaluate")
+        r = N.mwsep_result()
+        N.check(N.lib().mwsep_ctx_evaluate(self._h, _dptr(t), precision, C.byref(r)), "evaluate")
+        return Result.from_c(r)
+
+    def evaluate_batch(self, thetas, precision: int = N.MWSEP_PLAIN_F64) -> List[Result]:
+        t = np.ascontiguousarray(thetas, dtype=np.float64)
+        if t.ndim != 2 or t.shape[1] != self.theta_count:
+            raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "evaluate_batch")
+        out = (N.mwsep_result * t.shape[0])()
+        N.check(N.lib().mwsep_ctx_evaluate_batch(self._h, t.shape[0], _dptr(t), precision, out),
+                "evaluate_batch")
+        return [Result.from_c(out[i]) for i in range(t.shape[0])]
+
+    @property
+    def device_bytes(self) -> int:
+        v = C.c_size_t()
+        N.check(N.lib().mwsep_ctx_device_bytes(self._h, C.byref(v)))
+        return v.value
+
+    def last_timings(self) -> dict:
+        a = (C.c_double * 5)()
+        N.check(N.lib().mwsep_ctx_last_timings(self._h, a))
+        return {"integral_ms": a[0], "integral_reduce_ms": a[1], "likelihood_ms": a[2],
+                "likelihood_reduce_ms": a[3], "total_ms": a[4]}
+
+    def last_launches(self) -> int:
+        v = C.c_int()
+        N.check(N.lib().mwsep_ctx_last_launches(self._h, C.byref(v)))
+        return v.value

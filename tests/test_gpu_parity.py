@@ -1,0 +1,126 @@
+"""GPU parity: the CUDA path against the reference's own outputs (golden
+fixtures made by the reference CPU evaluator, tests/golden/make_golden.py) and
+against the oracle restatement run live.
+
+Tolerances (plain FP64 form): 1e-12 relative on every integral, 1e-12
+absolute on the log-likelihood.  Compensated-FP32 form: 1e-7 absolute on the
+log-likelihood.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_case
+
+pytestmark = pytest.mark.gpu
+
+REL_INT_F64 = 1e-12
+ABS_LOGL_F64 = 1e-12
+ABS_LOGL_F32 = 1e-7
+
+
+def _close_rel(a, b, tol):
+    if math.isnan(a) or math.isnan(b):
+        return math.isnan(a) and math.isnan(b)
+    if b == 0.0:
+        return a == 0.0
+    return abs(a - b) <= tol * abs(b)
+
+
+def _close_abs(a, b, tol):
+    if math.isnan(a) or math.isnan(b):
+        return math.isnan(a) and math.isnan(b)
+    return abs(a - b) <= tol
+
+
+def _setup(ctx, name):
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    ap = mw.AstronomyParameters.read(pf)
+    sp = mw.StarPoints.read(sf)
+    ctx.set_problem(ap)
+    ctx.set_stars(sp)
+    return ap, sp, g
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_plain_f64_matches_reference(gpu_ctx, name):
+    import milkywayathome_client_gb300 as mw
+    _, _, g = _setup(gpu_ctx, name)
+    r = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+    for a, (got_area, want_area) in enumerate(zip(r.area_integrals, g["area_integrals"])):
+        for k, (x, y) in enumerate(zip(got_area, want_area)):
+            assert _close_rel(x, y, REL_INT_F64), f"area {a} comp {k}: {x!r} vs {y!r}"
+    assert _close_rel(r.background_integral, g["background_integral"], REL_INT_F64)
+    for x, y in zip(r.stream_integrals, g["stream_integrals"]):
+        assert _close_rel(x, y, REL_INT_F64), (x, y)
+    assert _close_abs(r.likelihood, g["likelihood"], ABS_LOGL_F64), (r.likelihood, g["likelihood"])
+    assert r.num_zero == g["num_zero"]
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_mixed_f32_within_1e7(gpu_ctx, name):
+    import milkywayathome_client_gb300 as mw
+    _, _, g = _setup(gpu_ctx, name)
+    r = gpu_ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32)
+    assert _close_abs(r.likelihood, g["likelihood"], ABS_LOGL_F32), (r.likelihood, g["likelihood"])
+    assert r.num_zero == g["num_zero"]
+
+
+@pytest.mark.parametrize("name", ["basic_1stream", "cut_area", "three_streams"])
+def test_evalfunc_dropin(built_library, name):
+    """The EvalFunc entry fills EVALUATION_STATE like cpu_evaluate."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    ap = mw.AstronomyParameters.read(pf)
+    sp = mw.StarPoints.read(sf)
+    es = mw.EvaluationState(ap, sp)
+    v = mw.evaluate(g["theta"], ap, es, sp)
+    assert _close_abs(v - 3.0, g["likelihood"], ABS_LOGL_F64)
+    assert _close_rel(es.background_integral, g["background_integral"], REL_INT_F64)
+    for x, y in zip(es.stream_integrals, g["stream_integrals"]):
+        assert _close_rel(x, y, REL_INT_F64)
+    for got_area, want_area in zip(es.area_integrals, g["area_integrals"]):
+        for x, y in zip(got_area, want_area):
+            assert _close_rel(x, y, REL_INT_F64)
+    assert _close_rel(es.prob_sum, g["prob_sum"], 1e-12)
+    # theta was applied to the struct, as set_astronomy_parameters does
+    np.testing.assert_array_equal(ap.search_parameters(), np.asarray(g["theta"]))
+    vm = mw.evaluate_mixed(g["theta"], ap, es, sp)
+    assert abs((vm - 3.0) - g["likelihood"]) <= ABS_LOGL_F32
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_equals_single_bitwise(gpu_ctx, precision):
+    """Each result of a batch is bit-identical to the same theta alone."""
+    _, _, g = _setup(gpu_ctx, "three_streams")
+    base = np.asarray(g["theta"])
+    rng = np.random.default_rng(3)
+    thetas = base + rng.normal(0, 0.01, size=(5, base.size)) * np.abs(base)
+    batch = gpu_ctx.evaluate_batch(thetas, precision)
+    for t, b in zip(thetas, batch):
+        s = gpu_ctx.evaluate(t, precision)
+        assert s.likelihood == b.likelihood
+        assert s.integrals == b.integrals
+
+
+def test_repeatable_bitwise(gpu_ctx):
+    _, _, g = _setup(gpu_ctx, "config0")
+    a = gpu_ctx.evaluate(g["theta"], 0)
+    b = gpu_ctx.evaluate(g["theta"], 0)
+    assert a.likelihood == b.likelihood and a.integrals == b.integrals
+
+
+@pytest.mark.parametrize("name", ["basic_1stream", "general_alpha_delta", "sgr_coordinates"])
+def test_against_live_oracle(gpu_ctx, oracle_built, name):
+    """Also compare with the oracle restatement (diagnostics included)."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    want = oracle_built.Oracle(pf, sf).evaluate(g["theta"])
+    _setup(gpu_ctx, name)
+    r = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+    assert _close_abs(r.likelihood, want["likelihood"], ABS_LOGL_F64)
+    assert _close_abs(r.background_only_likelihood, want["background_only_likelihood"], 1e-12)
+    for x, y in zip(r.stream_only_likelihood, want["stream_only_likelihood"]):
+        assert _close_abs(x, y, 1e-12)
