@@ -1,0 +1,89 @@
+"""The C-ABI library: it loads, it exports every function the header
+declares, its struct layouts match the header (and the reference's), and
+without an sm_103 GPU it fails loudly instead of falling back."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "milkyway_separation_gb300.h")
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mwsep_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function(built_library):
+    lib = ctypes.CDLL(built_library)
+    names = _declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(built_library):
+    from milkywayathome_client_gb300 import native
+    assert set(_declared_functions()) <= set(native.exported_symbols())
+
+
+def test_struct_layouts_match_c(tmp_path, built_library):
+    """sizeof/offsetof from a C compiler vs the ctypes mirror."""
+    from milkywayathome_client_gb300 import native as N
+    structs = {
+        "INTEGRAL": N.INTEGRAL, "ASTRONOMY_PARAMETERS": N.ASTRONOMY_PARAMETERS, "STAR_POINTS": N.STAR_POINTS,
+        "INTEGRAL_AREA": N.INTEGRAL_AREA, "EVALUATION_STATE": N.EVALUATION_STATE, "mwsep_result": N.mwsep_result,
+    }
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.split("\n") if l)
+    for cname, py in structs.items():
+        assert int(out[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(out[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"
+
+
+def test_header_compiles_after_reference_headers(tmp_path):
+    """The reference's own headers and this header can share a translation
+    unit: the structs are guarded by the reference include guards."""
+    ref = os.environ.get("MW_REFERENCE_DIR", "/root/reference")
+    cpu = os.path.join(ref, "milkyway_separation", "cpu")
+    if not os.path.isdir(cpu):
+        pytest.skip("reference sources not present")
+    src = tmp_path / "both.c"
+    src.write_text(f'#include "parameters.h"\n#include "star_points.h"\n#include "evaluation_state.h"\n'
+                   f'#include "simple_evaluator.h"\n#include "{HEADER}"\n'
+                   "EvalFunc f = mwsep_evaluate;\nint main(void){return f == 0;}\n")
+    subprocess.run(["gcc", "-std=gnu99", "-c", "-o", str(tmp_path / "both.o"), "-I", cpu, str(src)], check=True)
+
+
+def _has_sm103():
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=compute_cap", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30)
+        return out.returncode == 0 and "10.3" in out.stdout
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_sm103(), reason="a GB300 is present; this checks the no-GPU behaviour")
+def test_no_gpu_fails_loudly(built_library):
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    with pytest.raises(mw.MwsepError) as e:
+        mw.Context(0)
+    assert e.value.status == N.MWSEP_ERR_CUDA

@@ -1,0 +1,122 @@
+"""The oracle is pinned before it is trusted.
+
+* The C restatement (oracle/sep_oracle.c) against the golden values that the
+  reference's own CPU evaluator produced (tests/golden/cases/*/golden.json).
+* The restatement against the reference compiled from its sources, on the
+  reference's own test fixtures (only where the reference sources exist).
+* Known-answer checks taken from the reference code.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REFERENCE_DIR, golden_cases, load_case
+
+REL = 1e-14  # the restatement reproduces the reference's doubles; allow a few ulp across libm builds
+
+
+def _eq(a, b, rel=REL):
+    if math.isnan(a) or math.isnan(b):
+        return math.isnan(a) and math.isnan(b)
+    return a == b or abs(a - b) <= rel * abs(b)
+
+
+@pytest.mark.parametrize("name", [n for n in golden_cases() if n != "config0"])
+def test_restatement_matches_reference_goldens(oracle_built, name):
+    pf, sf, g = load_case(name)
+    o = oracle_built.Oracle(pf, sf)
+    r = o.evaluate(g["theta"])
+    for got, want in zip(r["area_integrals"], g["area_integrals"]):
+        for x, y in zip(got, want):
+            assert _eq(x, y), (x, y)
+    assert _eq(r["background_integral"], g["background_integral"])
+    for x, y in zip(r["stream_integrals"], g["stream_integrals"]):
+        assert _eq(x, y)
+    assert _eq(r["prob_sum"], g["prob_sum"], 1e-13)
+    assert _eq(r["likelihood"], g["likelihood"], 1e-13)
+    assert r["num_zero"] == g["num_zero"]
+
+
+def test_restatement_config0(oracle_built):
+    pf, sf, g = load_case("config0")
+    r = oracle_built.Oracle(pf, sf).evaluate(g["theta"])
+    assert _eq(r["likelihood"], g["likelihood"], 1e-13)
+    assert _eq(r["background_integral"], g["background_integral"])
+
+
+REF_FIXTURES = os.path.join(GOLDEN, "reference_fixtures.json")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE_DIR, "tests")),
+                    reason="reference test fixtures not present")
+@pytest.mark.parametrize("case", ["79", "86", "11", "12"])
+def test_restatement_on_reference_fixtures(oracle_built, case):
+    """The reference's own small test fixtures, with the theta vectors of its
+    tests/CMakeLists.txt, against the reference compiled from source."""
+    with open(REF_FIXTURES) as f:
+        want = json.load(f)[case]
+    pf = os.path.join(REFERENCE_DIR, want["params_file"])
+    sf = os.path.join(REFERENCE_DIR, want["stars_file"])
+    r = oracle_built.Oracle(pf, sf).evaluate(want["theta"])
+    assert _eq(r["background_integral"], want["background_integral"])
+    for x, y in zip(r["stream_integrals"], want["stream_integrals"]):
+        assert _eq(x, y)
+    assert _eq(r["likelihood"], want["likelihood"], 1e-13)
+
+
+def test_reference_fixture_values_match_published_survey_numbers():
+    """The recorded reference outputs equal the values measured when the
+    reference was first compiled (I_bg, I_s, logL of the -small fixtures)."""
+    with open(REF_FIXTURES) as f:
+        d = json.load(f)
+    assert abs(d["79"]["background_integral"] - 7.9416894656949719913e-05) < 1e-19
+    assert abs(d["79"]["likelihood"] - (-2.94673379590026485175)) < 1e-14
+    assert abs(d["86"]["stream_integrals"][0] - 374.13823192303391352) < 1e-11
+    assert abs(d["11"]["likelihood"] - (-3.12509788380322994783)) < 1e-14
+    assert abs(d["12"]["stream_integrals"][1] - 693.31476977139573137) < 1e-11
+
+
+def test_gauss_legendre_known_answers(oracle_built):
+    # The reference stops Newton at |dz| <= 3e-11 (include/milkyway.h:54), so
+    # its weights are good to ~1e-10, not to the last ulp.
+    for n in (1, 2, 7, 30, 120):
+        x, w = oracle_built.Oracle.gauss_legendre(n)
+        assert abs(w.sum() - 2.0) < 1e-9
+        np.testing.assert_allclose(x, -x[::-1], atol=1e-15)
+        # exact for polynomials of degree 2n-1
+        for k in range(0, 2 * n, 2):
+            assert abs(np.sum(w * x ** k) - 2.0 / (k + 1)) < 1e-9
+
+
+def test_lbr2xyz_matches_zp_form(oracle_built):
+    """stCoords.c:43-47 (law of cosines) agrees with the per-point form
+    x = zp cos l - 8.5 of evaluation_optimized.c:224-227."""
+    for l, b, r in [(10.0, 20.0, 5.0), (200.0, -45.0, 30.0), (359.0, 60.0, 2.5)]:
+        xyz = oracle_built.Oracle.lbr_to_xyz(l, b, r)
+        zp = r * math.cos(math.radians(b))
+        np.testing.assert_allclose(xyz, [zp * math.cos(math.radians(l)) - 8.5, zp * math.sin(math.radians(l)),
+                                         r * math.sin(math.radians(b))], rtol=1e-12, atol=1e-12)
+
+
+def test_survey_transform_matches_generator(oracle_built):
+    """The oracle's gc->(l,b) (atGCToEq + atEqToGal) and the workload
+    generator's vectorised transform agree."""
+    from milkywayathome_client_gb300 import synthetic as syn
+    for wedge in (11, 79, 82, 86):
+        for mu, nu in [(310.0, 0.0), (330.5, -1.1), (150.0, 1.2)]:
+            l, b = oracle_built.Oracle.gc_to_lb(wedge, mu, nu)
+            L, B = syn.gc_to_lb(wedge, mu, nu)
+            assert abs(l - float(L)) < 1e-9 and abs(b - float(B)) < 1e-9
+
+
+def test_slicing_composes_like_integral_compose(oracle_built):
+    """Rank slices of the linearised cell index (parameters.c:502-522) sum
+    to the whole integral (astronomy_worker.c:67-99)."""
+    pf, sf, g = load_case("three_streams")
+    o = oracle_built.Oracle(pf, sf)
+    whole, _ = o.integrals(g["theta"])
+    parts = sum(o.integrals(g["theta"], rank=r, nranks=3)[0] for r in range(3))
+    np.testing.assert_allclose(parts, whole, rtol=1e-13)
