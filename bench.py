@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Separation-likelihood throughput on GB300: evaluations per second.
+
+Workload: the full-size single evaluation (1600 x 640 x 140 cells, 120
+convolution points, 3 streams, 100k stars; seeded synthetic wedge, see
+milkywayathome_client_gb300/synthetic.py).  A step is one evaluation
+(integrals over every cell + likelihood over every star).
+
+  value      evaluations/s in the compensated-FP32 form with the wedge and
+             catalogue resident in HBM (device time from CUDA events on the
+             library's stream; L2 flushed between steps)
+  plain_f64  the same for the plain FP64 drop-in form
+  e2e        evaluations/s through the reference-facing EvalFunc C-ABI call
+             (mwsep_evaluate_mixed) with host structs: every step uploads the
+             catalogue, rebuilds the wedge and star tables, evaluates and
+             reads the result back
+  roofline   the dominant kernel (compensated integral) against the SFU
+             throughput measured by the library's own pipe microbenchmark
+  cpu_baseline  the reference CPU evaluator (or its C restatement where the
+             reference is not compiled on this host) on a bounded slice of
+             the same evaluation, all host cores
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "evals/s mixed-FP32 vs plain FP64 at |dlogL|<=1e-7"
+CONFIG_INDEX = 1
+CPU_SLICES = 400  # the CPU baseline evaluates 1/400-slices of the workload
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--data-dir", default=os.path.join(tempfile.gettempdir(), "mwsep_bench_data"))
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(ws, x):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_desc(files):
+    f = files[0]
+    p = f["problem"]
+    a = p.areas[0]
+    return {"workload": f"separation likelihood, one evaluation: {a.mu[2]}x{a.nu[2]}x{a.r[2]} (mu x nu x r) "
+                        f"cells, convolve {p.convolve}, {len(p.streams)} streams, {f['n_stars']} stars",
+            "mu_steps": a.mu[2], "nu_steps": a.nu[2], "r_steps": a.r[2], "convolve": p.convolve,
+            "streams": len(p.streams), "stars": f["n_stars"], "wedge": p.wedge}
+
+
+def points_per_eval(files):
+    f = files[0]
+    p = f["problem"]
+    cells = p.cells()
+    return cells * p.convolve, f["n_stars"] * p.convolve
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.fh = open(self.path, "w")
+        self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                      "-lms", "200", "-i", str(self.device)], stdout=self.fh,
+                                     stderr=subprocess.DEVNULL)
+        time.sleep(0.3)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                mx = float(parts[2].split()[0])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_sample(files, theta, n_procs, slices=CPU_SLICES):
+    """Run n_procs concurrent slices (ranks 0..n_procs-1 of `slices`) of the
+    evaluation on the host and return (wall seconds, kind, binary)."""
+    from oracle import oracle as orc
+    ref_bin, port_bin = orc.REF_BIN, orc.ORACLE_BIN
+    kind, binary = None, None
+    f = files[0]
+    args_theta = [repr(float(x)) for x in theta]
+    for k, b in (("reference", ref_bin), ("port", port_bin)):
+        if os.path.exists(b):
+            try:
+                r = subprocess.run([b, "-a", f["params"], "-p", f["stars"], "-r", "0", "-n", "100000",
+                                    *args_theta], capture_output=True, timeout=60)
+                if r.returncode == 0:
+                    kind, binary = k, b
+                    break
+            except OSError:
+                continue
+    if binary is None:
+        orc.build(reference=False)
+        kind, binary = "port", port_bin
+    t0 = time.perf_counter()
+    procs = [subprocess.Popen([binary, "-a", f["params"], "-p", f["stars"], "-r", str(r), "-n", str(slices),
+                               *args_theta], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+             for r in range(n_procs)]
+    rcs = [p.wait() for p in procs]
+    wall = time.perf_counter() - t0
+    if any(rcs):
+        raise RuntimeError(f"CPU baseline slices failed: {rcs}")
+    return wall, kind, binary
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference_arm(args, ws, rank):
+    """--impl reference: the reference's CPU evaluator on the host cores."""
+    if rank != 0:
+        return
+    from milkywayathome_client_gb300 import synthetic as syn
+    files = syn.materialise(CONFIG_INDEX, os.path.join(args.data_dir, "rank0"))["files"]
+    theta = files[0]["theta"]
+    n = min(host_cores(), 64)
+    times = []
+    kind = "port"
+    for i in range(args.warmup + args.steps):
+        wall, kind, _ = cpu_sample(files, theta, n)
+        if i >= args.warmup:
+            times.append(wall)
+    t = sum(times) / len(times)
+    value = (n / CPU_SLICES) / t
+    sample = (f"{n} concurrent processes, each 1/{CPU_SLICES} of the evaluation (the reference's own "
+              f"rank slicing of cells and stars), per step")
+    cpu = {"value": value, "unit": "evals/s", "cores": n, "kind": kind, "sample": sample}
+    out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": workload_desc(files), "cpu_baseline": cpu,
+           "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def traffic_from_profiles(kernel_key):
+    """dram bytes per launch recorded from an ncu capture (profiles/)."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_key and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gb300_arm(args, ws, rank, local):
+    import ctypes as C
+    import torch
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    from milkywayathome_client_gb300 import synthetic as syn
+
+    N.lib(build_if_missing=True)
+    device = local
+    torch.cuda.set_device(device)
+    files = syn.materialise(CONFIG_INDEX, os.path.join(args.data_dir, f"rank{rank}"))["files"]
+    f = files[0]
+    theta = f["theta"]
+    S = len(f["problem"].streams)
+    ap = mw.AstronomyParameters.read(f["params"])
+    sp = mw.StarPoints.read(f["stars"])
+    ctx = mw.Context(device)
+    ctx.set_problem(ap)
+    ctx.set_stars(sp)
+
+    peaks = N.mwsep_pipe_peaks()
+    N.check(N.lib().mwsep_measure_pipe_peaks(device, C.byref(peaks)), "pipe microbenchmark")
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{device}")
+
+    def step(precision):
+        flush.zero_()
+        torch.cuda.synchronize(device)
+        r = ctx.evaluate(theta, precision)
+        t = ctx.last_timings()
+        return r, t, ctx.last_launches()
+
+    # compensated FP32: warm-up then K timed steps
+    for _ in range(max(args.warmup, 3)):
+        step(N.MWSEP_MIXED_F32)
+    clocks = ClockSampler(device)
+    barrier(ws)
+    torch.cuda.synchronize(device)
+    clocks.start()
+    dev_ms, integ_ms, launches = [], [], 0
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        r32, t, nl = step(N.MWSEP_MIXED_F32)
+        dev_ms.append(t["total_ms"])
+        integ_ms.append(t["integral_ms"])
+        launches += nl
+    torch.cuda.synchronize(device)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    barrier(ws)
+    total_ms = allreduce_max(ws, sum(dev_ms))
+    ms_per_step = total_ms / args.steps
+    value = ws * args.steps / (total_ms * 1e-3)
+
+    # plain FP64 (the drop-in form) for the headline comparison
+    step(N.MWSEP_PLAIN_F64)
+    f64_ms = []
+    for _ in range(args.plain_steps):
+        r64, t, _ = step(N.MWSEP_PLAIN_F64)
+        f64_ms.append(t["total_ms"])
+    f64_ms_step = allreduce_max(ws, sum(f64_ms)) / args.plain_steps
+    plain_value = ws / (f64_ms_step * 1e-3)
+
+    # e2e through the EvalFunc C ABI with host buffers
+    es = mw.EvaluationState(ap, sp)
+    mw.evaluate_mixed(theta, ap, es, sp)  # warm-up (creates the library's default context)
+    e2e_t = []
+    h2d = C.c_size_t()
+    d2h = C.c_size_t()
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        v = mw.evaluate_mixed(theta, ap, es, sp)
+        e2e_t.append(time.perf_counter() - t0)
+    N.lib().mwsep_evalfunc_transfer_bytes(C.byref(h2d), C.byref(d2h))
+    e2e_step = allreduce_max(ws, sum(e2e_t)) / args.e2e_steps
+    e2e_value = ws / e2e_step
+    e2e_logl = v - 3.0
+
+    # roofline of the dominant kernel (the compensated integral)
+    cell_pts, star_pts = points_per_eval(files)
+    mufu_per_point = 2 + S  # rsqrt + rcp for the halo, one ex2 per stream
+    integ_s = statistics.median(integ_ms) * 1e-3
+    achieved = cell_pts * mufu_per_point / integ_s / 1e9
+    # peak for this op mix: the SFU time of one point at the measured rates
+    peak = mufu_per_point / (1.0 / peaks.rsqrt_gops + 1.0 / peaks.rcp_gops + S / peaks.ex2_gops)
+    traffic = traffic_from_profiles("integral_f32_config1")
+    roofline = {"bound": "sfu", "achieved": achieved, "peak": peak, "unit": "Gop/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "integral_f32_kernel",
+                "peak_source": "measured (project pipe microbenchmark, mwsep_measure_pipe_peaks): "
+                               "rsqrt, rcp and ex2 rates weighted by this kernel's op mix",
+                "work_per_point": f"{mufu_per_point} SFU ops (rsqrt, rcp, {S} ex2)",
+                "points_per_launch": cell_pts}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": dict(workload_desc(files), l2="flushed between steps (256 MB write)",
+                       parallelism="replicas" if ws > 1 else "single GPU"),
+        "impl": "gb300",
+        "plain_f64": {"value": plain_value, "unit": "evals/s", "ms_per_step": f64_ms_step, "dtype": "f64"},
+        "speedup_mixed_vs_plain": value / plain_value,
+        "dlogL_mixed_vs_plain": r32.likelihood - r64.likelihood,
+        "integral_rel_err_mixed_vs_plain": [(a - b) / b if b else 0.0 for a, b in zip(r32.integrals,
+                                                                                    r64.integrals)],
+        "likelihood": {"plain_f64": r64.likelihood, "mixed_f32": r32.likelihood, "e2e_mixed": e2e_logl},
+        "points_per_s": {"integral": ws * cell_pts / (ms_per_step * 1e-3),
+                         "likelihood": ws * star_pts / (ms_per_step * 1e-3)},
+        "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d.value,
+                "d2h_bytes_per_step": d2h.value, "api": "mwsep_evaluate_mixed (EvalFunc, host structs)"},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "pipe_peaks": {"fp64_tflops": peaks.fp64_fma_tflops, "fp32_tflops": peaks.fp32_fma_tflops,
+                       "ex2_gops": peaks.ex2_gops, "rsqrt_gops": peaks.rsqrt_gops, "rcp_gops": peaks.rcp_gops},
+        "wall_s_timed": wall,
+    }
+    if clk:
+        out["clocks"] = clk
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        n = min(host_cores(), 64)
+        cw, kind, _ = cpu_sample(files, theta, n)
+        cv = (n / CPU_SLICES) / cw
+        out["cpu_baseline"] = {"value": cv, "unit": "evals/s", "cores": n, "kind": kind,
+                               "sample": f"{n} concurrent 1/{CPU_SLICES} slices of the evaluation "
+                                         f"(reference rank slicing of cells and stars), {cw:.1f} s wall"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+    else:
+        run_gb300_arm(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

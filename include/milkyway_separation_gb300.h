@@ -302,6 +302,33 @@ int mwsep_ctx_last_timings(const mwsep_ctx* ctx, double* out5);
 /* Number of kernel launches issued by the last evaluate/evaluate_batch. */
 int mwsep_ctx_last_launches(const mwsep_ctx* ctx, int* out);
 
+/* Bytes the context has copied host->device and device->host since it was
+ * created (tables, catalogue, constants, results). */
+int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);
+
+/* Bytes copied host->device and device->host by the most recent
+ * mwsep_evaluate / mwsep_evaluate_mixed call on this process. */
+int mwsep_evalfunc_transfer_bytes(size_t* h2d, size_t* d2h);
+
+/* ------------------------------------------------------------------ */
+/* Pipe microbenchmark                                                  */
+/* ------------------------------------------------------------------ */
+
+/* Measured arithmetic-pipe throughput of one GPU: the denominators of the
+ * kernels' roofline fractions (the plain form is bound by the FP64 pipe,
+ * the compensated form by the FP32 pipe and the SFU). */
+typedef struct
+{
+    double fp64_fma_tflops;  /* 2 flops per DFMA */
+    double fp32_fma_tflops;  /* 2 flops per FFMA */
+    double ex2_gops;         /* ex2.approx.f32 per second, 1e9 */
+    double rsqrt_gops;       /* rsqrt.approx.f32 */
+    double rcp_gops;         /* rcp.approx.f32 */
+    int sm_count;
+} mwsep_pipe_peaks;
+
+int mwsep_measure_pipe_peaks(int device, mwsep_pipe_peaks* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,7 @@ UNITS = [
     ("mwsep_f64.cu", ["-fmad=false"]),
     ("mwsep_reduce.cu", ["-fmad=false"]),
     ("mwsep_f32.cu", ["-fmad=true"]),
+    ("mwsep_peaks.cu", ["-fmad=true"]),
     ("mwsep_io.cpp", []),
 ]
 
@@ -54,9 +55,9 @@ def _sources_newer_than(target: str) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(unit, extra, verbose):
+def _compile(unit, extra, verbose, build_dir=BUILD_DIR):
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD_DIR, unit + ".o")
+    obj = os.path.join(build_dir, unit + ".o")
     cmd = [nvcc(), "-c", src, "-o", obj, "-std=c++17", "-O3", "-lineinfo", *ARCH,
            "-I" + INCLUDE, "-I" + CSRC, "-Xcompiler", ",".join(HOST_FLAGS), *extra]
     if unit.endswith(".cpp"):
@@ -71,23 +72,27 @@ def _compile(unit, extra, verbose):
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every translation unit and link the shared library."""
-    if not force and not _sources_newer_than(LIB_PATH):
-        return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    os.makedirs(LIB_DIR, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: str = LIB_PATH,
+          build_dir: str = BUILD_DIR) -> str:
+    """Compile every translation unit and link the shared library.
+
+    extra_flags / lib_path / build_dir build a variant elsewhere (for tuning
+    experiments); the default is the in-tree library the package loads."""
+    if not force and not extra_flags and not _sources_newer_than(lib_path):
+        return lib_path
+    os.makedirs(build_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib_path), exist_ok=True)
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda u: _compile(u[0], u[1], verbose), UNITS))
-    tmp = LIB_PATH + ".tmp"
+        objs = list(ex.map(lambda u: _compile(u[0], list(u[1]) + list(extra_flags), verbose, build_dir), UNITS))
+    tmp = lib_path + ".tmp"
     cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lpthread"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"linking libmwsep_gb300.so failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

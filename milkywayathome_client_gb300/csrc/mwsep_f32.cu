@@ -16,10 +16,15 @@
  *   background: x0^2 + x1^2 + x2^2/q^2 = B2 (r - rb)^2 + Db
  *   stream s:   |x - c - ((x - c).a) a|^2 = A2 (r - rs)^2 + Ds
  * with B2, rb, Db, A2, rs, Ds >= 0 computed per column in FP64.  Both forms
- * are sums of non-negative terms, so FP32 evaluation has no cancellation;
- * r - rb is formed from (hi, lo) float pairs so it keeps full relative
- * accuracy even when r and rb are close.  The stream exponent
- * -|.|^2/(2 sigma^2) becomes a base-2 polynomial k2 t^2 + k0 fed to ex2.
+ * are sums of non-negative terms, so FP32 evaluation has no cancellation.
+ * t = r - rb is formed from (hi, lo) float pairs, so it keeps full relative
+ * accuracy even where r and rb are close, and each stream reuses it:
+ * r - rs = t + (rb - rs) with the FP64 offset split into (hi, lo) too.
+ * The stream exponent -|.|^2/(2 sigma^2) becomes k2 ts^2 + k0 in base 2.
+ *
+ * Kernels are specialised on the exact stream count (1..4; 8 covers 5..8
+ * with guards) and on the background form, so the inner loop carries no
+ * dead work.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -31,6 +36,15 @@ using mwsep::comp_sum;
 namespace {
 
 constexpr double kLog2e = 1.4426950408889634073599246810018921;
+
+/* background forms */
+enum BgForm
+{
+    BG_HERNQUIST = 0,     /* alpha = delta = 1 (:220-258) */
+    BG_HERNQUIST_AUX = 1, /* ... plus the quadratic-in-g aux profile (:234-239) */
+    BG_GENERAL = 2,       /* pow(rg, alpha) pow(rg + r0, 3 - alpha + delta) (:259-272) */
+    BG_NONE = 3           /* q == 0: bg = -1 per point set, no reff (:213-216) */
+};
 
 __device__ __forceinline__ float ex2a(float x)
 {
@@ -57,7 +71,7 @@ __device__ __forceinline__ float lg2a(float x)
     return y;
 }
 
-/* FP32 Kahan accumulator. */
+/* FP32 Kahan accumulator (value = s - c). */
 struct fkahan
 {
     float s, c;
@@ -78,34 +92,42 @@ __device__ __forceinline__ void split(double v, float& hi, float& lo)
     lo = (float)(v - (double)hi);
 }
 
-/* Per-column (or per-star) constants of one theta, FP64 -> FP32. */
-template <int SMAX>
-struct ColumnConsts
+template <int S>
+struct SArr
 {
-    float B2, Db, rb_hi, rb_lo;
-    float k2[SMAX], k0[SMAX], rs_hi[SMAX], rs_lo[SMAX];
+    static constexpr int N = S > 0 ? S : 1;
 };
 
-template <int SMAX>
-__device__ __forceinline__ void column_consts(double bsin, double bcos, double lsin, double lcos,
-                                              const mwsep_theta_consts& th, ColumnConsts<SMAX>& cc)
+/* Per-column (or per-star) constants of one theta.  Stream s: with
+ * u = t + d_hi and d = rb - rs = d_hi + d_lo, the base-2 exponent is
+ *   k2 (u + d_lo)^2 + k0 = u (k2 u + k2dl) + k0c,
+ * k2dl = 2 k2 d_lo, k0c = k0 + k2 d_lo^2 (two FMAs per point). */
+template <int S>
+struct Col
 {
+    float B2, Db, rb_hi, rb_lo;
+    float k2[SArr<S>::N], k2dl[SArr<S>::N], k0c[SArr<S>::N], d_hi[SArr<S>::N];
+};
+
+template <int S>
+__device__ __forceinline__ void column_consts(const double* g, const mwsep_theta_consts& th, Col<S>& cc)
+{
+    const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
     const double u0 = bcos * lcos, u1 = bcos * lsin, u2 = bsin;
     const double iq2 = 1.0 / (th.q * th.q);
     const double perp = u1 * u1 + u2 * u2 * iq2;
     const double B2 = u0 * u0 + perp;
     const double rb = MW_LBR_R * u0 / B2;
-    const double Db = (MW_LBR_R * MW_LBR_R) * perp / B2;
     cc.B2 = (float)B2;
-    cc.Db = (float)Db;
+    cc.Db = (float)((MW_LBR_R * MW_LBR_R) * perp / B2);
     split(rb, cc.rb_hi, cc.rb_lo);
 #pragma unroll
-    for (int s = 0; s < SMAX; ++s)
+    for (int s = 0; s < S; ++s)
     {
         if (s < th.n_streams)
         {
             const double a0 = th.a[s][0], a1 = th.a[s][1], a2 = th.a[s][2];
-            /* c' = c + Sun offset: x - c = r u - c' */
+            /* c' = c + Sun offset so that x - c = r u - c' */
             const double c0 = th.c[s][0] + MW_LBR_R, c1 = th.c[s][1], c2 = th.c[s][2];
             const double au = a0 * u0 + a1 * u1 + a2 * u2;
             const double p0 = u0 - au * a0, p1 = u1 - au * a1, p2 = u2 - au * a2;
@@ -115,82 +137,87 @@ __device__ __forceinline__ void column_consts(double bsin, double bcos, double l
             const double rs = (A2 > 1e-300) ? (p0 * q0 + p1 * q1 + p2 * q2) / A2 : 0.0;
             const double e0 = q0 - rs * p0, e1 = q1 - rs * p1, e2 = q2 - rs * p2;
             const double Ds = e0 * e0 + e1 * e1 + e2 * e2;
-            const double f = -kLog2e / th.sigma_sq2[s];
-            cc.k2[s] = (float)(A2 * f);
-            cc.k0[s] = (float)(Ds * f);
-            split(rs, cc.rs_hi[s], cc.rs_lo[s]);
+            const double f = th.stream_on[s] ? -kLog2e / th.sigma_sq2[s] : 0.0;
+            const double k2 = A2 * f;
+            float d_lo;
+            split(rb - rs, cc.d_hi[s], d_lo);
+            cc.k2[s] = (float)k2;
+            cc.k2dl[s] = (float)(2.0 * k2 * (double)d_lo);
+            /* a switched-off stream gets an exponent far below the FTZ range */
+            cc.k0c[s] = th.stream_on[s] ? (float)(Ds * f + k2 * (double)d_lo * (double)d_lo) : -1.0e30f;
         }
         else
         {
             cc.k2[s] = 0.f;
-            cc.k0[s] = 0.f;
-            cc.rs_hi[s] = 0.f;
-            cc.rs_lo[s] = 0.f;
+            cc.k2dl[s] = 0.f;
+            cc.k0c[s] = -1.0e30f;
+            cc.d_hi[s] = 0.f;
         }
     }
 }
 
-/* Sum over the C convolution points of one cell or star.  rh/rl/qv/gm are
- * read at [n*stride].  Returns plain FP32 sums (bg, st[]), each already
- * weighted by the folded table factor qv. */
-template <int SMAX>
-__device__ __forceinline__ void convolve_f32(const float* __restrict__ rh, const float* __restrict__ rl,
-                                             const float* __restrict__ qv, const float* __restrict__ gm,
-                                             size_t stride, int C, const ColumnConsts<SMAX>& cc,
-                                             const mwsep_theta_consts& th, float r0f, float auxa, float auxb,
-                                             float auxc, float alpha, float ad3, float& bg, float (&st)[SMAX])
+struct BgConsts
 {
-    const int S = th.n_streams;
-    float bgs = 0.f;
-    float sts[SMAX];
-#pragma unroll
-    for (int s = 0; s < SMAX; ++s) sts[s] = 0.f;
-    const int mode = th.bg_mode;
-    const bool aux = th.aux != 0;
+    float r0, aux_a, aux_b, aux_c, alpha, ad3;
+};
 
-#pragma unroll 4
-    for (int n = 0; n < C; ++n)
-    {
-        const size_t o = (size_t)n * stride;
-        const float r_hi = rh[o], r_lo = rl[o], q = qv[o];
-        if (mode == 0)
+/* The density sums of one cell (or star) over its C convolution points:
+ * points at p[n * stride], {r_hi, r_lo, weight, g}.  Plain FP32 sums in two
+ * interleaved halves (more independent chains, smaller rounding). */
+template <int S, int FORM>
+__device__ __forceinline__ void convolve(const float4* __restrict__ p, int stride, int C, const Col<S>& cc,
+                                         const BgConsts& bc, float& bg, float (&st)[SArr<S>::N])
+{
+    float bga = 0.f, bgb = 0.f;
+    float sa[SArr<S>::N], sb[SArr<S>::N];
+#pragma unroll
+    for (int s = 0; s < S; ++s) sa[s] = sb[s] = 0.f;
+
+    auto point = [&](const float4 v, float& bgacc, float (&sacc)[SArr<S>::N]) {
+        const float t = (v.x - cc.rb_hi) + (v.y - cc.rb_lo);
+        if (FORM == BG_HERNQUIST || FORM == BG_HERNQUIST_AUX)
         {
-            const float t = (r_hi - cc.rb_hi) + (r_lo - cc.rb_lo);
             const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
-            const float y = rsqa(rg2);            /* 1/rg */
-            const float rs = fmaf(rg2, y, r0f);    /* rg + r0 */
+            const float y = rsqa(rg2);           /* 1 / rg */
+            const float rs = fmaf(rg2, y, bc.r0); /* rg + r0 */
             const float den = rs * rs * rs;
-            float term = q * y * rcpa(den);
-            if (aux)
-            {
-                const float g = gm[o];
-                term = fmaf(q, fmaf(fmaf(auxa, g, auxb), g, auxc), term);
-            }
-            bgs += term;
+            bgacc = fmaf(v.z * y, rcpa(den), bgacc);
+            if (FORM == BG_HERNQUIST_AUX)
+                bgacc = fmaf(v.z, fmaf(fmaf(bc.aux_a, v.w, bc.aux_b), v.w, bc.aux_c), bgacc);
         }
-        else if (mode == 1)
+        else if (FORM == BG_GENERAL)
         {
-            const float t = (r_hi - cc.rb_hi) + (r_lo - cc.rb_lo);
             const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
             const float rg = rg2 * rsqa(rg2);
-            /* rg^alpha (rg + r0)^(3 - alpha + delta) in base 2 */
-            const float l2 = fmaf(alpha, lg2a(rg), ad3 * lg2a(rg + r0f));
-            bgs += q * ex2a(-l2);
+            const float l2 = fmaf(bc.alpha, lg2a(rg), bc.ad3 * lg2a(rg + bc.r0));
+            bgacc = fmaf(v.z, ex2a(-l2), bgacc);
         }
 #pragma unroll
-        for (int s = 0; s < SMAX; ++s)
+        for (int s = 0; s < S; ++s)
         {
-            if (s < S)
-            {
-                const float t = (r_hi - cc.rs_hi[s]) + (r_lo - cc.rs_lo[s]);
-                const float e = ex2a(fmaf(cc.k2[s] * t, t, cc.k0[s]));
-                sts[s] = fmaf(q, e, sts[s]);
-            }
+            const float u = t + cc.d_hi[s];
+            const float arg = fmaf(u, fmaf(cc.k2[s], u, cc.k2dl[s]), cc.k0c[s]);
+            sacc[s] = fmaf(v.z, ex2a(arg), sacc[s]);
         }
+    };
+
+    /* four points per trip, loads issued before any arithmetic */
+    int n = 0;
+    for (; n + 3 < C; n += 4)
+    {
+        const float4 v0 = p[(size_t)n * stride];
+        const float4 v1 = p[(size_t)(n + 1) * stride];
+        const float4 v2 = p[(size_t)(n + 2) * stride];
+        const float4 v3 = p[(size_t)(n + 3) * stride];
+        point(v0, bga, sa);
+        point(v1, bgb, sb);
+        point(v2, bga, sa);
+        point(v3, bgb, sb);
     }
-    bg = bgs;
+    for (; n < C; ++n) point(p[(size_t)n * stride], bga, sa);
+    bg = bga + bgb;
 #pragma unroll
-    for (int s = 0; s < SMAX; ++s) st[s] = sts[s];
+    for (int s = 0; s < S; ++s) st[s] = sa[s] + sb[s];
 }
 
 __device__ __forceinline__ void load_theta(mwsep_theta_consts& dst, const mwsep_theta_consts* src)
@@ -200,173 +227,230 @@ __device__ __forceinline__ void load_theta(mwsep_theta_consts& dst, const mwsep_
     for (int i = threadIdx.x; i < (int)(sizeof(mwsep_theta_consts) / 8); i += blockDim.x) d[i] = s[i];
 }
 
-template <int SMAX>
-__global__ void __launch_bounds__(256) integral_f32_kernel(const mwsep_area_dev A,
-                                                           const mwsep_theta_consts* __restrict__ thetas,
-                                                           double2* __restrict__ partials,
-                                                           long long theta_stride)
+__device__ __forceinline__ BgConsts bg_consts(const mwsep_theta_consts& th)
+{
+    BgConsts b;
+    b.r0 = (float)th.r0;
+    b.aux_a = (float)th.bg_a;
+    b.aux_b = (float)th.bg_b;
+    b.aux_c = (float)th.bg_c;
+    b.alpha = (float)th.alpha;
+    b.ad3 = (float)th.alpha_delta3;
+    return b;
+}
+
+/* Block-level reduction of plain per-thread doubles into compensated pairs. */
+template <int NC>
+__device__ __forceinline__ void reduce_and_store(const double (&v)[NC], int ncomp, double* smem, double2* out)
+{
+    comp_sum acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+    {
+        acc[k].s = v[k];
+        acc[k].c = 0.0;
+    }
+    mwsep::block_reduce<NC>(acc, smem);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+            if (k < ncomp) out[k] = make_double2(acc[k].s, acc[k].c);
+    }
+}
+
+constexpr int kBlock = 256;
+#ifndef MWSEP_F32_MINB
+#define MWSEP_F32_MINB 2 /* 2 x 256 threads per SM: <= 128 registers, no spills up to 3 streams */
+#endif
+
+template <int S, int FORM>
+__global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32_kernel(const mwsep_area_dev A,
+                                                                 const mwsep_theta_consts* __restrict__ thetas,
+                                                                 double2* __restrict__ partials,
+                                                                 long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (1 + SMAX) * 32];
+    __shared__ double red[2 * (1 + S) * 32];
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
+    /* a batch mixing background forms gets one launch per form */
+    if (mwsep_bg_form(&th) != FORM) return;
 
-    comp_sum acc[1 + SMAX];
+    double acc[1 + S];
 #pragma unroll
-    for (int k = 0; k < 1 + SMAX; ++k) acc[k].zero();
+    for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
 
-    const int S = th.n_streams;
     const int C = A.convolve;
-    const float r0f = (float)th.r0;
-    const float auxa = (float)th.bg_a, auxb = (float)th.bg_b, auxc = (float)th.bg_c;
-    const float alpha = (float)th.alpha, ad3 = (float)th.alpha_delta3;
+    const BgConsts bc = bg_consts(th);
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < A.n_items; item += stride)
     {
         const int kc = (int)(item / A.n_cols);
         const int col = (int)(item - (long long)kc * A.n_cols);
-        const int j = col % A.nu_steps;
-        const double* g = A.geom + 4 * (size_t)col;
-        ColumnConsts<SMAX> cc;
-        column_consts<SMAX>(g[0], g[1], g[2], g[3], th, cc);
+        Col<S> cc;
+        column_consts<S>(A.geom + 4 * (size_t)col, th, cc);
         const int k0 = kc * A.k_chunk;
         const int k1 = min(k0 + A.k_chunk, A.r_steps);
-        fkahan kb, ks[SMAX];
+        fkahan kb, ks[SArr<S>::N];
         kb.zero();
 #pragma unroll
-        for (int s = 0; s < SMAX; ++s) ks[s].zero();
+        for (int s = 0; s < S; ++s) ks[s].zero();
         for (int k = k0; k < k1; ++k)
         {
-            float bg, st[SMAX];
-            const size_t row = (size_t)k * C;
-            convolve_f32<SMAX>(A.r_hi + row, A.r_lo + row, A.qwv + row, A.gmag + row, 1, C, cc, th, r0f, auxa,
-                               auxb, auxc, alpha, ad3, bg, st);
-            if (th.bg_mode == 2) bg = -(float)A.irv[k]; /* bg = -1 times V, no reff (:213-216) */
+            float bg, st[SArr<S>::N];
+            convolve<S, FORM>(A.pts + (size_t)k * C, 1, C, cc, bc, bg, st);
+            /* q == 0: bg = -1, times V but not reff (:213-216, :504) */
+            if (FORM == BG_NONE) bg = -(float)A.irv[k];
             kb.add(bg);
 #pragma unroll
-            for (int s = 0; s < SMAX; ++s)
-                if (s < S && th.stream_on[s]) ks[s].add(st[s]);
+            for (int s = 0; s < S; ++s) ks[s].add(st[s]);
         }
-        /* the folded qwv carries reff*irv; the nu-slab factor ids[j] and the
-         * hand-off to FP64 happen once per item */
-        const double idsj = A.ids[j];
-        acc[0].add(kb.value() * idsj);
+        /* the table weights carry reff*irv; the nu-slab factor ids[j] and
+         * the hand-off to FP64 happen once per item */
+        const double idsj = A.ids[col % A.nu_steps];
+        acc[0] += kb.value() * idsj;
 #pragma unroll
-        for (int s = 0; s < SMAX; ++s)
-            if (s < S) acc[1 + s].add(ks[s].value() * idsj);
+        for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * idsj;
     }
-    mwsep::block_reduce<1 + SMAX>(acc, red);
-    if (threadIdx.x == 0)
-    {
-        double2* out = partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + S);
-        out[0] = make_double2(acc[0].s, acc[0].c);
-#pragma unroll
-        for (int s = 0; s < SMAX; ++s)
-            if (s < S) out[1 + s] = make_double2(acc[1 + s].s, acc[1 + s].c);
-    }
+    reduce_and_store<1 + S>(acc, 1 + th.n_streams, red,
+                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams));
 }
 
-template <int SMAX>
-__global__ void __launch_bounds__(256) likelihood_f32_kernel(const mwsep_stars_dev St,
-                                                             const mwsep_theta_consts* __restrict__ thetas,
-                                                             const double* __restrict__ integrals,
-                                                             double2* __restrict__ partials,
-                                                             long long theta_stride)
+/* calculate_likelihood per star (cpu/evaluation_optimized.c:665-717); the
+ * density sums in FP32, everything after them in FP64. */
+template <int S>
+__global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_stars_dev St,
+                                                                const mwsep_theta_consts* __restrict__ thetas,
+                                                                const double* __restrict__ integrals,
+                                                                double2* __restrict__ partials,
+                                                                long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (3 + SMAX) * 32];
+    __shared__ double red[2 * (3 + S) * 32];
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
-    const int S = th.n_streams;
-    const double* I = integrals + (size_t)blockIdx.y * (1 + S);
+    const int NS = th.n_streams;
+    const double* I = integrals + (size_t)blockIdx.y * (1 + NS);
     const double Ibg = I[0];
-    const float r0f = (float)th.r0;
-    const float auxa = (float)th.bg_a, auxb = (float)th.bg_b, auxc = (float)th.bg_c;
-    const float alpha = (float)th.alpha, ad3 = (float)th.alpha_delta3;
+    const BgConsts bc = bg_consts(th);
 
-    comp_sum acc[3 + SMAX];
+    double acc[3 + S];
 #pragma unroll
-    for (int k = 0; k < 3 + SMAX; ++k) acc[k].zero();
+    for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
 
     const int N = St.n_stars;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
     {
-        const double* g = St.geom + 4 * (size_t)s0;
-        ColumnConsts<SMAX> cc;
-        column_consts<SMAX>(g[0], g[1], g[2], g[3], th, cc);
-        float bgf, stf[SMAX];
-        convolve_f32<SMAX>(St.r_hi + s0, St.r_lo + s0, St.qwv + s0, St.gmag + s0, (size_t)N, St.convolve, cc,
-                           th, r0f, auxa, auxb, auxc, alpha, ad3, bgf, stf);
-        /* qwv already carries the star's reff_xr_rp3 */
+        Col<S> cc;
+        column_consts<S>(St.geom + 4 * (size_t)s0, th, cc);
+        float bgf = 0.f, stf[SArr<S>::N];
+        switch (th.bg_mode == 2 ? BG_NONE : th.bg_mode == 1 ? BG_GENERAL : th.aux ? BG_HERNQUIST_AUX : BG_HERNQUIST)
+        {
+        case BG_HERNQUIST: convolve<S, BG_HERNQUIST>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
+        case BG_HERNQUIST_AUX: convolve<S, BG_HERNQUIST_AUX>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
+        case BG_GENERAL: convolve<S, BG_GENERAL>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
+        default: convolve<S, BG_NONE>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
+        }
+        /* the star weights carry its reff_xr_rp3 */
         const double bg = (th.bg_mode == 2) ? -1.0 : (double)bgf;
 
         double bg_only = (bg / Ibg) * th.exp_bg_weight;
         double star_prob = bg_only;
-        bg_only = (bg_only == 0.0) ? -238.0 : log10(bg_only / th.sum_exp_weights);
-        acc[2].add(bg_only);
+        acc[2] += (bg_only == 0.0) ? -238.0 : log10(bg_only / th.sum_exp_weights);
 #pragma unroll
-        for (int s = 0; s < SMAX; ++s)
+        for (int s = 0; s < S; ++s)
         {
-            if (s < S)
+            if (s < NS)
             {
-                const double v = th.stream_on[s] ? (double)stf[s] : 0.0;
-                double st_only = v / I[1 + s] * th.exp_stream_weight[s];
+                double st_only = (double)stf[s] / I[1 + s] * th.exp_stream_weight[s];
                 star_prob += st_only;
-                st_only = (st_only == 0.0) ? -238.0 : log10(st_only / th.sum_exp_weights);
-                acc[3 + s].add(st_only);
+                acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only / th.sum_exp_weights);
             }
         }
         star_prob /= th.sum_exp_weights;
         if (star_prob != 0.0)
-            acc[0].add(log10(star_prob));
+            acc[0] += log10(star_prob);
         else
         {
-            acc[0].add(-238.0);
-            acc[1].add(1.0);
+            acc[0] += -238.0;
+            acc[1] += 1.0;
         }
     }
-    mwsep::block_reduce<3 + SMAX>(acc, red);
-    if (threadIdx.x == 0)
-    {
-        double2* out = partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + S);
-#pragma unroll
-        for (int k = 0; k < 3 + SMAX; ++k)
-            if (k < 3 + S) out[k] = make_double2(acc[k].s, acc[k].c);
-    }
+    reduce_and_store<3 + S>(acc, 3 + NS, red,
+                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }
 
-template <int SMAX>
+template <int S>
 int launch_integral(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
-                    double2* partials, cudaStream_t st)
+                    int form, double2* partials, cudaStream_t st)
 {
     const long long ncomp = 1 + sh->n_streams;
     const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
+    double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
-    integral_f32_kernel<SMAX><<<g, sh->block, 0, st>>>(*A, th, partials + (size_t)sh->area_index * sh->grid * ncomp,
-                                                        theta_stride);
+    switch (form)
+    {
+    case BG_HERNQUIST: integral_f32_kernel<S, BG_HERNQUIST><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+    case BG_HERNQUIST_AUX:
+        integral_f32_kernel<S, BG_HERNQUIST_AUX><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
+        break;
+    case BG_GENERAL: integral_f32_kernel<S, BG_GENERAL><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+    default: integral_f32_kernel<S, BG_NONE><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+    }
     return (int)cudaGetLastError();
 }
 
-template <int SMAX>
-int launch_likelihood(const mwsep_stars_dev* S, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
+template <int S>
+int launch_likelihood(const mwsep_stars_dev* St, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
                       const double* integrals, double2* partials, cudaStream_t st)
 {
     const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
     dim3 g(sh->grid, sh->n_theta);
-    likelihood_f32_kernel<SMAX><<<g, sh->block, 0, st>>>(*S, th, integrals, partials, theta_stride);
+    likelihood_f32_kernel<S><<<g, kBlock, 0, st>>>(*St, th, integrals, partials, theta_stride);
     return (int)cudaGetLastError();
 }
 
 } // namespace
 
+/* Resident blocks per SM of the compensated integral kernel for S streams
+ * (sizes the persistent grid). */
+extern "C" int mwsep_integral_f32_blocks_per_sm(int n_streams)
+{
+    int b = 0;
+    cudaError_t e;
+    switch (n_streams)
+    {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<0, BG_HERNQUIST>, kBlock, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<1, BG_HERNQUIST>, kBlock, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<2, BG_HERNQUIST>, kBlock, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<3, BG_HERNQUIST>, kBlock, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<4, BG_HERNQUIST>, kBlock, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<8, BG_HERNQUIST>, kBlock, 0); break;
+    }
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return b > 0 ? b : 1;
+}
+
+/* shape->block is fixed at kBlock (256) for these kernels. */
 extern "C" int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                                          const mwsep_launch_shape* sh, double2* partials, void* stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (sh->n_streams <= 1) return launch_integral<1>(area, th_dev, sh, partials, st);
-    if (sh->n_streams <= 2) return launch_integral<2>(area, th_dev, sh, partials, st);
-    if (sh->n_streams <= 4) return launch_integral<4>(area, th_dev, sh, partials, st);
-    return launch_integral<8>(area, th_dev, sh, partials, st);
+    const int form = sh->bg_form;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_integral<0>(area, th_dev, sh, form, partials, st);
+    case 1: return launch_integral<1>(area, th_dev, sh, form, partials, st);
+    case 2: return launch_integral<2>(area, th_dev, sh, form, partials, st);
+    case 3: return launch_integral<3>(area, th_dev, sh, form, partials, st);
+    case 4: return launch_integral<4>(area, th_dev, sh, form, partials, st);
+    default: return launch_integral<8>(area, th_dev, sh, form, partials, st);
+    }
 }
 
 extern "C" int mwsep_launch_likelihood_f32(const mwsep_stars_dev* stars, const mwsep_theta_consts* th_dev,
@@ -374,8 +458,13 @@ extern "C" int mwsep_launch_likelihood_f32(const mwsep_stars_dev* stars, const m
                                            double2* partials, void* stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (sh->n_streams <= 1) return launch_likelihood<1>(stars, th_dev, sh, integrals, partials, st);
-    if (sh->n_streams <= 2) return launch_likelihood<2>(stars, th_dev, sh, integrals, partials, st);
-    if (sh->n_streams <= 4) return launch_likelihood<4>(stars, th_dev, sh, integrals, partials, st);
-    return launch_likelihood<8>(stars, th_dev, sh, integrals, partials, st);
+    switch (sh->n_streams)
+    {
+    case 0: return launch_likelihood<0>(stars, th_dev, sh, integrals, partials, st);
+    case 1: return launch_likelihood<1>(stars, th_dev, sh, integrals, partials, st);
+    case 2: return launch_likelihood<2>(stars, th_dev, sh, integrals, partials, st);
+    case 3: return launch_likelihood<3>(stars, th_dev, sh, integrals, partials, st);
+    case 4: return launch_likelihood<4>(stars, th_dev, sh, integrals, partials, st);
+    default: return launch_likelihood<8>(stars, th_dev, sh, integrals, partials, st);
+    }
 }

@@ -252,6 +252,22 @@ int launch_likelihood(const mwsep_stars_dev* S, const mwsep_theta_consts* th, co
 
 } // namespace
 
+extern "C" int mwsep_integral_f64_blocks_per_sm(int n_streams, int block)
+{
+    int b = 0;
+    cudaError_t e;
+    if (n_streams <= 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f64_kernel<1>, block, 0);
+    else if (n_streams <= 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f64_kernel<2>, block, 0);
+    else if (n_streams <= 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f64_kernel<4>, block, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f64_kernel<8>, block, 0);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return b > 0 ? b : 1;
+}
+
 extern "C" int mwsep_launch_integral_f64(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                                          const mwsep_launch_shape* sh, double2* partials, void* stream)
 {

@@ -44,8 +44,7 @@ __global__ void star_tables_kernel(int n, const double* __restrict__ l, const do
                                    const double* __restrict__ gl_w, double coeff, double* __restrict__ geom,
                                    double* __restrict__ r_point, double* __restrict__ qw,
                                    double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
-                                   double* __restrict__ reff, float* __restrict__ r_hi, float* __restrict__ r_lo,
-                                   float* __restrict__ qwv, float* __restrict__ gmag)
+                                   double* __restrict__ reff, float4* __restrict__ pts)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
@@ -62,10 +61,7 @@ __global__ void star_tables_kernel(int n, const double* __restrict__ l, const do
             r_point[o] = rp;
             qw[o] = q;
             const float hi = (float)rp;
-            r_hi[o] = hi;
-            r_lo[o] = (float)(rp - (double)hi);
-            qwv[o] = (float)(q * rf);
-            gmag[o] = (float)g;
+            pts[o] = make_float4(hi, (float)(rp - (double)hi), (float)(q * rf), (float)g);
         }
         double* gg = geom + 4 * (size_t)s;
         gg[0] = sin(b[s] / MW_DEG);
@@ -92,14 +88,12 @@ extern "C" int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps
 extern "C" int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
                                         const double* dx, const double* gl_w, double coeff, double* geom,
                                         double* r_point, double* qw, double* r_in_mag, double* r_in_mag2,
-                                        double* reff, float* r_hi, float* r_lo, float* qwv, float* gmag,
-                                        void* stream)
+                                        double* reff, float4* pts, void* stream)
 {
     if (n <= 0) return 0;
     int grid = (n + 127) / 128;
     if (grid > 152 * 32) grid = 152 * 32;
     star_tables_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(n, l, b, r, convolve, dx, gl_w, coeff, geom,
-                                                               r_point, qw, r_in_mag, r_in_mag2, reff, r_hi,
-                                                               r_lo, qwv, gmag);
+                                                               r_point, qw, r_in_mag, r_in_mag2, reff, pts);
     return (int)cudaGetLastError();
 }

@@ -198,7 +198,7 @@ struct AreaHost
 
 struct AreaDev
 {
-    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, r_hi, r_lo, qwv, gmag;
+    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, pts;
     mwsep_area_dev view{};
 };
 
@@ -249,8 +249,7 @@ struct mwsep_ctx
 
     bool has_stars = false;
     int n_stars = 0;
-    DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_r_hi, s_r_lo, s_qwv,
-        s_gmag;
+    DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_pts;
     mwsep_stars_dev stars_view{};
     HostPinned h_stars;
 
@@ -260,9 +259,22 @@ struct mwsep_ctx
     Tune tune[2];
     double last_ms[5] = {};
     int last_launches = 0;
+    size_t xfer_h2d = 0, xfer_d2h = 0;
 };
 
 namespace {
+
+/* cudaMemcpyAsync with transfer accounting */
+cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    c->xfer_h2d += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+}
+cudaError_t d2h(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    c->xfer_d2h += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+}
 
 int check_problem(const ASTRONOMY_PARAMETERS* ap)
 {
@@ -404,9 +416,18 @@ int occupancy_grid(mwsep_ctx* c, int block, long long items)
     return (int)g;
 }
 
+long env_long(const char* name, long dflt)
+{
+    const char* v = getenv(name);
+    return (v && *v) ? strtol(v, nullptr, 10) : dflt;
+}
+
 /* Default launch shapes for the resident problem.  The shape depends only
  * on the problem, never on the batch, so a theta gives the same bits alone
- * and inside any batch. */
+ * and inside any batch.  Integral kernels run a persistent grid (resident
+ * blocks per SM x SMs); items (column x r-run) are sized so each thread gets
+ * many, which keeps the static tail short.  MWSEP_TUNE_{KCHUNK,GRID_F32,
+ * GRID_F64} override the choice (the autotuner's search space). */
 void default_tune(mwsep_ctx* c)
 {
     const ProblemHost& p = c->prob;
@@ -421,14 +442,21 @@ void default_tune(mwsep_ctx* c)
     {
         Tune& t = c->tune[prec];
         t.block = 256;
-        /* enough items for ~32 per thread of a full-occupancy grid */
-        const long long want_items = (long long)c->sm_count * 2048 * 32;
+        const int per_sm = prec == MWSEP_PLAIN_F64 ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
+                                                   : mwsep_integral_f32_blocks_per_sm(p.n_streams);
+        const long long threads = (long long)c->sm_count * per_sm * t.block;
+        /* ~48 items per thread keeps the static tail of the grid-stride
+         * loop near 2%; the compensated kernel's FP64 column prologue per
+         * item stays a few percent of its work at that length */
+        const long long want_items = threads * 48;
         long long chunks = (want_items + max_cols - 1) / std::max<long long>(max_cols, 1);
-        if (chunks < 1) chunks = 1;
-        if (chunks > max_r) chunks = max_r;
+        chunks = std::max<long long>(1, std::min<long long>(chunks, max_r));
         t.k_chunk = (int)((max_r + chunks - 1) / chunks);
-        long long items = max_cols * ((max_r + t.k_chunk - 1) / t.k_chunk);
-        t.grid = occupancy_grid(c, t.block, items);
+        t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", t.k_chunk);
+        const long long items = max_cols * ((max_r + t.k_chunk - 1) / t.k_chunk);
+        long long g = std::min<long long>((long long)c->sm_count * per_sm, (items + t.block - 1) / t.block);
+        g = env_long(prec == MWSEP_PLAIN_F64 ? "MWSEP_TUNE_GRID_F64" : "MWSEP_TUNE_GRID_F32", g);
+        t.grid = (int)std::max<long long>(1, g);
         t.lk_block = 256;
         t.lk_grid = occupancy_grid(c, t.lk_block, std::max(c->n_stars, 1));
     }
@@ -444,7 +472,7 @@ int build_area(mwsep_ctx* c, int a)
 
     /* cpu__r_constants (cpu/evaluation_optimized.c:360-422) on the host */
     std::vector<double> irv(R), reff(R), rp(RC), qw(RC), gm(RC), gm2(RC), ids(NU), nus(NU);
-    std::vector<float> rhi(RC), rlo(RC), qwv(RC), gmf(RC);
+    std::vector<float4> pts(RC);
     for (int i = 0; i < R; ++i)
     {
         const double log_r = A.r_min + (i * A.r_step);
@@ -462,10 +490,7 @@ int build_area(mwsep_ctx* c, int a)
             gm[o] = g;
             gm2[o] = g * g;
             const float hi = (float)rp[o];
-            rhi[o] = hi;
-            rlo[o] = (float)(rp[o] - (double)hi);
-            qwv[o] = (float)(qw[o] * (reff[i] * irv[i]));
-            gmf[o] = (float)g;
+            pts[o] = make_float4(hi, (float)(rp[o] - (double)hi), (float)(qw[o] * (reff[i] * irv[i])), (float)g);
         }
     }
     for (int j = 0; j < NU; ++j)
@@ -487,25 +512,19 @@ int build_area(mwsep_ctx* c, int a)
     rc |= D.irv.ensure(R * 8, tot);
     rc |= D.ids.ensure(NU * 8, tot);
     rc |= D.nus.ensure(NU * 8, tot);
-    rc |= D.r_hi.ensure(RC * 4, tot);
-    rc |= D.r_lo.ensure(RC * 4, tot);
-    rc |= D.qwv.ensure(RC * 4, tot);
-    rc |= D.gmag.ensure(RC * 4, tot);
+    rc |= D.pts.ensure(RC * sizeof(float4), tot);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
 
     cudaStream_t st = c->stream;
-    CU(cudaMemcpyAsync(D.r_point.p, rp.data(), RC * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.qw.p, qw.data(), RC * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.r_in_mag.p, gm.data(), RC * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.r_in_mag2.p, gm2.data(), RC * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.reff.p, reff.data(), R * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.irv.p, irv.data(), R * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.ids.p, ids.data(), NU * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.nus.p, nus.data(), NU * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.r_hi.p, rhi.data(), RC * 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.r_lo.p, rlo.data(), RC * 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.qwv.p, qwv.data(), RC * 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(D.gmag.p, gmf.data(), RC * 4, cudaMemcpyHostToDevice, st));
+    CU(h2d(c, D.r_point.p, rp.data(), RC * 8));
+    CU(h2d(c, D.qw.p, qw.data(), RC * 8));
+    CU(h2d(c, D.r_in_mag.p, gm.data(), RC * 8));
+    CU(h2d(c, D.r_in_mag2.p, gm2.data(), RC * 8));
+    CU(h2d(c, D.reff.p, reff.data(), R * 8));
+    CU(h2d(c, D.irv.p, irv.data(), R * 8));
+    CU(h2d(c, D.ids.p, ids.data(), NU * 8));
+    CU(h2d(c, D.nus.p, nus.data(), NU * 8));
+    CU(h2d(c, D.pts.p, pts.data(), RC * sizeof(float4)));
     CK(mwsep_launch_geometry(A.mu_min, A.mu_step, A.mu_steps, D.nus.as<double>(), NU, p.sgr, p.wedge,
                              D.geom.as<double>(), st));
     /* the host vectors die with this frame: wait for the copies */
@@ -525,10 +544,7 @@ int build_area(mwsep_ctx* c, int a)
     v.reff = D.reff.as<double>();
     v.irv = D.irv.as<double>();
     v.ids = D.ids.as<double>();
-    v.r_hi = D.r_hi.as<float>();
-    v.r_lo = D.r_lo.as<float>();
-    v.qwv = D.qwv.as<float>();
-    v.gmag = D.gmag.as<float>();
+    v.pts = D.pts.as<float4>();
     return MWSEP_OK;
 }
 
@@ -556,20 +572,16 @@ int upload_stars(mwsep_ctx* c, int n, const double* l, const double* b, const do
     rc |= c->s_r_in_mag.ensure(NC * 8, tot);
     rc |= c->s_r_in_mag2.ensure(NC * 8, tot);
     rc |= c->s_reff.ensure((size_t)n * 8, tot);
-    rc |= c->s_r_hi.ensure(NC * 4, tot);
-    rc |= c->s_r_lo.ensure(NC * 4, tot);
-    rc |= c->s_qwv.ensure(NC * 4, tot);
-    rc |= c->s_gmag.ensure(NC * 4, tot);
+    rc |= c->s_pts.ensure(NC * sizeof(float4), tot);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
     cudaStream_t st = c->stream;
-    CU(cudaMemcpyAsync(c->s_l.p, l, (size_t)n * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(c->s_b.p, b, (size_t)n * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(c->s_r.p, r, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    CU(h2d(c, c->s_l.p, l, (size_t)n * 8));
+    CU(h2d(c, c->s_b.p, b, (size_t)n * 8));
+    CU(h2d(c, c->s_r.p, r, (size_t)n * 8));
     CK(mwsep_launch_star_tables(n, c->s_l.as<double>(), c->s_b.as<double>(), c->s_r.as<double>(), C,
                                 c->d_dx.as<double>(), c->d_glw.as<double>(), c->coeff, c->s_geom.as<double>(),
                                 c->s_r_point.as<double>(), c->s_qw.as<double>(), c->s_r_in_mag.as<double>(),
-                                c->s_r_in_mag2.as<double>(), c->s_reff.as<double>(), c->s_r_hi.as<float>(),
-                                c->s_r_lo.as<float>(), c->s_qwv.as<float>(), c->s_gmag.as<float>(), st));
+                                c->s_r_in_mag2.as<double>(), c->s_reff.as<double>(), c->s_pts.as<float4>(), st));
     mwsep_stars_dev& v = c->stars_view;
     v.n_stars = n;
     v.convolve = C;
@@ -579,10 +591,7 @@ int upload_stars(mwsep_ctx* c, int n, const double* l, const double* b, const do
     v.r_in_mag = c->s_r_in_mag.as<double>();
     v.r_in_mag2 = c->s_r_in_mag2.as<double>();
     v.reff = c->s_reff.as<double>();
-    v.r_hi = c->s_r_hi.as<float>();
-    v.r_lo = c->s_r_lo.as<float>();
-    v.qwv = c->s_qwv.as<float>();
-    v.gmag = c->s_gmag.as<float>();
+    v.pts = c->s_pts.as<float4>();
     c->n_stars = n;
     c->has_stars = true;
     for (int prec = 0; prec < 2; ++prec)
@@ -624,7 +633,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     cudaStream_t st = c->stream;
     int launches = 0;
     CU(cudaEventRecord(c->ev[0], st));
-    CU(cudaMemcpyAsync(c->d_theta.p, hth, th_bytes, cudaMemcpyHostToDevice, st));
+    CU(h2d(c, c->d_theta.p, hth, th_bytes));
     CU(cudaEventRecord(c->ev[1], st));
     mwsep_launch_shape sh;
     sh.n_theta = B;
@@ -632,18 +641,33 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     sh.n_areas = A;
     sh.block = t.block;
     sh.grid = t.grid;
+    /* background forms present in the batch (the compensated integral is
+     * specialised on the form) */
+    bool forms[4] = {false, false, false, false};
+    for (int i = 0; i < B; ++i) forms[mwsep_bg_form(&hth[i])] = true;
+    sh.bg_form = 0;
     for (int a = 0; a < A; ++a)
     {
         mwsep_area_dev v = c->areas[a].view;
         set_chunking(v, t.k_chunk);
         sh.area_index = a;
         if (precision == MWSEP_PLAIN_F64)
+        {
             CK(mwsep_launch_integral_f64(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
                                          c->d_partials.as<double2>(), st));
+            ++launches;
+        }
         else
-            CK(mwsep_launch_integral_f32(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
-                                         c->d_partials.as<double2>(), st));
-        ++launches;
+        {
+            for (int form = 0; form < 4; ++form)
+            {
+                if (!forms[form]) continue;
+                sh.bg_form = form;
+                CK(mwsep_launch_integral_f32(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                             c->d_partials.as<double2>(), st));
+                ++launches;
+            }
+        }
     }
     CU(cudaEventRecord(c->ev[2], st));
     CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
@@ -663,7 +687,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     CU(cudaEventRecord(c->ev[4], st));
     CK(mwsep_launch_reduce_likelihood(c->d_lkpartials.as<double2>(), &lk, d_lk, st));
     ++launches;
-    CU(cudaMemcpyAsync(c->h_out.p, c->d_out.p, out_doubles * 8, cudaMemcpyDeviceToHost, st));
+    CU(d2h(c, c->h_out.p, c->d_out.p, out_doubles * 8));
     CU(cudaEventRecord(c->ev[5], st));
     CU(cudaStreamSynchronize(st));
 
@@ -758,12 +782,12 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     {
         AreaDev& D = c->areas[a];
         DevBuf* bufs[] = {&D.geom, &D.r_point, &D.qw, &D.r_in_mag, &D.r_in_mag2, &D.reff, &D.irv,
-                          &D.ids, &D.nus, &D.r_hi, &D.r_lo, &D.qwv, &D.gmag};
+                          &D.ids, &D.nus, &D.pts};
         for (DevBuf* b : bufs) b->release(t);
     }
     DevBuf* bufs[] = {&c->d_dx, &c->d_glw, &c->s_l, &c->s_b, &c->s_r, &c->s_geom, &c->s_r_point, &c->s_qw,
-                      &c->s_r_in_mag, &c->s_r_in_mag2, &c->s_reff, &c->s_r_hi, &c->s_r_lo, &c->s_qwv,
-                      &c->s_gmag, &c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out};
+                      &c->s_r_in_mag, &c->s_r_in_mag2, &c->s_reff, &c->s_pts, &c->d_theta, &c->d_partials,
+                      &c->d_lkpartials, &c->d_out};
     for (DevBuf* b : bufs) b->release(t);
     c->h_stars.release();
     c->h_theta.release();
@@ -793,8 +817,8 @@ extern "C" int mwsep_ctx_set_problem(mwsep_ctx* c, const ASTRONOMY_PARAMETERS* a
     c->coeff = 1 / (MW_STDEV * sqrt(2 * MW_PI));                     /* :84 */
     if (c->d_dx.ensure((size_t)C * 8, c->dev_bytes) || c->d_glw.ensure((size_t)C * 8, c->dev_bytes))
         return mwsep_fail(MWSEP_ERR_NOMEM);
-    CU(cudaMemcpyAsync(c->d_dx.p, c->dx.data(), (size_t)C * 8, cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(c->d_glw.p, c->gl_w.data(), (size_t)C * 8, cudaMemcpyHostToDevice, c->stream));
+    CU(h2d(c, c->d_dx.p, c->dx.data(), (size_t)C * 8));
+    CU(h2d(c, c->d_glw.p, c->gl_w.data(), (size_t)C * 8));
     for (int a = 0; a < c->prob.n_areas; ++a)
     {
         rc = build_area(c, a);
@@ -883,12 +907,21 @@ extern "C" int mwsep_ctx_last_launches(const mwsep_ctx* c, int* out)
     return MWSEP_OK;
 }
 
+extern "C" int mwsep_ctx_transfer_bytes(const mwsep_ctx* c, size_t* h2d_out, size_t* d2h_out)
+{
+    if (!c || !h2d_out || !d2h_out) return mwsep_fail(MWSEP_ERR_ARG);
+    *h2d_out = c->xfer_h2d;
+    *d2h_out = c->xfer_d2h;
+    return MWSEP_OK;
+}
+
 /* --------------------------------------------------------- EvalFunc path */
 
 namespace {
 
 std::mutex g_default_mu;
 mwsep_ctx* g_default = nullptr;
+size_t g_last_h2d = 0, g_last_d2h = 0;
 
 double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp,
                      int precision)
@@ -908,6 +941,7 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
     }
     /* cpu_evaluate: set_astronomy_parameters (:763), then integrals and
      * likelihood. */
+    const size_t h2d0 = g_default->xfer_h2d, d2h0 = g_default->xfer_d2h;
     if (mwsep_set_astronomy_parameters(ap, parameters) != MWSEP_OK) return nan;
     if (mwsep_ctx_set_problem(g_default, ap) != MWSEP_OK) return nan;
     if (mwsep_ctx_set_stars(g_default, sp) != MWSEP_OK) return nan;
@@ -918,6 +952,8 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
     }
     mwsep_result r;
     if (mwsep_ctx_evaluate(g_default, parameters, precision, &r) != MWSEP_OK) return nan;
+    g_last_h2d = g_default->xfer_h2d - h2d0;
+    g_last_d2h = g_default->xfer_d2h - d2h0;
 
     const int S = ap->number_streams;
     for (int a = 0; a < ap->number_integrals; ++a)
@@ -939,6 +975,15 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
 }
 
 } // namespace
+
+extern "C" int mwsep_evalfunc_transfer_bytes(size_t* h2d_out, size_t* d2h_out)
+{
+    if (!h2d_out || !d2h_out) return mwsep_fail(MWSEP_ERR_ARG);
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    *h2d_out = g_last_h2d;
+    *d2h_out = g_last_d2h;
+    return MWSEP_OK;
+}
 
 extern "C" double mwsep_evaluate(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
                                  STAR_POINTS* sp)

@@ -66,11 +66,9 @@ typedef struct
     const double* reff;      /* [R] reff_xr_rp3 */
     const double* irv;       /* [R] */
     const double* ids;       /* [NU] */
-    /* compensated-FP32 tables */
-    const float* r_hi;       /* [R][C] */
-    const float* r_lo;       /* [R][C] */
-    const float* qwv;        /* [R][C]  qw * reff * irv, rounded once */
-    const float* gmag;       /* [R][C]  r_in_mag (aux only) */
+    /* compensated-FP32 table: per (k, n) {r_hi, r_lo, qw*reff*irv, g}
+     * where r = r_hi + r_lo to ~2^-48 and the weight is rounded once */
+    const float4* pts;       /* [R][C] */
 } mwsep_area_dev;
 
 /* A resident catalogue on the device (tables are [C][N], star-minor). */
@@ -83,10 +81,7 @@ typedef struct
     const double* r_in_mag;  /* [C][N] */
     const double* r_in_mag2; /* [C][N] */
     const double* reff;      /* [N] */
-    const float* r_hi;       /* [C][N] */
-    const float* r_lo;       /* [C][N] */
-    const float* qwv;        /* [C][N]  qw * reff */
-    const float* gmag;       /* [C][N] */
+    const float4* pts;       /* [C][N] {r_hi, r_lo, qw*reff, g} */
 } mwsep_stars_dev;
 
 /* Per-evaluation likelihood sums written by the reduction kernels:
@@ -105,7 +100,20 @@ typedef struct
     int area_index;  /* which area this launch covers */
     int block;       /* threads per block */
     int grid;        /* blocks per theta (gridDim.x) */
+    int bg_form;     /* compensated kernels: the background form this launch
+                        evaluates (thetas of other forms are skipped) */
 } mwsep_launch_shape;
+
+/* Background form of one theta (the compensated kernels specialise on it):
+ * 0 alpha=delta=1, 1 the same plus the aux profile, 2 general alpha/delta,
+ * 3 q == 0. */
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+static inline int mwsep_bg_form(const mwsep_theta_consts* th)
+{
+    return th->bg_mode == 2 ? 3 : th->bg_mode == 1 ? 2 : th->aux ? 1 : 0;
+}
 
 #ifdef __cplusplus
 extern "C" {
@@ -116,7 +124,7 @@ int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps, const dou
 int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
                              const double* dx, const double* gl_w, double coeff, double* geom,
                              double* r_point, double* qw, double* r_in_mag, double* r_in_mag2,
-                             double* reff, float* r_hi, float* r_lo, float* qwv, float* gmag, void* stream);
+                             double* reff, float4* pts, void* stream);
 int mwsep_launch_integral_f64(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                               const mwsep_launch_shape* shape, double2* partials, void* stream);
 int mwsep_launch_likelihood_f64(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
@@ -127,6 +135,9 @@ int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep_theta_cons
 int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
                                 const mwsep_launch_shape* shape, const double* integrals,
                                 double2* partials, void* stream);
+/* Resident blocks per SM of the integral kernels (persistent-grid sizing). */
+int mwsep_integral_f32_blocks_per_sm(int n_streams);
+int mwsep_integral_f64_blocks_per_sm(int n_streams, int block);
 /* Reduce per-block compensated partials of every area into area integrals
  * and subtract the cut areas (cpu/evaluation_optimized.c:584-593):
  * out_areas [n_theta][n_areas][1+S], out_integrals [n_theta][1+S]. */

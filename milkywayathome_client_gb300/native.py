@@ -121,6 +121,11 @@ class mwsep_result(C.Structure):
     ]
 
 
+class mwsep_pipe_peaks(C.Structure):
+    _fields_ = [("fp64_fma_tflops", C.c_double), ("fp32_fma_tflops", C.c_double), ("ex2_gops", C.c_double),
+                ("rsqrt_gops", C.c_double), ("rcp_gops", C.c_double), ("sm_count", C.c_int)]
+
+
 EvalFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.POINTER(ASTRONOMY_PARAMETERS),
                        C.POINTER(EVALUATION_STATE), C.POINTER(STAR_POINTS))
 
@@ -159,6 +164,9 @@ _SIGS = {
     "mwsep_ctx_device_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t)]),
     "mwsep_ctx_last_timings": (C.c_int, [C.c_void_p, _P(C.c_double)]),
     "mwsep_ctx_last_launches": (C.c_int, [C.c_void_p, _P(C.c_int)]),
+    "mwsep_ctx_transfer_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t), _P(C.c_size_t)]),
+    "mwsep_evalfunc_transfer_bytes": (C.c_int, [_P(C.c_size_t), _P(C.c_size_t)]),
+    "mwsep_measure_pipe_peaks": (C.c_int, [C.c_int, _P(mwsep_pipe_peaks)]),
 }
 
 _lib = None
@@ -166,7 +174,8 @@ _lock = threading.Lock()
 
 
 def library_path() -> str:
-    return _build.LIB_PATH
+    """The in-tree library, or MWSEP_LIBRARY when set (a variant build)."""
+    return os.environ.get("MWSEP_LIBRARY") or _build.LIB_PATH
 
 
 def lib(build_if_missing: bool = False):
