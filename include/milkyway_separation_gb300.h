@@ -311,6 +311,63 @@ int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);
 int mwsep_evalfunc_transfer_bytes(size_t* h2d, size_t* d2h);
 
 /* ------------------------------------------------------------------ */
+/* Allocation-free area integral                                        */
+/* ------------------------------------------------------------------ */
+
+/* Device tables of one integral area, in the quantities the reference's
+ * cpu__r_constants and calculate_probabilities use.  All pointers are device
+ * memory owned by the caller; tables are row-major. */
+typedef struct
+{
+    int mu_steps, nu_steps, r_steps, convolve;
+    const double* geom;        /* [mu_steps*nu_steps][4]: sin(b), cos(b), sin(l), cos(l) of each
+                                  (mu, nu) column centre, (l, b) in degrees divided by 180/pi */
+    const double* r_point;     /* [r_steps][convolve] */
+    const double* qw_r3_N;     /* [r_steps][convolve] */
+    const double* r_in_mag;    /* [r_steps][convolve], read only when aux_bg_profile == 1 */
+    const double* r_in_mag2;   /* [r_steps][convolve], read only when aux_bg_profile == 1 */
+    const double* reff_xr_rp3; /* [r_steps] */
+    const double* irv;         /* [r_steps] */
+    const double* ids;         /* [nu_steps] */
+} mwsep_area_tables;
+
+/* The density constants of one evaluation (init_constants' results). */
+typedef struct
+{
+    double alpha, q, r0, delta;
+    int aux_bg_profile;        /* 0 or 1 */
+    double bg_a, bg_b, bg_c;   /* used when aux_bg_profile == 1 */
+    int number_streams;        /* 0 .. MWSEP_MAX_STREAMS */
+    double stream_sigma[MWSEP_MAX_STREAMS];
+    double stream_a[MWSEP_MAX_STREAMS][3];
+    double stream_c[MWSEP_MAX_STREAMS][3];
+} mwsep_density_params;
+
+/* Size of the fixed device array the allocation-free entry point works in. */
+#define MWSEP_NOALLOC_SCRATCH_BYTES (256 * 1024)
+
+/* Plain-FP64 background and stream integrals of one area, written to
+ * d_integrals (device, 1 + number_streams doubles), for callers that cannot
+ * let a library allocate device memory: programs that give all device
+ * memory to their own pool, hot paths where a cudaMalloc would synchronise
+ * the device, loops that must not fail on allocation once running.  No
+ * counterpart in the reference (its evaluators allocate per call).
+ *
+ * The call allocates nothing.  Its only working memory besides the caller's
+ * buffers is a fixed MWSEP_NOALLOC_SCRATCH_BYTES array inside the library
+ * image, which every GPU that loads the library holds until the process
+ * exits.  The first call on a device looks that array up (once per device):
+ * make that first call before any stream capture.  Calls share the array, so
+ * calls that overlap on the GPU (different streams, or threads) race; order
+ * them on one stream.  Work is queued on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream) and the call returns without waiting; the
+ * result is in d_integrals when that stream reaches it.  number_streams above
+ * MWSEP_MAX_STREAMS or convolve above MWSEP_MAX_CONVOLVE is rejected with
+ * MWSEP_ERR_UNSUPPORTED. */
+int mwsep_area_integrals_noalloc(const mwsep_area_tables* tables, const mwsep_density_params* params,
+                                 double* d_integrals, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* Pipe microbenchmark                                                  */
 /* ------------------------------------------------------------------ */
 

@@ -33,6 +33,7 @@ UNITS = [
     ("mwsep_reduce.cu", ["-fmad=false"]),
     ("mwsep_f32.cu", ["-fmad=true"]),
     ("mwsep_peaks.cu", ["-fmad=true"]),
+    ("mwsep_noalloc.cu", ["-fmad=false"]),
     ("mwsep_io.cpp", []),
 ]
 

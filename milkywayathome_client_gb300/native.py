@@ -126,6 +126,23 @@ class mwsep_pipe_peaks(C.Structure):
                 ("rsqrt_gops", C.c_double), ("rcp_gops", C.c_double), ("sm_count", C.c_int)]
 
 
+class mwsep_area_tables(C.Structure):
+    _fields_ = [("mu_steps", C.c_int), ("nu_steps", C.c_int), ("r_steps", C.c_int), ("convolve", C.c_int),
+                ("geom", C.c_void_p), ("r_point", C.c_void_p), ("qw_r3_N", C.c_void_p),
+                ("r_in_mag", C.c_void_p), ("r_in_mag2", C.c_void_p), ("reff_xr_rp3", C.c_void_p),
+                ("irv", C.c_void_p), ("ids", C.c_void_p)]
+
+
+class mwsep_density_params(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("q", C.c_double), ("r0", C.c_double), ("delta", C.c_double),
+                ("aux_bg_profile", C.c_int), ("bg_a", C.c_double), ("bg_b", C.c_double), ("bg_c", C.c_double),
+                ("number_streams", C.c_int), ("stream_sigma", C.c_double * MWSEP_MAX_STREAMS),
+                ("stream_a", (C.c_double * 3) * MWSEP_MAX_STREAMS),
+                ("stream_c", (C.c_double * 3) * MWSEP_MAX_STREAMS)]
+
+
+MWSEP_NOALLOC_SCRATCH_BYTES = 256 * 1024
+
 EvalFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.POINTER(ASTRONOMY_PARAMETERS),
                        C.POINTER(EVALUATION_STATE), C.POINTER(STAR_POINTS))
 
@@ -167,6 +184,8 @@ _SIGS = {
     "mwsep_ctx_transfer_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t), _P(C.c_size_t)]),
     "mwsep_evalfunc_transfer_bytes": (C.c_int, [_P(C.c_size_t), _P(C.c_size_t)]),
     "mwsep_measure_pipe_peaks": (C.c_int, [C.c_int, _P(mwsep_pipe_peaks)]),
+    "mwsep_area_integrals_noalloc": (C.c_int, [_P(mwsep_area_tables), _P(mwsep_density_params), C.c_void_p,
+                                               C.c_void_p]),
 }
 
 _lib = None
