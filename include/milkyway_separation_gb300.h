@@ -302,6 +302,43 @@ int mwsep_ctx_last_timings(const mwsep_ctx* ctx, double* out5);
 /* Number of kernel launches issued by the last evaluate/evaluate_batch. */
 int mwsep_ctx_last_launches(const mwsep_ctx* ctx, int* out);
 
+/* ---- Many resident wedges, one launch per phase for a whole batch ---- */
+
+/* Make another wedge (problem + catalogue) resident; *wedge_id receives its
+ * id.  The single-problem calls above work on wedge 0.  Fails with
+ * MWSEP_ERR_BUDGET when a device-memory budget is set and the wedge would
+ * exceed it. */
+int mwsep_ctx_add_wedge(mwsep_ctx* ctx, const ASTRONOMY_PARAMETERS* ap, const STAR_POINTS* sp, int* wedge_id);
+/* theta length of a resident wedge (negative status on error). */
+int mwsep_ctx_wedge_theta_count(const mwsep_ctx* ctx, int wedge_id);
+/* Device bytes a resident wedge holds (tables + catalogue). */
+int mwsep_ctx_wedge_bytes(const mwsep_ctx* ctx, int wedge_id, size_t* out);
+/* Cap the context's device memory (0 = no cap). */
+int mwsep_ctx_set_hbm_budget(mwsep_ctx* ctx, size_t bytes);
+
+/* One evaluation request: a resident wedge and its parameter vector. */
+typedef struct
+{
+    int wedge;
+    const double* theta;
+} mwsep_request;
+
+/* Evaluate n requests over any resident wedges in `precision`.  All
+ * requests of up to 4 streams run in one persistent launch per phase (5..8
+ * streams in a second), blocks taking (request, area, item-run) tiles from a
+ * global counter; the launch sequence is a captured CUDA graph, replayed
+ * while the batch fits the engine's buffers.  Each result is the same as that
+ * request evaluated alone (its reduction order depends on its wedge's tile
+ * shape only).  out[n]. */
+int mwsep_ctx_evaluate_requests(mwsep_ctx* ctx, int n, const mwsep_request* reqs, int precision, mwsep_result* out);
+
+/* The autotuner: time candidate tile shapes (r-bins per item, items per
+ * tile) for one wedge and precision and keep the fastest; *predicted_ms is
+ * the predicted integral time of one evaluation with the chosen shape. */
+int mwsep_ctx_autotune(mwsep_ctx* ctx, int wedge_id, int precision, double* predicted_ms);
+/* The tile shape a wedge uses for one precision. */
+int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* ctx, int wedge_id, int precision, int* k_chunk, int* tile_items);
+
 /* Bytes the context has copied host->device and device->host since it was
  * created (tables, catalogue, constants, results). */
 int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);

@@ -21,6 +21,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_DIR = os.path.join(PKG_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libmwsep_gb300.so")
+CLIENT_PATH = os.path.join(LIB_DIR, "mwsep_client")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
@@ -34,6 +35,9 @@ UNITS = [
     ("mwsep_f32.cu", ["-fmad=true"]),
     ("mwsep_peaks.cu", ["-fmad=true"]),
     ("mwsep_noalloc.cu", ["-fmad=false"]),
+    ("mwsep_engine.cu", ["-fmad=false"]),
+    ("mwsep_engine_f32.cu", ["-fmad=true"]),
+    ("mwsep_engine_f64.cu", ["-fmad=false"]),
     ("mwsep_io.cpp", []),
 ]
 
@@ -80,6 +84,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: 
     extra_flags / lib_path / build_dir build a variant elsewhere (for tuning
     experiments); the default is the in-tree library the package loads."""
     if not force and not extra_flags and not _sources_newer_than(lib_path):
+        if lib_path == LIB_PATH and not os.path.exists(CLIENT_PATH):
+            _build_client(verbose)
         return lib_path
     os.makedirs(build_dir, exist_ok=True)
     os.makedirs(os.path.dirname(lib_path), exist_ok=True)
@@ -93,7 +99,23 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: 
     if r.returncode != 0:
         raise RuntimeError(f"linking libmwsep_gb300.so failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, lib_path)
+    if lib_path == LIB_PATH:
+        _build_client(verbose)
     return lib_path
+
+
+def _build_client(verbose: bool) -> None:
+    """The C command-line client (csrc/mwsep_client.c) linked against the library."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("a C compiler is required to build mwsep_client")
+    cmd = [cc, "-O2", "-std=gnu99", "-I" + INCLUDE, os.path.join(CSRC, "mwsep_client.c"), "-L" + LIB_DIR,
+           "-lmwsep_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLIENT_PATH]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"building mwsep_client failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

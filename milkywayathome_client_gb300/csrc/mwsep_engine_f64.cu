@@ -1,0 +1,139 @@
+/* mwsep_engine_f64.cu -- plain-FP64 kernels of the tiled engine (same tile
+ * scheme as mwsep_engine_f32.cu; density arithmetic of mwsep_f64_point.cuh,
+ * compiled with -fmad=false). */
+#include <cuda_runtime.h>
+#include "mwsep_internal.h"
+#include "mwsep_reduce.cuh"
+#include "mwsep_f64_point.cuh"
+
+namespace {
+
+using namespace mwsep::f64;
+using mwsep::comp_sum;
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ void load_area(mwsep_area_dev& dst, const mwsep_area_dev* src)
+{
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(mwsep_area_dev) / 8); i += blockDim.x) d[i] = s[i];
+}
+
+template <int NC>
+__device__ __forceinline__ void store_partial(comp_sum (&acc)[NC], int ncomp, double* red, double2* out)
+{
+    mwsep::block_reduce<NC>(acc, red);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+            if (k < ncomp) out[k] = make_double2(acc[k].s, acc[k].c);
+    }
+}
+
+template <int SMAX>
+__device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const mwsep_itile& t,
+                                      double* red, double2* out)
+{
+    comp_sum acc[1 + SMAX];
+#pragma unroll
+    for (int k = 0; k < 1 + SMAX; ++k) acc[k].zero();
+    for (long long item = t.item_begin + threadIdx.x; item < t.item_end; item += blockDim.x)
+        integral_item<SMAX>(A, th, item, acc);
+    store_partial<1 + SMAX>(acc, 1 + th.n_streams, red, out);
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep_engine_args a)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ mwsep_area_dev A;
+    __shared__ double red[2 * (CLS == 0 ? 5 : MWSEP_ENG_ICOMP) * 32];
+    __shared__ int s_tile;
+    const int n_tiles = a.counters[4 * CLS + 2];
+    for (;;)
+    {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 0], 1);
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= n_tiles) break;
+        const mwsep_itile tile = a.itiles[t];
+        load_theta(th, a.thetas + tile.req);
+        load_area(A, a.areas + tile.area_desc);
+        __syncthreads();
+        double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
+        if (CLS == 1) itile<8>(A, th, tile, red, out);
+        else if (th.n_streams <= 1) itile<1>(A, th, tile, red, out);
+        else if (th.n_streams <= 2) itile<2>(A, th, tile, red, out);
+        else itile<4>(A, th, tile, red, out);
+        __syncthreads();
+    }
+}
+
+template <int SMAX>
+__device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_theta_consts& th, const double* I,
+                                      const mwsep_ltile& t, double* red, double2* out)
+{
+    comp_sum acc[3 + SMAX];
+#pragma unroll
+    for (int k = 0; k < 3 + SMAX; ++k) acc[k].zero();
+    for (int s0 = t.star_begin + threadIdx.x; s0 < t.star_end; s0 += blockDim.x)
+        likelihood_star<SMAX>(St, th, I, s0, acc);
+    store_partial<3 + SMAX>(acc, 3 + th.n_streams, red, out);
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(kBlock) engine_likelihood_f64_kernel(const mwsep_engine_args a)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ double red[2 * (CLS == 0 ? 7 : MWSEP_ENG_LCOMP) * 32];
+    __shared__ int s_tile;
+    const int n_tiles = a.counters[4 * CLS + 3];
+    for (;;)
+    {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 1], 1);
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= n_tiles) break;
+        const mwsep_ltile tile = a.ltiles[t];
+        load_theta(th, a.thetas + tile.req);
+        __syncthreads();
+        const mwsep_stars_dev St = a.stars[a.reqs[tile.req].stars];
+        const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
+        double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
+        if (CLS == 1) ltile<8>(St, th, I, tile, red, out);
+        else if (th.n_streams <= 1) ltile<1>(St, th, I, tile, red, out);
+        else if (th.n_streams <= 2) ltile<2>(St, th, I, tile, red, out);
+        else ltile<4>(St, th, I, tile, red, out);
+        __syncthreads();
+    }
+}
+
+} // namespace
+
+extern "C" int mwsep_engine_f64_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (phase == 0 && cls == 0) engine_integral_f64_kernel<0><<<grid, kBlock, 0, st>>>(*a);
+    else if (phase == 0) engine_integral_f64_kernel<1><<<grid, kBlock, 0, st>>>(*a);
+    else if (cls == 0) engine_likelihood_f64_kernel<0><<<grid, kBlock, 0, st>>>(*a);
+    else engine_likelihood_f64_kernel<1><<<grid, kBlock, 0, st>>>(*a);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mwsep_engine_f64_blocks_per_sm(int phase, int cls)
+{
+    int b = 0;
+    cudaError_t e;
+    if (phase == 0 && cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f64_kernel<0>, kBlock, 0);
+    else if (phase == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f64_kernel<1>, kBlock, 0);
+    else if (cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f64_kernel<0>, kBlock, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f64_kernel<1>, kBlock, 0);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return b > 0 ? b : 1;
+}

@@ -1,0 +1,183 @@
+/* mwsep_f64_point.cuh -- the plain-FP64 density evaluation shared by every
+ * FP64 kernel (single evaluation, batches, the tiled engine).
+ *
+ * Every operation of calculate_probabilities
+ * (cpu/evaluation_optimized.c:190-299) in the reference's association order;
+ * translation units that include this compile with -fmad=false (no a*b+c
+ * contraction), with IEEE division and square root.  Per cell the
+ * convolution points are summed in the reference's order n = 0..C-1, then
+ * multiplied by reff_xr_rp3 and by the cell volume V = irv[k]*ids[j]
+ * (:500-504, :513), and cells are Kahan-summed as the reference does.
+ */
+#ifndef MWSEP_F64_POINT_CUH
+#define MWSEP_F64_POINT_CUH
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include "mwsep_internal.h"
+#include "mwsep_reduce.cuh"
+
+namespace mwsep {
+namespace f64 {
+
+using mwsep::comp_sum;
+
+__device__ __forceinline__ void load_theta(mwsep_theta_consts& dst, const mwsep_theta_consts* src)
+{
+    static_assert(sizeof(mwsep_theta_consts) % 8 == 0, "theta consts must be 8-byte sized");
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(mwsep_theta_consts) / 8); i += blockDim.x) d[i] = s[i];
+}
+
+/* The convolution loop of calculate_probabilities for one point (a cell's
+ * r-bin or a star): tables are read at p[n*stride].  Returns bg and st[]
+ * before the reff_xr_rp3 factor. */
+template <int SMAX>
+__device__ __forceinline__ void convolve_f64(const double* __restrict__ rp, const double* __restrict__ qwt,
+                                             const double* __restrict__ gm, const double* __restrict__ gm2,
+                                             size_t stride, int C, double bsin, double bcos, double lsin,
+                                             double lcos, const mwsep_theta_consts& th, double& bg,
+                                             double (&st)[SMAX])
+{
+    const int S = th.n_streams;
+    const double qq = th.q * th.q;
+    bg = (th.bg_mode == 2) ? -1.0 : 0.0;
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) st[s] = 0.0;
+
+    for (int n = 0; n < C; ++n)
+    {
+        const size_t o = (size_t)n * stride;
+        const double r = rp[o];
+        const double qw = qwt[o];
+        const double x2 = r * bsin;
+        const double zp = r * bcos;
+        const double x0 = zp * lcos - MW_LBR_R;
+        const double x1 = zp * lsin;
+        if (th.bg_mode == 0)
+        {
+            const double rg = sqrt(x0 * x0 + x1 * x1 + (x2 * x2) / qq);
+            const double rs = rg + th.r0;
+            if (th.aux)
+            {
+                const double h_prob = qw / (rg * rs * rs * rs);
+                const double aux_prob = qw * (th.bg_a * gm2[o] + th.bg_b * gm[o] + th.bg_c);
+                bg += h_prob + aux_prob;
+            }
+            else
+            {
+                bg += qw / (rg * rs * rs * rs);
+            }
+        }
+        else if (th.bg_mode == 1)
+        {
+            const double rg = sqrt(x0 * x0 + x1 * x1 + (x2 * x2) / qq);
+            bg += qw / (pow(rg, th.alpha) * pow(rg + th.r0, th.alpha_delta3));
+        }
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s)
+        {
+            if (s < S && th.stream_on[s])
+            {
+                double d0 = x0 - th.c[s][0];
+                double d1 = x1 - th.c[s][1];
+                double d2 = x2 - th.c[s][2];
+                const double dotted = th.a[s][0] * d0 + th.a[s][1] * d1 + th.a[s][2] * d2;
+                d0 = d0 - dotted * th.a[s][0];
+                d1 = d1 - dotted * th.a[s][1];
+                d2 = d2 - dotted * th.a[s][2];
+                const double norm = d0 * d0 + d1 * d1 + d2 * d2;
+                st[s] += qw * exp(-norm / th.sigma_sq2[s]);
+            }
+        }
+    }
+}
+
+/* One item of an integral (a column and its run of r-bins): Kahan-adds
+ * each cell's bg*V and st*V into acc (cpu/evaluation_optimized.c:498-520). */
+template <int SMAX>
+__device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mwsep_theta_consts& th,
+                                              long long item, comp_sum (&acc)[1 + SMAX])
+{
+    const int S = th.n_streams;
+    const int C = A.convolve;
+    const int kc = (int)(item / A.n_cols);
+    const int col = (int)(item - (long long)kc * A.n_cols);
+    const int j = col % A.nu_steps;
+    const double* g = A.geom + 4 * (size_t)col;
+    const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
+    const double idsj = A.ids[j];
+    const int k0 = kc * A.k_chunk;
+    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    for (int k = k0; k < k1; ++k)
+    {
+        const double V = A.irv[k] * idsj;
+        double bg, st[SMAX];
+        const size_t row = (size_t)k * C;
+        convolve_f64<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, 1, C, bsin, bcos,
+                           lsin, lcos, th, bg, st);
+        const double rf = A.reff[k];
+        if (th.bg_mode != 2) bg *= rf;
+        bg *= V;
+        acc[0].add(bg);
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s)
+        {
+            if (s < S)
+            {
+                double v = st[s];
+                if (th.stream_on[s]) v *= rf;
+                v *= V;
+                acc[1 + s].add(v);
+            }
+        }
+    }
+}
+
+/* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717).
+ * acc slots: [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
+template <int SMAX>
+__device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
+                                                const double* I, int s0, comp_sum (&acc)[3 + SMAX])
+{
+    const int S = th.n_streams;
+    const int N = St.n_stars;
+    const double* g = St.geom + 4 * (size_t)s0;
+    double bg, st[SMAX];
+    convolve_f64<SMAX>(St.r_point + s0, St.qw + s0, St.r_in_mag + s0, St.r_in_mag2 + s0, (size_t)N, St.convolve,
+                       g[0], g[1], g[2], g[3], th, bg, st);
+    const double rf = St.reff[s0];
+    if (th.bg_mode != 2) bg *= rf;
+
+    double bg_only = (bg / I[0]) * th.exp_bg_weight;
+    double star_prob = bg_only;
+    bg_only = (bg_only == 0.0) ? -238.0 : log10(bg_only / th.sum_exp_weights);
+    acc[2].add(bg_only);
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s)
+    {
+        if (s < S)
+        {
+            double v = st[s];
+            if (th.stream_on[s]) v *= rf;
+            double st_only = v / I[1 + s] * th.exp_stream_weight[s];
+            star_prob += st_only;
+            st_only = (st_only == 0.0) ? -238.0 : log10(st_only / th.sum_exp_weights);
+            acc[3 + s].add(st_only);
+        }
+    }
+    star_prob /= th.sum_exp_weights;
+    if (star_prob != 0.0)
+        acc[0].add(log10(star_prob));
+    else
+    {
+        acc[0].add(-238.0);
+        acc[1].add(1.0);
+    }
+}
+
+} // namespace f64
+} // namespace mwsep
+
+#endif

@@ -17,16 +17,17 @@
  */
 #include <cuda_runtime.h>
 #include <math.h>
-#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
 #include <mutex>
+#include <new>
 #include <vector>
 
 #include "milkyway_separation_gb300.h"
+#include "mwsep_ctx.h"
 #include "mwsep_geometry.cuh"
 #include "mwsep_internal.h"
 #include "mwsep_status.h"
@@ -64,98 +65,77 @@ extern "C" const char* mwsep_status_string(int s)
 
 extern "C" const char* mwsep_version(void) { return "libmwsep_gb300 1.0 (sm_103a)"; }
 
-#define CU(call)                                                                                           \
-    do                                                                                                     \
-    {                                                                                                      \
-        cudaError_t e_ = (call);                                                                           \
-        if (e_ != cudaSuccess)                                                                             \
-        {                                                                                                  \
-            if (getenv("MWSEP_DEBUG"))                                                                     \
-                fprintf(stderr, "mwsep: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), __FILE__, \
-                        __LINE__);                                                                         \
-            return mwsep_fail(MWSEP_ERR_CUDA);                                                             \
-        }                                                                                                  \
-    } while (0)
-
-#define CK(expr)                                                                                           \
-    do                                                                                                     \
-    {                                                                                                      \
-        int s_ = (expr);                                                                                   \
-        if (s_ != 0)                                                                                       \
-        {                                                                                                  \
-            if (getenv("MWSEP_DEBUG"))                                                                     \
-                fprintf(stderr, "mwsep: %s failed: %d (%s:%d)\n", #expr, s_, __FILE__, __LINE__);          \
-            return mwsep_fail(MWSEP_ERR_CUDA);                                                             \
-        }                                                                                                  \
-    } while (0)
+namespace mwsep {
 
 /* --------------------------------------------------------- device memory */
 
+int DevBuf::ensure(size_t want, size_t& total)
+{
+    if (want <= bytes) return MWSEP_OK;
+    if (p)
+    {
+        cudaFree(p);
+        total -= bytes;
+        p = nullptr;
+        bytes = 0;
+    }
+    if (want == 0) return MWSEP_OK;
+    if (cudaMalloc(&p, want) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return MWSEP_ERR_NOMEM;
+    }
+    bytes = want;
+    total += bytes;
+    return MWSEP_OK;
+}
+
+void DevBuf::release(size_t& total)
+{
+    if (p)
+    {
+        cudaFree(p);
+        total -= bytes;
+    }
+    p = nullptr;
+    bytes = 0;
+}
+
+int HostPinned::ensure(size_t want)
+{
+    if (want <= bytes) return MWSEP_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaMallocHost(&p, want) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return MWSEP_ERR_NOMEM;
+    }
+    bytes = want;
+    return MWSEP_OK;
+}
+
+void HostPinned::release()
+{
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+/* cudaMemcpyAsync with transfer accounting */
+cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    c->xfer_h2d += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+}
+cudaError_t d2h(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    c->xfer_d2h += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+}
+
 namespace {
-
-struct DevBuf
-{
-    void* p = nullptr;
-    size_t bytes = 0;
-    int ensure(size_t want, size_t& total)
-    {
-        if (want <= bytes) return MWSEP_OK;
-        if (p)
-        {
-            cudaFree(p);
-            total -= bytes;
-            p = nullptr;
-            bytes = 0;
-        }
-        if (want == 0) return MWSEP_OK;
-        if (cudaMalloc(&p, want) != cudaSuccess)
-        {
-            cudaGetLastError();
-            return MWSEP_ERR_NOMEM;
-        }
-        bytes = want;
-        total += bytes;
-        return MWSEP_OK;
-    }
-    void release(size_t& total)
-    {
-        if (p)
-        {
-            cudaFree(p);
-            total -= bytes;
-        }
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T* as() const { return (T*)p; }
-};
-
-struct HostPinned
-{
-    void* p = nullptr;
-    size_t bytes = 0;
-    int ensure(size_t want)
-    {
-        if (want <= bytes) return MWSEP_OK;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        if (cudaMallocHost(&p, want) != cudaSuccess)
-        {
-            cudaGetLastError();
-            return MWSEP_ERR_NOMEM;
-        }
-        bytes = want;
-        return MWSEP_OK;
-    }
-    void release()
-    {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T* as() const { return (T*)p; }
-};
 
 /* numericalIntegration.c:67-104 (Numerical Recipes gauleg on [-1, 1]). */
 void gauss_legendre(int n, double* x, double* w)
@@ -188,93 +168,7 @@ void gauss_legendre(int n, double* x, double* w)
     }
 }
 
-/* Host description of one integral area. */
-struct AreaHost
-{
-    int mu_steps, nu_steps, r_steps;
-    double mu_min, mu_max, nu_min, nu_max, r_min, r_max;
-    double mu_step, nu_step, r_step;
-};
-
-struct AreaDev
-{
-    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, pts;
-    mwsep_area_dev view{};
-};
-
-/* The theta layout and the fixed values of the problem (a private copy of
- * the reference struct's values). */
-struct ProblemHost
-{
-    int n_bg = 0, n_streams = 0, n_sparams = 0;
-    double bg_weight = 0.0;
-    double bg[MWSEP_MAX_BG_PARAMS] = {};
-    int bg_opt[MWSEP_MAX_BG_PARAMS] = {};
-    double st_weight[MWSEP_MAX_STREAMS] = {};
-    int st_weight_opt[MWSEP_MAX_STREAMS] = {};
-    double st[MWSEP_MAX_STREAMS][MWSEP_MAX_STREAM_PARAMS] = {};
-    int st_opt[MWSEP_MAX_STREAMS][MWSEP_MAX_STREAM_PARAMS] = {};
-    int convolve = 0, sgr = 0, aux = 0, wedge = 0;
-    int n_areas = 0;
-    AreaHost area[MWSEP_MAX_AREAS];
-    int n_theta = 0;
-};
-
-/* Launch tuning of one precision. */
-struct Tune
-{
-    int block = 256;
-    int grid = 0;
-    int k_chunk = 0;
-    int lk_block = 256;
-    int lk_grid = 0;
-};
-
 } // namespace
-
-struct mwsep_ctx
-{
-    int device = 0;
-    int sm_count = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
-    size_t dev_bytes = 0;
-
-    bool has_problem = false;
-    ProblemHost prob;
-    std::vector<double> gl_x, gl_w, dx;
-    double coeff = 0.0;
-    AreaDev areas[MWSEP_MAX_AREAS];
-    DevBuf d_dx, d_glw;
-
-    bool has_stars = false;
-    int n_stars = 0;
-    DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_pts;
-    mwsep_stars_dev stars_view{};
-    HostPinned h_stars;
-
-    DevBuf d_theta, d_partials, d_lkpartials, d_out;
-    HostPinned h_theta, h_out;
-
-    Tune tune[2];
-    double last_ms[5] = {};
-    int last_launches = 0;
-    size_t xfer_h2d = 0, xfer_d2h = 0;
-};
-
-namespace {
-
-/* cudaMemcpyAsync with transfer accounting */
-cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
-{
-    c->xfer_h2d += bytes;
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
-}
-cudaError_t d2h(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
-{
-    c->xfer_d2h += bytes;
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
-}
 
 int check_problem(const ASTRONOMY_PARAMETERS* ap)
 {
@@ -298,6 +192,8 @@ int check_problem(const ASTRONOMY_PARAMETERS* ap)
     }
     return MWSEP_OK;
 }
+
+namespace {
 
 /* Copy the reference struct's values into the context's private copy. */
 void copy_problem(const ASTRONOMY_PARAMETERS* ap, ProblemHost& p)
@@ -355,6 +251,8 @@ void copy_problem(const ASTRONOMY_PARAMETERS* ap, ProblemHost& p)
     p.n_theta = n;
 }
 
+} // namespace
+
 /* theta -> constants: set_astronomy_parameters (cpu/parameters.c:332-363),
  * init_constants (cpu/evaluation_optimized.c:54-133) and the likelihood
  * weights (:639-646). */
@@ -407,6 +305,8 @@ void theta_consts(const ProblemHost& base, const double* theta, mwsep_theta_cons
     th.sum_exp_weights = sum * 0.001;
 }
 
+namespace {
+
 int occupancy_grid(mwsep_ctx* c, int block, long long items)
 {
     long long g = (items + block - 1) / block;
@@ -416,21 +316,23 @@ int occupancy_grid(mwsep_ctx* c, int block, long long items)
     return (int)g;
 }
 
+} // namespace
+
 long env_long(const char* name, long dflt)
 {
     const char* v = getenv(name);
     return (v && *v) ? strtol(v, nullptr, 10) : dflt;
 }
 
-/* Default launch shapes for the resident problem.  The shape depends only
- * on the problem, never on the batch, so a theta gives the same bits alone
- * and inside any batch.  Integral kernels run a persistent grid (resident
- * blocks per SM x SMs); items (column x r-run) are sized so each thread gets
- * many, which keeps the static tail short.  MWSEP_TUNE_{KCHUNK,GRID_F32,
- * GRID_F64} override the choice (the autotuner's search space). */
-void default_tune(mwsep_ctx* c)
+/* Default launch shapes for a resident wedge.  The shape depends only on the
+ * wedge, never on the batch, so a theta gives the same bits alone and inside
+ * any batch.  Grid-stride kernels run a persistent grid (resident blocks per
+ * SM x SMs); items (column x r-run) are sized so each thread gets ~48, which
+ * keeps the static tail near 2%.  The engine uses the same items, in tiles of
+ * tile_items.  MWSEP_TUNE_{KCHUNK,GRID_F32,GRID_F64} override the choice. */
+void default_tune(mwsep_ctx* c, Wedge& w)
 {
-    const ProblemHost& p = c->prob;
+    const ProblemHost& p = w.prob;
     long long max_cols = 0;
     int max_r = 1;
     for (int a = 0; a < p.n_areas; ++a)
@@ -440,14 +342,11 @@ void default_tune(mwsep_ctx* c)
     }
     for (int prec = 0; prec < 2; ++prec)
     {
-        Tune& t = c->tune[prec];
+        Tune& t = w.tune[prec];
         t.block = 256;
         const int per_sm = prec == MWSEP_PLAIN_F64 ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
                                                    : mwsep_integral_f32_blocks_per_sm(p.n_streams);
         const long long threads = (long long)c->sm_count * per_sm * t.block;
-        /* ~48 items per thread keeps the static tail of the grid-stride
-         * loop near 2%; the compensated kernel's FP64 column prologue per
-         * item stays a few percent of its work at that length */
         const long long want_items = threads * 48;
         long long chunks = (want_items + max_cols - 1) / std::max<long long>(max_cols, 1);
         chunks = std::max<long long>(1, std::min<long long>(chunks, max_r));
@@ -458,15 +357,20 @@ void default_tune(mwsep_ctx* c)
         g = env_long(prec == MWSEP_PLAIN_F64 ? "MWSEP_TUNE_GRID_F64" : "MWSEP_TUNE_GRID_F32", g);
         t.grid = (int)std::max<long long>(1, g);
         t.lk_block = 256;
-        t.lk_grid = occupancy_grid(c, t.lk_block, std::max(c->n_stars, 1));
+        t.lk_grid = occupancy_grid(c, t.lk_block, std::max(w.n_stars, 1));
+        t.tile_items = t.block * 8;
+        t.tile_stars = 1024;
+        t.tuned = false;
     }
 }
 
-int build_area(mwsep_ctx* c, int a)
+namespace {
+
+int build_area(mwsep_ctx* c, Wedge& w, int a)
 {
-    const ProblemHost& p = c->prob;
+    const ProblemHost& p = w.prob;
     const AreaHost& A = p.area[a];
-    AreaDev& D = c->areas[a];
+    AreaDev& D = w.areas[a];
     const int R = A.r_steps, C = p.convolve, NU = A.nu_steps;
     const size_t RC = (size_t)R * C;
 
@@ -486,7 +390,7 @@ int build_area(mwsep_ctx* c, int a)
         {
             const size_t o = (size_t)i * C + n;
             double g;
-            mwsep::prob_consts_point(gPrime, c->dx[n], c->gl_w[n], c->coeff, g, rp[o], qw[o]);
+            mwsep::prob_consts_point(gPrime, w.dx[n], w.gl_w[n], w.coeff, g, rp[o], qw[o]);
             gm[o] = g;
             gm2[o] = g * g;
             const float hi = (float)rp[o];
@@ -502,6 +406,7 @@ int build_area(mwsep_ctx* c, int a)
 
     const size_t cols = (size_t)A.mu_steps * NU;
     size_t& tot = c->dev_bytes;
+    const size_t before = tot;
     int rc = 0;
     rc |= D.geom.ensure(cols * 4 * sizeof(double), tot);
     rc |= D.r_point.ensure(RC * 8, tot);
@@ -513,6 +418,7 @@ int build_area(mwsep_ctx* c, int a)
     rc |= D.ids.ensure(NU * 8, tot);
     rc |= D.nus.ensure(NU * 8, tot);
     rc |= D.pts.ensure(RC * sizeof(float4), tot);
+    w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
 
     cudaStream_t st = c->stream;
@@ -548,6 +454,8 @@ int build_area(mwsep_ctx* c, int a)
     return MWSEP_OK;
 }
 
+} // namespace
+
 void set_chunking(mwsep_area_dev& v, int k_chunk)
 {
     v.k_chunk = std::max(1, std::min(k_chunk, v.r_steps));
@@ -555,58 +463,138 @@ void set_chunking(mwsep_area_dev& v, int k_chunk)
     v.n_items = (long long)v.n_cols * v.n_kchunks;
 }
 
-int upload_stars(mwsep_ctx* c, int n, const double* l, const double* b, const double* r)
+int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r)
 {
-    if (!c->has_problem) return mwsep_fail(MWSEP_ERR_STATE);
+    if (!w.has_problem) return mwsep_fail(MWSEP_ERR_STATE);
     if (n < 1) return mwsep_fail(MWSEP_ERR_ARG);
-    const int C = c->prob.convolve;
+    const int C = w.prob.convolve;
     const size_t NC = (size_t)n * C;
     size_t& tot = c->dev_bytes;
+    const size_t before = tot;
     int rc = 0;
-    rc |= c->s_l.ensure((size_t)n * 8, tot);
-    rc |= c->s_b.ensure((size_t)n * 8, tot);
-    rc |= c->s_r.ensure((size_t)n * 8, tot);
-    rc |= c->s_geom.ensure((size_t)n * 32, tot);
-    rc |= c->s_r_point.ensure(NC * 8, tot);
-    rc |= c->s_qw.ensure(NC * 8, tot);
-    rc |= c->s_r_in_mag.ensure(NC * 8, tot);
-    rc |= c->s_r_in_mag2.ensure(NC * 8, tot);
-    rc |= c->s_reff.ensure((size_t)n * 8, tot);
-    rc |= c->s_pts.ensure(NC * sizeof(float4), tot);
+    rc |= w.s_l.ensure((size_t)n * 8, tot);
+    rc |= w.s_b.ensure((size_t)n * 8, tot);
+    rc |= w.s_r.ensure((size_t)n * 8, tot);
+    rc |= w.s_geom.ensure((size_t)n * 32, tot);
+    rc |= w.s_r_point.ensure(NC * 8, tot);
+    rc |= w.s_qw.ensure(NC * 8, tot);
+    rc |= w.s_r_in_mag.ensure(NC * 8, tot);
+    rc |= w.s_r_in_mag2.ensure(NC * 8, tot);
+    rc |= w.s_reff.ensure((size_t)n * 8, tot);
+    rc |= w.s_pts.ensure(NC * sizeof(float4), tot);
+    w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
     cudaStream_t st = c->stream;
-    CU(h2d(c, c->s_l.p, l, (size_t)n * 8));
-    CU(h2d(c, c->s_b.p, b, (size_t)n * 8));
-    CU(h2d(c, c->s_r.p, r, (size_t)n * 8));
-    CK(mwsep_launch_star_tables(n, c->s_l.as<double>(), c->s_b.as<double>(), c->s_r.as<double>(), C,
-                                c->d_dx.as<double>(), c->d_glw.as<double>(), c->coeff, c->s_geom.as<double>(),
-                                c->s_r_point.as<double>(), c->s_qw.as<double>(), c->s_r_in_mag.as<double>(),
-                                c->s_r_in_mag2.as<double>(), c->s_reff.as<double>(), c->s_pts.as<float4>(), st));
-    mwsep_stars_dev& v = c->stars_view;
+    CU(h2d(c, w.s_l.p, l, (size_t)n * 8));
+    CU(h2d(c, w.s_b.p, b, (size_t)n * 8));
+    CU(h2d(c, w.s_r.p, r, (size_t)n * 8));
+    CK(mwsep_launch_star_tables(n, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(), C,
+                                w.d_dx.as<double>(), w.d_glw.as<double>(), w.coeff, w.s_geom.as<double>(),
+                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
+                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
+    mwsep_stars_dev& v = w.stars_view;
     v.n_stars = n;
     v.convolve = C;
-    v.geom = c->s_geom.as<double>();
-    v.r_point = c->s_r_point.as<double>();
-    v.qw = c->s_qw.as<double>();
-    v.r_in_mag = c->s_r_in_mag.as<double>();
-    v.r_in_mag2 = c->s_r_in_mag2.as<double>();
-    v.reff = c->s_reff.as<double>();
-    v.pts = c->s_pts.as<float4>();
-    c->n_stars = n;
-    c->has_stars = true;
+    v.geom = w.s_geom.as<double>();
+    v.r_point = w.s_r_point.as<double>();
+    v.qw = w.s_qw.as<double>();
+    v.r_in_mag = w.s_r_in_mag.as<double>();
+    v.r_in_mag2 = w.s_r_in_mag2.as<double>();
+    v.reff = w.s_reff.as<double>();
+    v.pts = w.s_pts.as<float4>();
+    w.n_stars = n;
+    w.has_stars = true;
     for (int prec = 0; prec < 2; ++prec)
-        c->tune[prec].lk_grid = occupancy_grid(c, c->tune[prec].lk_block, n);
+        w.tune[prec].lk_grid = occupancy_grid(c, w.tune[prec].lk_block, n);
     return MWSEP_OK;
 }
 
+int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp)
+{
+    if (!sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
+    const int n = sp->number_stars;
+    if (w.h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
+    double* l = w.h_stars.as<double>();
+    double* b = l + n;
+    double* r = b + n;
+    for (int i = 0; i < n; ++i)
+    {
+        const double* row = sp->stars[i];
+        if (!row) return mwsep_fail(MWSEP_ERR_ARG);
+        l[i] = row[0];
+        b[i] = row[1];
+        r[i] = row[2];
+    }
+    int rc = wedge_set_stars(c, w, n, l, b, r);
+    if (rc) return rc;
+    /* the pinned staging buffer is reused: wait for the copies */
+    CU(cudaStreamSynchronize(c->stream));
+    return MWSEP_OK;
+}
+
+int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap)
+{
+    int rc = check_problem(ap);
+    if (rc) return mwsep_fail(rc);
+    const int old_convolve = w.has_problem ? w.prob.convolve : -1;
+    copy_problem(ap, w.prob);
+    w.has_problem = false;
+    const int C = w.prob.convolve;
+    w.gl_x.assign(C, 0.0);
+    w.gl_w.assign(C, 0.0);
+    w.dx.assign(C, 0.0);
+    gauss_legendre(C, w.gl_x.data(), w.gl_w.data());
+    for (int i = 0; i < C; ++i) w.dx[i] = 3 * MW_STDEV * w.gl_x[i]; /* evaluation_optimized.c:131 */
+    w.coeff = 1 / (MW_STDEV * sqrt(2 * MW_PI));                      /* :84 */
+    const size_t before = c->dev_bytes;
+    if (w.d_dx.ensure((size_t)C * 8, c->dev_bytes) || w.d_glw.ensure((size_t)C * 8, c->dev_bytes))
+        return mwsep_fail(MWSEP_ERR_NOMEM);
+    w.bytes += c->dev_bytes - before;
+    CU(h2d(c, w.d_dx.p, w.dx.data(), (size_t)C * 8));
+    CU(h2d(c, w.d_glw.p, w.gl_w.data(), (size_t)C * 8));
+    for (int a = 0; a < w.prob.n_areas; ++a)
+    {
+        rc = build_area(c, w, a);
+        if (rc) return rc;
+    }
+    /* a catalogue built for another convolve count is stale */
+    if (old_convolve != C) w.has_stars = false;
+    w.has_problem = true;
+    default_tune(c, w);
+    c->eng.desc_dirty = true;
+    return MWSEP_OK;
+}
+
+void wedge_release(mwsep_ctx* c, Wedge& w)
+{
+    size_t& t = c->dev_bytes;
+    for (int a = 0; a < MWSEP_MAX_AREAS; ++a)
+    {
+        AreaDev& D = w.areas[a];
+        DevBuf* bufs[] = {&D.geom, &D.r_point, &D.qw, &D.r_in_mag, &D.r_in_mag2, &D.reff, &D.irv,
+                          &D.ids, &D.nus, &D.pts};
+        for (DevBuf* b : bufs) b->release(t);
+    }
+    DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
+                      &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts};
+    for (DevBuf* b : bufs) b->release(t);
+    w.h_stars.release();
+    w.bytes = 0;
+    w.has_problem = w.has_stars = false;
+}
+
+namespace {
+
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out)
 {
-    if (!c->has_problem || !c->has_stars) return mwsep_fail(MWSEP_ERR_STATE);
+    if (c->wedges.empty() || !c->wedges[0]->has_problem || !c->wedges[0]->has_stars)
+        return mwsep_fail(MWSEP_ERR_STATE);
+    Wedge& w = *c->wedges[0];
     if (B < 1 || B > 65535 || !thetas || !out) return mwsep_fail(MWSEP_ERR_ARG);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
-    const ProblemHost& p = c->prob;
+    const ProblemHost& p = w.prob;
     const int S = p.n_streams, A = p.n_areas, P = p.n_theta;
-    const Tune& t = c->tune[precision];
+    const Tune& t = w.tune[precision];
     const int ncomp = 1 + S, nslots = 3 + S;
 
     size_t& tot = c->dev_bytes;
@@ -648,7 +636,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     sh.bg_form = 0;
     for (int a = 0; a < A; ++a)
     {
-        mwsep_area_dev v = c->areas[a].view;
+        mwsep_area_dev v = w.areas[a].view;
         set_chunking(v, t.k_chunk);
         sh.area_index = a;
         if (precision == MWSEP_PLAIN_F64)
@@ -678,10 +666,10 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     lk.grid = t.lk_grid;
     lk.area_index = 0;
     if (precision == MWSEP_PLAIN_F64)
-        CK(mwsep_launch_likelihood_f64(&c->stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+        CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
     else
-        CK(mwsep_launch_likelihood_f32(&c->stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+        CK(mwsep_launch_likelihood_f32(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
     ++launches;
     CU(cudaEventRecord(c->ev[4], st));
@@ -707,7 +695,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     const double* h_areas = c->h_out.as<double>();
     const double* h_ints = h_areas + (size_t)B * A * ncomp;
     const double* h_lk = h_ints + (size_t)B * ncomp;
-    const double N = (double)c->n_stars;
+    const double N = (double)w.n_stars;
     for (int i = 0; i < B; ++i)
     {
         mwsep_result& r = out[i];
@@ -731,7 +719,21 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     return MWSEP_OK;
 }
 
+Wedge* wedge0(mwsep_ctx* c)
+{
+    if (c->wedges.empty())
+    {
+        Wedge* w = new (std::nothrow) Wedge();
+        if (!w) return nullptr;
+        c->wedges.push_back(w);
+    }
+    return c->wedges[0];
+}
+
 } // namespace
+} // namespace mwsep
+
+using namespace mwsep;
 
 /* ------------------------------------------------------------ public API */
 
@@ -772,24 +774,23 @@ extern "C" int mwsep_ctx_create(int device, mwsep_ctx** out)
     return MWSEP_OK;
 }
 
+extern "C" void mwsep_engine_release(mwsep_ctx* c);
+
 extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
 {
     if (!c) return mwsep_fail(MWSEP_ERR_ARG);
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    size_t& t = c->dev_bytes;
-    for (int a = 0; a < MWSEP_MAX_AREAS; ++a)
+    mwsep_engine_release(c);
+    for (Wedge* w : c->wedges)
     {
-        AreaDev& D = c->areas[a];
-        DevBuf* bufs[] = {&D.geom, &D.r_point, &D.qw, &D.r_in_mag, &D.r_in_mag2, &D.reff, &D.irv,
-                          &D.ids, &D.nus, &D.pts};
-        for (DevBuf* b : bufs) b->release(t);
+        wedge_release(c, *w);
+        delete w;
     }
-    DevBuf* bufs[] = {&c->d_dx, &c->d_glw, &c->s_l, &c->s_b, &c->s_r, &c->s_geom, &c->s_r_point, &c->s_qw,
-                      &c->s_r_in_mag, &c->s_r_in_mag2, &c->s_reff, &c->s_pts, &c->d_theta, &c->d_partials,
-                      &c->d_lkpartials, &c->d_out};
+    c->wedges.clear();
+    size_t& t = c->dev_bytes;
+    DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out};
     for (DevBuf* b : bufs) b->release(t);
-    c->h_stars.release();
     c->h_theta.release();
     c->h_out.release();
     for (int i = 0; i < 6; ++i)
@@ -802,41 +803,20 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
 extern "C" int mwsep_ctx_set_problem(mwsep_ctx* c, const ASTRONOMY_PARAMETERS* ap)
 {
     if (!c || !ap) return mwsep_fail(MWSEP_ERR_ARG);
-    int rc = check_problem(ap);
-    if (rc) return mwsep_fail(rc);
     CU(cudaSetDevice(c->device));
-    const int old_convolve = c->has_problem ? c->prob.convolve : -1;
-    copy_problem(ap, c->prob);
-    c->has_problem = false;
-    const int C = c->prob.convolve;
-    c->gl_x.assign(C, 0.0);
-    c->gl_w.assign(C, 0.0);
-    c->dx.assign(C, 0.0);
-    gauss_legendre(C, c->gl_x.data(), c->gl_w.data());
-    for (int i = 0; i < C; ++i) c->dx[i] = 3 * MW_STDEV * c->gl_x[i]; /* :131 */
-    c->coeff = 1 / (MW_STDEV * sqrt(2 * MW_PI));                     /* :84 */
-    if (c->d_dx.ensure((size_t)C * 8, c->dev_bytes) || c->d_glw.ensure((size_t)C * 8, c->dev_bytes))
-        return mwsep_fail(MWSEP_ERR_NOMEM);
-    CU(h2d(c, c->d_dx.p, c->dx.data(), (size_t)C * 8));
-    CU(h2d(c, c->d_glw.p, c->gl_w.data(), (size_t)C * 8));
-    for (int a = 0; a < c->prob.n_areas; ++a)
-    {
-        rc = build_area(c, a);
-        if (rc) return rc;
-    }
-    /* a catalogue built for another convolve count is stale */
-    if (old_convolve != C) c->has_stars = false;
-    c->has_problem = true;
-    default_tune(c);
-    return MWSEP_OK;
+    Wedge* w = wedge0(c);
+    if (!w) return mwsep_fail(MWSEP_ERR_NOMEM);
+    return wedge_set_problem(c, *w, ap);
 }
 
 extern "C" int mwsep_ctx_set_stars_soa(mwsep_ctx* c, int n, const double* l, const double* b, const double* r)
 {
     if (!c || !l || !b || !r) return mwsep_fail(MWSEP_ERR_ARG);
     CU(cudaSetDevice(c->device));
-    int rc = upload_stars(c, n, l, b, r);
+    if (c->wedges.empty()) return mwsep_fail(MWSEP_ERR_STATE);
+    int rc = wedge_set_stars(c, *c->wedges[0], n, l, b, r);
     if (rc) return rc;
+    c->eng.desc_dirty = true;
     CU(cudaStreamSynchronize(c->stream));
     return MWSEP_OK;
 }
@@ -845,30 +825,17 @@ extern "C" int mwsep_ctx_set_stars(mwsep_ctx* c, const STAR_POINTS* sp)
 {
     if (!c || !sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
     CU(cudaSetDevice(c->device));
-    const int n = sp->number_stars;
-    if (c->h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
-    double* l = c->h_stars.as<double>();
-    double* b = l + n;
-    double* r = b + n;
-    for (int i = 0; i < n; ++i)
-    {
-        const double* row = sp->stars[i];
-        if (!row) return mwsep_fail(MWSEP_ERR_ARG);
-        l[i] = row[0];
-        b[i] = row[1];
-        r[i] = row[2];
-    }
-    int rc = upload_stars(c, n, l, b, r);
+    if (c->wedges.empty()) return mwsep_fail(MWSEP_ERR_STATE);
+    int rc = wedge_set_stars_rows(c, *c->wedges[0], sp);
     if (rc) return rc;
-    /* the pinned staging buffer is reused: wait for the copies */
-    CU(cudaStreamSynchronize(c->stream));
+    c->eng.desc_dirty = true;
     return MWSEP_OK;
 }
 
 extern "C" int mwsep_ctx_theta_count(const mwsep_ctx* c)
 {
-    if (!c || !c->has_problem) return -mwsep_fail(MWSEP_ERR_STATE);
-    return c->prob.n_theta;
+    if (!c || c->wedges.empty() || !c->wedges[0]->has_problem) return -mwsep_fail(MWSEP_ERR_STATE);
+    return c->wedges[0]->prob.n_theta;
 }
 
 extern "C" int mwsep_ctx_evaluate(mwsep_ctx* c, const double* theta, int precision, mwsep_result* out)

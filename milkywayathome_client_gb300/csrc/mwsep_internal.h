@@ -115,9 +115,82 @@ static inline int mwsep_bg_form(const mwsep_theta_consts* th)
     return th->bg_mode == 2 ? 3 : th->bg_mode == 1 ? 2 : th->aux ? 1 : 0;
 }
 
+/* ---- tiled engine: many requests over many resident wedges ---- */
+
+/* Components of one integral tile partial and one likelihood tile partial. */
+#define MWSEP_ENG_ICOMP (1 + MWSEP_KMAX_STREAMS)
+#define MWSEP_ENG_LCOMP (3 + MWSEP_KMAX_STREAMS)
+/* Per-request output block: area integrals [MWSEP_MAX_AREAS][ICOMP], the
+ * cut-subtracted integrals [ICOMP], the likelihood sums [LCOMP]. */
+#define MWSEP_ENG_OUT_AREAS 0
+#define MWSEP_ENG_OUT_INTS (MWSEP_MAX_AREAS * MWSEP_ENG_ICOMP)
+#define MWSEP_ENG_OUT_LK (MWSEP_ENG_OUT_INTS + MWSEP_ENG_ICOMP)
+#define MWSEP_ENG_OUT_STRIDE (MWSEP_ENG_OUT_LK + MWSEP_ENG_LCOMP)
+
+/* One request of an engine batch. */
+typedef struct
+{
+    int n_streams;                        /* S of its wedge */
+    int n_areas;                          /* integral areas of its wedge */
+    int stars;                            /* index of its catalogue descriptor */
+    int pad0;
+    int area_slot[MWSEP_MAX_AREAS + 1];   /* integral tiles of area a: [area_slot[a], area_slot[a+1]) */
+    int lk_slot0, lk_slot1;               /* likelihood tiles: [lk_slot0, lk_slot1) */
+} mwsep_req_dev;
+
+/* A run of items of one area for one request (an integral tile). */
+typedef struct
+{
+    int req;
+    int area_desc;       /* index into the area descriptors */
+    long long item_begin;
+    long long item_end;
+} mwsep_itile;
+
+/* A run of stars for one request (a likelihood tile). */
+typedef struct
+{
+    int req;
+    int star_begin;
+    int star_end;
+    int pad0;
+} mwsep_ltile;
+
+/* Requests are split into two kernel classes: up to 4 streams (class 0,
+ * the common case, specialised per stream count) and 5..8 streams
+ * (class 1).  Device-side counters of one engine launch, per class c:
+ * [4c+0] next integral tile, [4c+1] next likelihood tile, [4c+2] end of the
+ * class's integral tiles, [4c+3] end of its likelihood tiles; [8] requests.
+ * A class's tiles are contiguous and start where its "next" counters start. */
+#define MWSEP_ENG_COUNTERS 12
+#define MWSEP_ENG_NREQ 8
+
+typedef struct
+{
+    const mwsep_area_dev* areas;
+    const mwsep_stars_dev* stars;
+    const mwsep_req_dev* reqs;
+    const mwsep_theta_consts* thetas;     /* one per request */
+    const mwsep_itile* itiles;
+    const mwsep_ltile* ltiles;
+    double2* ipart;                       /* [itiles][ICOMP] */
+    double2* lpart;                       /* [ltiles][LCOMP] */
+    double* out;                          /* [requests][OUT_STRIDE] */
+    int* counters;
+} mwsep_engine_args;
+
 #ifdef __cplusplus
 extern "C" {
 #endif
+/* Engine launchers: persistent grids (grid = resident blocks x SMs). */
+/* phase 0: integrals, 1: likelihood; cls: 0 (<= 4 streams) or 1 (5..8) */
+int mwsep_engine_f32_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream);
+int mwsep_engine_f64_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream);
+int mwsep_engine_f32_blocks_per_sm(int phase, int cls);
+int mwsep_engine_f64_blocks_per_sm(int phase, int cls);
+/* per-request fixed-order reductions: phase 0 integrals (+ cut
+ * subtraction), phase 1 likelihood */
+int mwsep_engine_reduce(int phase, const mwsep_engine_args* a, int grid, void* stream);
 /* Launchers (defined in the .cu files).  All return cudaError_t as int. */
 int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps, const double* nus, int nu_steps,
                           int sgr, int wedge, double* geom_out, void* stream);

@@ -86,3 +86,81 @@ extern "C" int mwsep_launch_reduce_likelihood(const double2* partials, const mws
                                                                                       3 + sh->n_streams, out);
     return (int)cudaGetLastError();
 }
+
+/* ---- tiled engine: per-request fixed-order reductions ---- */
+
+namespace {
+
+/* Sum the tile partials [t0, t1) (stride `stride`, component c) of one
+ * request in a fixed order: thread-strided, then the block tree. */
+__device__ double sum_tiles(const double2* part, int stride, int c, int t0, int t1, double* red)
+{
+    comp_sum acc[1];
+    acc[0].zero();
+    for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x)
+    {
+        const double2 v = part[(size_t)t * stride + c];
+        acc[0].merge(v.x, v.y);
+    }
+    mwsep::block_reduce<1>(acc, red);
+    double r = acc[0].s + acc[0].c;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) engine_reduce_integrals_kernel(const mwsep_engine_args a)
+{
+    __shared__ double red[2 * 32];
+    const int n_req = a.counters[MWSEP_ENG_NREQ];
+    for (int r = blockIdx.x; r < n_req; r += gridDim.x)
+    {
+        const mwsep_req_dev q = a.reqs[r];
+        const int ncomp = 1 + q.n_streams;
+        double* out = a.out + (size_t)r * MWSEP_ENG_OUT_STRIDE;
+        for (int ar = 0; ar < q.n_areas; ++ar)
+            for (int c = 0; c < ncomp; ++c)
+            {
+                const double v = sum_tiles(a.ipart, MWSEP_ENG_ICOMP, c, q.area_slot[ar], q.area_slot[ar + 1], red);
+                if (threadIdx.x == 0) out[MWSEP_ENG_OUT_AREAS + ar * MWSEP_ENG_ICOMP + c] = v;
+            }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            /* cpu/evaluation_optimized.c:584-593 */
+            for (int c = 0; c < ncomp; ++c)
+            {
+                double I = out[MWSEP_ENG_OUT_AREAS + c];
+                for (int ar = 1; ar < q.n_areas; ++ar) I -= out[MWSEP_ENG_OUT_AREAS + ar * MWSEP_ENG_ICOMP + c];
+                out[MWSEP_ENG_OUT_INTS + c] = I;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kReduceThreads) engine_reduce_likelihood_kernel(const mwsep_engine_args a)
+{
+    __shared__ double red[2 * 32];
+    const int n_req = a.counters[MWSEP_ENG_NREQ];
+    for (int r = blockIdx.x; r < n_req; r += gridDim.x)
+    {
+        const mwsep_req_dev q = a.reqs[r];
+        double* out = a.out + (size_t)r * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_LK;
+        for (int c = 0; c < 3 + q.n_streams; ++c)
+        {
+            const double v = sum_tiles(a.lpart, MWSEP_ENG_LCOMP, c, q.lk_slot0, q.lk_slot1, red);
+            if (threadIdx.x == 0) out[c] = v;
+        }
+    }
+}
+
+} // namespace
+
+extern "C" int mwsep_engine_reduce(int phase, const mwsep_engine_args* a, int grid, void* stream)
+{
+    if (phase == 0)
+        engine_reduce_integrals_kernel<<<grid, kReduceThreads, 0, (cudaStream_t)stream>>>(*a);
+    else
+        engine_reduce_likelihood_kernel<<<grid, kReduceThreads, 0, (cudaStream_t)stream>>>(*a);
+    return (int)cudaGetLastError();
+}

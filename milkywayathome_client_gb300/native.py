@@ -143,6 +143,10 @@ class mwsep_density_params(C.Structure):
 
 MWSEP_NOALLOC_SCRATCH_BYTES = 256 * 1024
 
+
+class mwsep_request(C.Structure):
+    _fields_ = [("wedge", C.c_int), ("theta", C.POINTER(C.c_double))]
+
 EvalFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.POINTER(ASTRONOMY_PARAMETERS),
                        C.POINTER(EVALUATION_STATE), C.POINTER(STAR_POINTS))
 
@@ -182,6 +186,14 @@ _SIGS = {
     "mwsep_ctx_last_timings": (C.c_int, [C.c_void_p, _P(C.c_double)]),
     "mwsep_ctx_last_launches": (C.c_int, [C.c_void_p, _P(C.c_int)]),
     "mwsep_ctx_transfer_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t), _P(C.c_size_t)]),
+    "mwsep_ctx_add_wedge": (C.c_int, [C.c_void_p, _P(ASTRONOMY_PARAMETERS), _P(STAR_POINTS), _P(C.c_int)]),
+    "mwsep_ctx_wedge_theta_count": (C.c_int, [C.c_void_p, C.c_int]),
+    "mwsep_ctx_wedge_bytes": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_size_t)]),
+    "mwsep_ctx_set_hbm_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "mwsep_ctx_evaluate_requests": (C.c_int, [C.c_void_p, C.c_int, _P(mwsep_request), C.c_int,
+                                              _P(mwsep_result)]),
+    "mwsep_ctx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_double)]),
+    "mwsep_ctx_wedge_tile_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int)]),
     "mwsep_evalfunc_transfer_bytes": (C.c_int, [_P(C.c_size_t), _P(C.c_size_t)]),
     "mwsep_measure_pipe_peaks": (C.c_int, [C.c_int, _P(mwsep_pipe_peaks)]),
     "mwsep_area_integrals_noalloc": (C.c_int, [_P(mwsep_area_tables), _P(mwsep_density_params), C.c_void_p,

@@ -345,6 +345,50 @@ class Context:
         return {"integral_ms": a[0], "integral_reduce_ms": a[1], "likelihood_ms": a[2],
                 "likelihood_reduce_ms": a[3], "total_ms": a[4]}
 
+    # ---- many resident wedges (the tiled engine) ----
+    def add_wedge(self, ap: AstronomyParameters, sp: StarPoints) -> int:
+        wid = C.c_int()
+        N.check(N.lib().mwsep_ctx_add_wedge(self._h, C.byref(ap.struct), C.byref(sp.struct), C.byref(wid)),
+                "add_wedge")
+        return wid.value
+
+    def wedge_theta_count(self, wedge: int) -> int:
+        return N.lib().mwsep_ctx_wedge_theta_count(self._h, wedge)
+
+    def wedge_bytes(self, wedge: int) -> int:
+        v = C.c_size_t()
+        N.check(N.lib().mwsep_ctx_wedge_bytes(self._h, wedge, C.byref(v)))
+        return v.value
+
+    def set_hbm_budget(self, nbytes: int) -> None:
+        N.check(N.lib().mwsep_ctx_set_hbm_budget(self._h, nbytes))
+
+    def evaluate_requests(self, requests, precision: int = N.MWSEP_PLAIN_F64) -> List[Result]:
+        """requests: sequence of (wedge_id, theta)."""
+        keep = []
+        arr = (N.mwsep_request * len(requests))()
+        for i, (w, t) in enumerate(requests):
+            a = np.ascontiguousarray(t, dtype=np.float64)
+            if a.size != self.wedge_theta_count(w):
+                raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "evaluate_requests")
+            keep.append(a)
+            arr[i].wedge = w
+            arr[i].theta = _dptr(a)
+        out = (N.mwsep_result * len(requests))()
+        N.check(N.lib().mwsep_ctx_evaluate_requests(self._h, len(requests), arr, precision, out),
+                "evaluate_requests")
+        return [Result.from_c(out[i]) for i in range(len(requests))]
+
+    def autotune(self, wedge: int, precision: int) -> float:
+        ms = C.c_double()
+        N.check(N.lib().mwsep_ctx_autotune(self._h, wedge, precision, C.byref(ms)), "autotune")
+        return ms.value
+
+    def tile_shape(self, wedge: int, precision: int):
+        kc, ti = C.c_int(), C.c_int()
+        N.check(N.lib().mwsep_ctx_wedge_tile_shape(self._h, wedge, precision, C.byref(kc), C.byref(ti)))
+        return kc.value, ti.value
+
     def last_launches(self) -> int:
         v = C.c_int()
         N.check(N.lib().mwsep_ctx_last_launches(self._h, C.byref(v)))

@@ -132,3 +132,23 @@ def test_against_live_oracle(gpu_ctx, oracle_built, name):
     assert _close_abs(r.background_only_likelihood, want["background_only_likelihood"], 1e-12)
     for x, y in zip(r.stream_only_likelihood, want["stream_only_likelihood"]):
         assert _close_abs(x, y, 1e-12)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_c_client_matches_reference(built_library, mixed):
+    """The C command-line client (worker() on the C ABI) prints the
+    reference's result lines with the reference's numbers."""
+    import re
+    import subprocess
+    from milkywayathome_client_gb300 import build
+    pf, sf, g = load_case("cut_area")
+    cmd = [build.CLIENT_PATH, "-a", pf, "-p", sf] + (["--mixed"] if mixed else []) + \
+        [repr(float(x)) for x in g["theta"]]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    ll = float(re.search(r"<search_likelihood> (\S+) </search_likelihood>", r.stderr).group(1))
+    bg = float(re.search(r"<background_integral> (\S+) </background_integral>", r.stderr).group(1))
+    assert abs(ll - g["likelihood"]) <= (ABS_LOGL_F32 if mixed else ABS_LOGL_F64)
+    if not mixed:
+        # printed with %.20lf: compare at the printed precision
+        assert abs(bg - g["background_integral"]) <= max(1e-12 * abs(g["background_integral"]), 1e-20)
