@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the population-batch and serving measurements")
     ap.add_argument("--data-dir", default=os.path.join(tempfile.gettempdir(), "mwsep_bench_data"))
     return ap.parse_args()
 
@@ -354,6 +356,11 @@ def run_gb300_arm(args, ws, rank, local):
     }
     if clk:
         out["clocks"] = clk
+    if rank == 0 and not args.no_extras:
+        ctx.close()
+        ctx = None
+        out["population_batch"] = population_batch(args)
+        out["serving"] = serving(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         n = min(host_cores(), 64)
         cw, kind, _ = cpu_sample(files, theta, n)
@@ -361,9 +368,48 @@ def run_gb300_arm(args, ws, rank, local):
         out["cpu_baseline"] = {"value": cv, "unit": "evals/s", "cores": n, "kind": kind,
                                "sample": f"{n} concurrent 1/{CPU_SLICES} slices of the evaluation "
                                          f"(reference rank slicing of cells and stars), {cw:.1f} s wall"}
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def population_batch(args):
+    """256 parameter vectors on one wedge (400 x 160 x 140, convolve 60,
+    3 streams, 50k stars) evaluated as one engine batch, compensated FP32."""
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import synthetic as syn
+    m = syn.materialise(2, os.path.join(args.data_dir, "population"))
+    f = m["files"][0]
+    thetas = m["thetas"]
+    with mw.Context(0) as ctx:
+        wid = ctx.add_wedge(mw.AstronomyParameters.read(f["params"]), mw.StarPoints.read(f["stars"]))
+        ctx.autotune(wid, mw.MWSEP_MIXED_F32)
+        reqs = [(wid, t) for t in thetas]
+        ctx.evaluate_requests(reqs, mw.MWSEP_MIXED_F32)
+        times = []
+        for _ in range(3):
+            res = ctx.evaluate_requests(reqs, mw.MWSEP_MIXED_F32)
+            times.append(ctx.last_timings()["total_ms"])
+        launches = ctx.last_launches()
+        plain = ctx.evaluate_requests(reqs[:4], mw.MWSEP_PLAIN_F64)
+        plain_ms = ctx.last_timings()["total_ms"]
+    ms = statistics.median(times)
+    return {"workload": "256 parameter vectors, 400x160x140 cells, convolve 60, 3 streams, 50k stars",
+            "value": len(thetas) / (ms * 1e-3), "unit": "evals/s", "ms_per_batch": ms,
+            "launches_per_batch": launches, "graph": True,
+            "plain_f64_evals_per_s": 4 / (plain_ms * 1e-3),
+            "max_dlogL_mixed_vs_plain": max(abs(a.likelihood - b.likelihood) for a, b in zip(res[:4], plain))}
+
+
+def serving(args):
+    """Poisson arrivals over the 6 mixed-size wedges, compensated FP32."""
+    from milkywayathome_client_gb300 import native as N
+    from milkywayathome_client_gb300 import serve_bench
+    res = serve_bench.run([50.0, 200.0], 3.0, N.MWSEP_MIXED_F32, 2, 256,
+                          os.path.join(args.data_dir, "serving"))
+    return {"workload": "Poisson arrivals over 6 resident wedges (log-uniform sizes), wedge chosen by star count",
+            "lanes": 2, "precision": "mixed", "results": res}
 
 
 def main():

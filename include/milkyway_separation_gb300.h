@@ -339,6 +339,43 @@ int mwsep_ctx_autotune(mwsep_ctx* ctx, int wedge_id, int precision, double* pred
 /* The tile shape a wedge uses for one precision. */
 int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* ctx, int wedge_id, int precision, int* k_chunk, int* tile_items);
 
+/* ---- Serving: continuous batching over the resident wedges ---- */
+
+typedef struct mwsep_server mwsep_server;
+
+typedef struct
+{
+    int lanes;             /* execution lanes (own stream + engine buffers each); default 2 */
+    int max_batch;         /* requests per engine batch; default 256 */
+    size_t lane_hbm_bytes; /* device-memory share of each lane's batch buffers (0 = no cap);
+                              a batch that would exceed it is split until it fits */
+} mwsep_server_config;
+
+typedef struct
+{
+    long long completed, failed, cancelled, batches, queued;
+    double mean_batch;
+    double p50_latency_s, p99_latency_s, max_latency_s; /* submit -> result */
+    double evals_per_s;                                 /* completed / (last result - first submit) */
+} mwsep_server_stats;
+
+/* Start serving the wedges resident in ctx (add them first; the server
+ * snapshots the set).  cfg may be NULL for the defaults.  While the server
+ * runs, ctx itself must not evaluate or change its wedges. */
+int mwsep_server_create(mwsep_ctx* ctx, const mwsep_server_config* cfg, mwsep_server** out);
+/* Queue one evaluation; returns at once with its id. */
+int mwsep_server_submit(mwsep_server* s, int wedge_id, const double* theta, int precision, unsigned long long* id);
+/* Wait up to timeout_s for a request's result (MWSEP_ERR_TIMEOUT when the
+ * time runs out; the request stays pending and can be waited on again). */
+int mwsep_server_wait(mwsep_server* s, unsigned long long id, double timeout_s, mwsep_result* out);
+/* Cancel a request that has not started; its wait returns MWSEP_ERR_CANCELLED.
+ * A request already on the GPU cannot be cancelled (MWSEP_ERR_STATE). */
+int mwsep_server_cancel(mwsep_server* s, unsigned long long id);
+int mwsep_server_get_stats(mwsep_server* s, mwsep_server_stats* out);
+int mwsep_server_reset_stats(mwsep_server* s);
+/* Stop: queued requests are cancelled, running batches finish. */
+int mwsep_server_destroy(mwsep_server* s);
+
 /* Bytes the context has copied host->device and device->host since it was
  * created (tables, catalogue, constants, results). */
 int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);

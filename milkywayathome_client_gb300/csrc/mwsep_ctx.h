@@ -127,7 +127,8 @@ struct Wedge
     HostPinned h_stars;
 
     Tune tune[2];
-    size_t bytes = 0; /* device bytes this wedge holds */
+    unsigned tune_gen = 0; /* bumped whenever tune[] changes */
+    size_t bytes = 0;      /* device bytes this wedge holds */
 };
 
 /* Buffers and graph of the tiled engine (mwsep_engine.cu). */
@@ -137,7 +138,8 @@ struct EngineState
     HostPinned h_areas, h_stars, h_reqs, h_itiles, h_ltiles, h_theta, h_out, h_counters;
     bool desc_dirty = true;
     int n_area_desc = 0, n_star_desc = 0;
-    std::vector<int> area_base; /* first area descriptor of each wedge */
+    std::vector<int> area_base;     /* first area descriptor of each wedge */
+    std::vector<unsigned> seen_gen; /* wedge tune generations the descriptors reflect */
     /* the captured graph of the last request shape */
     cudaGraphExec_t graph = nullptr;
     long long graph_key[5] = {-1, -1, -1, -1, -1};
@@ -156,6 +158,7 @@ struct mwsep_ctx
     size_t hbm_budget = 0; /* 0: no budget */
 
     std::vector<mwsep::Wedge*> wedges;
+    bool shared_wedges = false; /* a serving lane: wedges belong to the parent context */
 
     /* single-problem path (wedge 0) */
     mwsep::DevBuf d_theta, d_partials, d_lkpartials, d_out;

@@ -62,8 +62,11 @@ void invalidate_graph(EngineState& e)
 int ensure_descriptors(mwsep_ctx* c)
 {
     EngineState& e = c->eng;
-    if (!e.desc_dirty) return MWSEP_OK;
     const int W = (int)c->wedges.size();
+    if (!e.desc_dirty && (int)e.seen_gen.size() == W)
+        for (int w = 0; w < W; ++w)
+            if (e.seen_gen[w] != c->wedges[w]->tune_gen) e.desc_dirty = true;
+    if (!e.desc_dirty && (int)e.seen_gen.size() == W) return MWSEP_OK;
     e.area_base.assign(W, 0);
     int na = 0;
     for (int w = 0; w < W; ++w)
@@ -101,6 +104,8 @@ int ensure_descriptors(mwsep_ctx* c)
     CU(cudaStreamSynchronize(c->stream));
     e.n_area_desc = na;
     e.n_star_desc = W;
+    e.seen_gen.assign(W, 0);
+    for (int w = 0; w < W; ++w) e.seen_gen[w] = c->wedges[w]->tune_gen;
     e.desc_dirty = false;
     return MWSEP_OK;
 }
@@ -557,6 +562,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
             t = saved;
             t.k_chunk = kc;
             t.tile_items = t.block * tm;
+            ++w.tune_gen;
             c->eng.desc_dirty = true;
             int rc = ensure_descriptors(c);
             if (rc) return rc;
@@ -587,6 +593,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
     }
     w.tune[precision] = best_t;
     w.tune[precision].tuned = true;
+    ++w.tune_gen;
     c->eng.desc_dirty = true;
     invalidate_graph(c->eng);
     if (predicted_ms) *predicted_ms = best < 1e299 ? best : -1.0;

@@ -362,6 +362,7 @@ void default_tune(mwsep_ctx* c, Wedge& w)
         t.tile_stars = 1024;
         t.tuned = false;
     }
+    ++w.tune_gen;
 }
 
 namespace {
@@ -782,11 +783,12 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     mwsep_engine_release(c);
-    for (Wedge* w : c->wedges)
-    {
-        wedge_release(c, *w);
-        delete w;
-    }
+    if (!c->shared_wedges)
+        for (Wedge* w : c->wedges)
+        {
+            wedge_release(c, *w);
+            delete w;
+        }
     c->wedges.clear();
     size_t& t = c->dev_bytes;
     DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out};
@@ -800,9 +802,22 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     return MWSEP_OK;
 }
 
+/* A serving lane: a context on the parent's device with its own stream and
+ * engine state that shares (does not own) the parent's resident wedges. */
+extern "C" mwsep_ctx* mwsep_ctx_lane(mwsep_ctx* parent)
+{
+    if (!parent) return nullptr;
+    mwsep_ctx* c = nullptr;
+    if (mwsep_ctx_create(parent->device, &c) != MWSEP_OK) return nullptr;
+    c->wedges = parent->wedges;
+    c->shared_wedges = true;
+    return c;
+}
+
 extern "C" int mwsep_ctx_set_problem(mwsep_ctx* c, const ASTRONOMY_PARAMETERS* ap)
 {
     if (!c || !ap) return mwsep_fail(MWSEP_ERR_ARG);
+    if (c->shared_wedges) return mwsep_fail(MWSEP_ERR_STATE);
     CU(cudaSetDevice(c->device));
     Wedge* w = wedge0(c);
     if (!w) return mwsep_fail(MWSEP_ERR_NOMEM);

@@ -144,6 +144,17 @@ class mwsep_density_params(C.Structure):
 MWSEP_NOALLOC_SCRATCH_BYTES = 256 * 1024
 
 
+class mwsep_server_config(C.Structure):
+    _fields_ = [("lanes", C.c_int), ("max_batch", C.c_int), ("lane_hbm_bytes", C.c_size_t)]
+
+
+class mwsep_server_stats(C.Structure):
+    _fields_ = [("completed", C.c_longlong), ("failed", C.c_longlong), ("cancelled", C.c_longlong),
+                ("batches", C.c_longlong), ("queued", C.c_longlong), ("mean_batch", C.c_double),
+                ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double),
+                ("evals_per_s", C.c_double)]
+
+
 class mwsep_request(C.Structure):
     _fields_ = [("wedge", C.c_int), ("theta", C.POINTER(C.c_double))]
 
@@ -194,6 +205,13 @@ _SIGS = {
                                               _P(mwsep_result)]),
     "mwsep_ctx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_double)]),
     "mwsep_ctx_wedge_tile_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int)]),
+    "mwsep_server_create": (C.c_int, [C.c_void_p, _P(mwsep_server_config), _P(C.c_void_p)]),
+    "mwsep_server_submit": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double), C.c_int, _P(C.c_ulonglong)]),
+    "mwsep_server_wait": (C.c_int, [C.c_void_p, C.c_ulonglong, C.c_double, _P(mwsep_result)]),
+    "mwsep_server_cancel": (C.c_int, [C.c_void_p, C.c_ulonglong]),
+    "mwsep_server_get_stats": (C.c_int, [C.c_void_p, _P(mwsep_server_stats)]),
+    "mwsep_server_reset_stats": (C.c_int, [C.c_void_p]),
+    "mwsep_server_destroy": (C.c_int, [C.c_void_p]),
     "mwsep_evalfunc_transfer_bytes": (C.c_int, [_P(C.c_size_t), _P(C.c_size_t)]),
     "mwsep_measure_pipe_peaks": (C.c_int, [C.c_int, _P(mwsep_pipe_peaks)]),
     "mwsep_area_integrals_noalloc": (C.c_int, [_P(mwsep_area_tables), _P(mwsep_density_params), C.c_void_p,

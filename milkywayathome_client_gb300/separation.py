@@ -393,3 +393,61 @@ class Context:
         v = C.c_int()
         N.check(N.lib().mwsep_ctx_last_launches(self._h, C.byref(v)))
         return v.value
+
+
+class Server:
+    """Continuous-batching server over a context's resident wedges
+    (mwsep_server_*).  Add the wedges to the context first."""
+
+    def __init__(self, ctx: Context, lanes: int = 2, max_batch: int = 256, lane_hbm_bytes: int = 0):
+        cfg = N.mwsep_server_config(lanes, max_batch, lane_hbm_bytes)
+        self._h = C.c_void_p()
+        self._ctx = ctx
+        N.check(N.lib().mwsep_server_create(ctx._h, C.byref(cfg), C.byref(self._h)), "server_create")
+
+    def submit(self, wedge: int, theta, precision: int = N.MWSEP_MIXED_F32) -> int:
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        if t.size != self._ctx.wedge_theta_count(wedge):
+            raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "submit")
+        rid = C.c_ulonglong()
+        N.check(N.lib().mwsep_server_submit(self._h, wedge, _dptr(t), precision, C.byref(rid)), "submit")
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = 60.0) -> Result:
+        r = N.mwsep_result()
+        N.check(N.lib().mwsep_server_wait(self._h, rid, timeout, C.byref(r)), "wait")
+        return Result.from_c(r)
+
+    def try_wait(self, rid: int, timeout: float):
+        """(status, Result or None) without raising."""
+        r = N.mwsep_result()
+        st = N.lib().mwsep_server_wait(self._h, rid, timeout, C.byref(r))
+        return st, (Result.from_c(r) if st == N.MWSEP_OK else None)
+
+    def cancel(self, rid: int) -> int:
+        return N.lib().mwsep_server_cancel(self._h, rid)
+
+    def stats(self) -> dict:
+        st = N.mwsep_server_stats()
+        N.check(N.lib().mwsep_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in N.mwsep_server_stats._fields_}
+
+    def reset_stats(self) -> None:
+        N.check(N.lib().mwsep_server_reset_stats(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            N.lib().mwsep_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -40,6 +40,7 @@ def test_struct_layouts_match_c(tmp_path, built_library):
         "INTEGRAL_AREA": N.INTEGRAL_AREA, "EVALUATION_STATE": N.EVALUATION_STATE, "mwsep_result": N.mwsep_result,
         "mwsep_pipe_peaks": N.mwsep_pipe_peaks, "mwsep_area_tables": N.mwsep_area_tables,
         "mwsep_density_params": N.mwsep_density_params, "mwsep_request": N.mwsep_request,
+        "mwsep_server_config": N.mwsep_server_config, "mwsep_server_stats": N.mwsep_server_stats,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():

@@ -1,0 +1,91 @@
+"""GPU: the serving loop.  Requests submitted concurrently from several
+client threads are batched on the fly over two lanes; every result must be
+bit-identical to the same request evaluated alone.  Host-side fault
+injection: a request cancelled while queued, a bounded wait that runs out.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import load_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["three_streams", "cut_area", "config0", "four_streams_c120"]
+
+
+@pytest.fixture(scope="module")
+def served(built_library):
+    import milkywayathome_client_gb300 as mw
+    ctx = mw.Context(0)
+    wedges, keep = [], []
+    for name in CASES:
+        pf, sf, g = load_case(name)
+        ap, sp = mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf)
+        keep.append((ap, sp))
+        wedges.append((ctx.add_wedge(ap, sp), np.asarray(g["theta"])))
+    yield ctx, wedges
+    ctx.close()
+
+
+def _workload(wedges, n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        w, base = wedges[rng.integers(len(wedges))]
+        out.append((w, base * (1.0 + 0.002 * rng.standard_normal(base.size)), int(rng.integers(2))))
+    return out
+
+
+def test_served_results_equal_alone(served):
+    import milkywayathome_client_gb300 as mw
+    ctx, wedges = served
+    work = _workload(wedges, 48, 11)
+    alone = [ctx.evaluate_requests([(w, t)], p)[0] for w, t, p in work]
+    with mw.Server(ctx, lanes=2, max_batch=16) as srv:
+        ids = [None] * len(work)
+
+        def client(k):
+            for i in range(k, len(work), 4):
+                w, t, p = work[i]
+                ids[i] = srv.submit(w, t, p)
+
+        ths = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        got = [srv.wait(i, timeout=300) for i in ids]
+        st = srv.stats()
+    for a, b in zip(alone, got):
+        assert a.likelihood == b.likelihood or (a.likelihood != a.likelihood and b.likelihood != b.likelihood)
+        assert a.integrals == b.integrals
+    assert st["completed"] == len(work)
+    assert st["batches"] <= len(work)
+    assert 0 < st["p50_latency_s"] <= st["p99_latency_s"] <= st["max_latency_s"]
+
+
+def test_cancel_and_timeout(served):
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    ctx, wedges = served
+    w, base = wedges[2]  # config 0: ~1.5 ms per FP64 evaluation
+    with mw.Server(ctx, lanes=1, max_batch=1) as srv:
+        ids = [srv.submit(w, base, mw.MWSEP_PLAIN_F64) for _ in range(40)]
+        last = ids[-1]
+        rc = srv.cancel(last)
+        st, res = srv.try_wait(last, 60.0)
+        if rc == N.MWSEP_OK:
+            assert st == N.MWSEP_ERR_CANCELLED and res is None
+        else:  # it had already started
+            assert rc == N.MWSEP_ERR_STATE and st == N.MWSEP_OK
+        # a wait that cannot be satisfied in time returns TIMEOUT and the
+        # request stays pending
+        fresh = srv.submit(w, base, mw.MWSEP_PLAIN_F64)
+        st0, _ = srv.try_wait(fresh, 0.0)
+        assert st0 in (N.MWSEP_ERR_TIMEOUT, N.MWSEP_OK)
+        if st0 == N.MWSEP_ERR_TIMEOUT:
+            assert srv.wait(fresh, 300).likelihood == srv.wait(ids[0], 300).likelihood
+        for i in ids[1:-1]:
+            srv.wait(i, 300)
