@@ -385,6 +385,47 @@ int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);
 int mwsep_evalfunc_transfer_bytes(size_t* h2d, size_t* d2h);
 
 /* ------------------------------------------------------------------ */
+/* Separation output                                                    */
+/* ------------------------------------------------------------------ */
+
+/* Totals of one separation (milkyway_separation/cpu/separation.c:37-254). */
+typedef struct
+{
+    int number_streams;
+    double likelihood;                            /* of the evaluation behind it */
+    double background_integral;
+    double stream_integrals[MWSEP_MAX_STREAMS];
+    double expected[MWSEP_MAX_STREAMS];           /* sum over stars of sprob (:193-196) */
+    long long assigned[MWSEP_MAX_STREAMS];        /* stars drawn into each stream */
+    long long background_assigned;                /* stars drawn into the background */
+} mwsep_separation_summary;
+
+/* Separate wedge 0's catalogue at theta: replaces the per-star loop of
+ * separation() (cpu/separation.c:150-234), which the reference builds no
+ * more.  Evaluates the integrals (plain FP64), then per star:
+ *   sprob[N][S]      psg_s / (sum psg + pbx), with epsilon_s = e^{w_s} /
+ *                    (1 + sum e^{w}), epsilon_b = 1 / (1 + sum e^{w}) (:128-196);
+ *   assignment[N]    0 for the background, k for stream k (1-based), drawn
+ *                    against the cumulative sprob (probability.c:310-397 prob_ok);
+ *                    the draw is SplitMix64(seed, star) / 2^53 instead of the
+ *                    reference's clock-seeded drand48, so it repeats for a seed;
+ *   xyz[N][3]        the star in the stripe frame: lbr -> xyz, to (l, b,
+ *                    magnitude - 11), back to xyz, shifted by the Sun, rotated
+ *                    by mwsep_stripe_transform (:75-116, :226-227).
+ * Any output may be NULL.  Up to MWSEP_MAX_STREAMS streams. */
+int mwsep_ctx_separation(mwsep_ctx* ctx, const double* theta, unsigned long long seed, double* sprob,
+                         int* assignment, double* xyz, mwsep_separation_summary* summary);
+
+/* The stripe-frame rotation (row-major 3x3) taking the stripe's normal onto
+ * the z axis: stripe_normal or sgr_stripe_normal (cpu/stCoords.c:142-174),
+ * then get_transform (cpu/stVector.c:109-137).  Host only. */
+int mwsep_stripe_transform(int sgr_coordinates, int wedge, double* mat9);
+
+/* Write separation()'s output file (cpu/separation.c:229): one line
+ * "<stream> <x> <y> <z>" per star, stream 0 for the background. */
+int mwsep_write_separation(const char* path, int n, const int* assignment, const double* xyz);
+
+/* ------------------------------------------------------------------ */
 /* Allocation-free area integral                                        */
 /* ------------------------------------------------------------------ */
 

@@ -7,7 +7,8 @@ interface.
 """
 from .native import (MWSEP_MIXED_F32, MWSEP_PLAIN_F64, MwsepError)  # noqa: F401
 from .separation import (AstronomyParameters, Context, EvaluationState, Result,  # noqa: F401
-                         Server, StarPoints, evaluate, evaluate_mixed)
+                         Server, StarPoints, evaluate, evaluate_mixed, stripe_transform,
+                         write_separation)
 
 __all__ = ["AstronomyParameters", "StarPoints", "EvaluationState", "Context", "Result", "Server",
-           "evaluate", "evaluate_mixed", "MWSEP_PLAIN_F64", "MWSEP_MIXED_F32", "MwsepError"]
+           "evaluate", "evaluate_mixed", "stripe_transform", "write_separation", "MWSEP_PLAIN_F64", "MWSEP_MIXED_F32", "MwsepError"]

@@ -38,6 +38,7 @@ UNITS = [
     ("mwsep_engine.cu", ["-fmad=false"]),
     ("mwsep_engine_f32.cu", ["-fmad=true"]),
     ("mwsep_engine_f64.cu", ["-fmad=false"]),
+    ("mwsep_separation.cu", ["-fmad=false"]),
     ("mwsep_io.cpp", []),
     ("mwsep_server.cpp", []),
 ]

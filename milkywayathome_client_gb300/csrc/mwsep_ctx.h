@@ -163,6 +163,9 @@ struct mwsep_ctx
     /* single-problem path (wedge 0) */
     mwsep::DevBuf d_theta, d_partials, d_lkpartials, d_out;
     mwsep::HostPinned h_theta, h_out;
+    /* separation output of wedge 0 (mwsep_separation.cu) */
+    mwsep::DevBuf d_sprob, d_assign, d_xyz;
+    mwsep::HostPinned h_sep;
 
     mwsep::EngineState eng;
 
@@ -186,6 +189,9 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp);
 void wedge_release(mwsep_ctx* c, Wedge& w);
 void set_chunking(mwsep_area_dev& v, int k_chunk);
 void default_tune(mwsep_ctx* c, Wedge& w);
+/* One evaluation (or a batch) of wedge 0 through the grid-stride kernels;
+ * leaves the integrals in c->d_out after the area block. */
+int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out);
 
 } // namespace mwsep
 

@@ -108,20 +108,69 @@ MWSEP_HD inline void gc_to_sgr(double mu, double nu, int wedge, double& lamda, d
     beta = beta / radpdeg;
 }
 
-/* atSurveyGeometry.c:276-412: Sgr (lambda, beta) -> Galactic (l, b).  The
- * rotation is the Euler-angle matrix of phi=183.75, theta=76.54,
- * psi=194.111534 degrees (the reference spells each entry as a ratio whose
- * denominator is identically one). */
-MWSEP_HD inline void sgr_to_gal(double lamda, double beta, double& l, double& b)
+/* The Sgr -> Galactic rotation: the Euler-angle matrix of phi=183.75,
+ * theta=76.54, psi=194.111534 degrees (atSurveyGeometry.c:278-290), in its
+ * reduced form.  The reference spells each entry as a ratio whose
+ * denominator is identically one; sgr_rotation_ratio_form keeps that
+ * spelling for host code that must round like the reference. */
+MWSEP_HD inline void sgr_rotation(double* r)
 {
     const double radpdeg = 3.141592653589793 / 180;
     const double phi = (180 + 3.75) * radpdeg;
     const double theta = (90 - 13.46) * radpdeg;
     const double psi = (180 + 14.111534) * radpdeg;
     const double cf = cos(phi), sf = sin(phi), ct = cos(theta), st = sin(theta), cp = cos(psi), sp = sin(psi);
-    const double r11 = cp * cf - ct * sf * sp, r12 = -ct * sf * cp - sp * cf, r13 = st * sf;
-    const double r21 = ct * cf * sp + cp * sf, r22 = ct * cf * cp - sp * sf, r23 = -st * cf;
-    const double r31 = sp * st, r32 = cp * st, r33 = ct;
+    r[0] = cp * cf - ct * sf * sp;
+    r[1] = -ct * sf * cp - sp * cf;
+    r[2] = st * sf;
+    r[3] = ct * cf * sp + cp * sf;
+    r[4] = ct * cf * cp - sp * sf;
+    r[5] = -st * cf;
+    r[6] = sp * st;
+    r[7] = cp * st;
+    r[8] = ct;
+}
+
+/* Host only: the entries as the reference's ratios, with the terms formed
+ * and summed in its order (same libm, same rounding). */
+inline void sgr_rotation_ratio_form(double* r)
+{
+    const double radpdeg = 3.141592653589793 / 180;
+    const double phi = (180 + 3.75) * radpdeg;
+    const double theta = (90 - 13.46) * radpdeg;
+    const double psi = (180 + 14.111534) * radpdeg;
+    const double ct = cos(theta), st = sin(theta), cf = cos(phi), sf = sin(phi), cp = cos(psi), sp = sin(psi);
+    const double ct2 = pow(ct, 2), st2 = pow(st, 2), cf2 = pow(cf, 2), sf2 = pow(sf, 2), cp2 = pow(cp, 2),
+                 sp2 = pow(sp, 2);
+    double d4 = cp2 * cf2 * ct2;
+    d4 += cp2 * cf2 * st2;
+    d4 += ct2 * sp2 * sf2;
+    d4 += sp2 * cf2 * ct2;
+    d4 += sp2 * cf2 * st2;
+    d4 += ct2 * cp2 * sf2;
+    d4 += st2 * sf2 * cp2;
+    d4 += st2 * sf2 * sp2;
+    const double d3a = ct2 * sf2 + cf2 * ct2 + cf2 * st2 + st2 * sf2;
+    const double d3b = cp2 * ct2 + sp2 * st2 + cp2 * st2 + sp2 * ct2;
+    r[0] = -(ct * sf * sp - ct2 * cf * cp - cp * st2 * cf) / d4;
+    r[1] = -(ct * sf * cp + ct2 * cf * sp + sp * st2 * cf) / d4;
+    r[2] = (st * sf) / d3a;
+    r[3] = (ct * cf * sp + ct2 * cp * sf + cp * st2 * sf) / d4;
+    r[4] = -(-ct * cf * cp + ct2 * sp * sf + sp * st2 * sf) / d4;
+    r[5] = -(st * cf) / d3a;
+    r[6] = (sp * st) / d3b;
+    r[7] = (cp * st) / d3b;
+    r[8] = ct / (ct2 + st2);
+}
+
+/* atSurveyGeometry.c:276-412: Sgr (lambda, beta) -> Galactic (l, b) with
+ * the rotation rot (row-major). */
+MWSEP_HD inline void sgr_to_gal(double lamda, double beta, const double* rot, double& l, double& b)
+{
+    const double radpdeg = 3.141592653589793 / 180;
+    const double r11 = rot[0], r12 = rot[1], r13 = rot[2];
+    const double r21 = rot[3], r22 = rot[4], r23 = rot[5];
+    const double r31 = rot[6], r32 = rot[7], r33 = rot[8];
     double x2 = 0.0, y2 = 0.0;
     if (beta > 90)
     {
@@ -182,6 +231,13 @@ MWSEP_HD inline void sgr_to_gal(double lamda, double beta, double& l, double& b)
         l = l / radpdeg;
         if (l < 0) l = l + 360;
     }
+}
+
+MWSEP_HD inline void sgr_to_gal(double lamda, double beta, double& l, double& b)
+{
+    double rot[9];
+    sgr_rotation(rot);
+    sgr_to_gal(lamda, beta, rot, l, b);
 }
 
 /* stCoords.c:108-130 */

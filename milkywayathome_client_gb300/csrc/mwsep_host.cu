@@ -503,6 +503,9 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     v.r_in_mag2 = w.s_r_in_mag2.as<double>();
     v.reff = w.s_reff.as<double>();
     v.pts = w.s_pts.as<float4>();
+    v.l = w.s_l.as<double>();
+    v.b = w.s_b.as<double>();
+    v.r = w.s_r.as<double>();
     w.n_stars = n;
     w.has_stars = true;
     for (int prec = 0; prec < 2; ++prec)
@@ -583,8 +586,6 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
     w.bytes = 0;
     w.has_problem = w.has_stars = false;
 }
-
-namespace {
 
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out)
 {
@@ -720,6 +721,8 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     return MWSEP_OK;
 }
 
+namespace {
+
 Wedge* wedge0(mwsep_ctx* c)
 {
     if (c->wedges.empty())
@@ -791,10 +794,12 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
         }
     c->wedges.clear();
     size_t& t = c->dev_bytes;
-    DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out};
+    DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out,
+                      &c->d_sprob, &c->d_assign, &c->d_xyz};
     for (DevBuf* b : bufs) b->release(t);
     c->h_theta.release();
     c->h_out.release();
+    c->h_sep.release();
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);

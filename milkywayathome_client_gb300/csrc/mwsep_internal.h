@@ -82,6 +82,9 @@ typedef struct
     const double* r_in_mag2; /* [C][N] */
     const double* reff;      /* [N] */
     const float4* pts;       /* [C][N] {r_hi, r_lo, qw*reff, g} */
+    const double* l;         /* [N] the catalogue as given (degrees, degrees, kpc) */
+    const double* b;
+    const double* r;
 } mwsep_stars_dev;
 
 /* Per-evaluation likelihood sums written by the reduction kernels:

@@ -463,6 +463,21 @@ extern "C" int mwsep_write_star_points(const char* path, const STAR_POINTS* sp)
     return MWSEP_OK;
 }
 
+/* The per-star lines of separation()'s output file
+ * (cpu/separation.c:229): "<stream> <x> <y> <z>" in the stripe frame,
+ * stream 0 for the background. */
+extern "C" int mwsep_write_separation(const char* path, int n, const int* assignment, const double* xyz)
+{
+    if (!path || n < 0 || (n > 0 && (!assignment || !xyz))) return mwsep_fail(MWSEP_ERR_ARG);
+    FILE* f = fopen(path, "w");
+    if (!f) return mwsep_fail(MWSEP_ERR_IO);
+    for (int i = 0; i < n; ++i)
+        fprintf(f, "%d %lf %lf %lf\n", assignment[i], xyz[3 * (size_t)i], xyz[3 * (size_t)i + 1],
+                xyz[3 * (size_t)i + 2]);
+    if (fclose(f) != 0) return mwsep_fail(MWSEP_ERR_IO);
+    return MWSEP_OK;
+}
+
 /* cpu/star_points.c:95-103 */
 extern "C" void mwsep_free_star_points(STAR_POINTS* sp)
 {

@@ -158,6 +158,12 @@ class mwsep_server_stats(C.Structure):
 class mwsep_request(C.Structure):
     _fields_ = [("wedge", C.c_int), ("theta", C.POINTER(C.c_double))]
 
+
+class mwsep_separation_summary(C.Structure):
+    _fields_ = [("number_streams", C.c_int), ("likelihood", C.c_double), ("background_integral", C.c_double),
+                ("stream_integrals", C.c_double * MWSEP_MAX_STREAMS), ("expected", C.c_double * MWSEP_MAX_STREAMS),
+                ("assigned", C.c_longlong * MWSEP_MAX_STREAMS), ("background_assigned", C.c_longlong)]
+
 EvalFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.POINTER(ASTRONOMY_PARAMETERS),
                        C.POINTER(EVALUATION_STATE), C.POINTER(STAR_POINTS))
 
@@ -197,6 +203,10 @@ _SIGS = {
     "mwsep_ctx_last_timings": (C.c_int, [C.c_void_p, _P(C.c_double)]),
     "mwsep_ctx_last_launches": (C.c_int, [C.c_void_p, _P(C.c_int)]),
     "mwsep_ctx_transfer_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t), _P(C.c_size_t)]),
+    "mwsep_ctx_separation": (C.c_int, [C.c_void_p, _P(C.c_double), C.c_ulonglong, _P(C.c_double), _P(C.c_int),
+                                       _P(C.c_double), _P(mwsep_separation_summary)]),
+    "mwsep_stripe_transform": (C.c_int, [C.c_int, C.c_int, _P(C.c_double)]),
+    "mwsep_write_separation": (C.c_int, [C.c_char_p, C.c_int, _P(C.c_int), _P(C.c_double)]),
     "mwsep_ctx_add_wedge": (C.c_int, [C.c_void_p, _P(ASTRONOMY_PARAMETERS), _P(STAR_POINTS), _P(C.c_int)]),
     "mwsep_ctx_wedge_theta_count": (C.c_int, [C.c_void_p, C.c_int]),
     "mwsep_ctx_wedge_bytes": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_size_t)]),

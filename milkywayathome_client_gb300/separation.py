@@ -279,6 +279,8 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
+        self._n_streams = 0
+        self._n_stars = 0
         N.check(N.lib().mwsep_ctx_create(device, C.byref(self._h)), "mwsep_ctx_create")
 
     def close(self):
@@ -300,10 +302,12 @@ class Context:
 
     def set_problem(self, ap: AstronomyParameters) -> None:
         N.check(N.lib().mwsep_ctx_set_problem(self._h, C.byref(ap.struct)), "set_problem")
+        self._n_streams = ap.number_streams
 
     def set_stars(self, sp) -> None:
         if isinstance(sp, StarPoints):
             N.check(N.lib().mwsep_ctx_set_stars(self._h, C.byref(sp.struct)), "set_stars")
+            self._n_stars = sp.number_stars
         else:
             a = np.asarray(sp, dtype=np.float64)
             l = np.ascontiguousarray(a[:, 0])
@@ -311,6 +315,7 @@ class Context:
             r = np.ascontiguousarray(a[:, 2])
             N.check(N.lib().mwsep_ctx_set_stars_soa(self._h, a.shape[0], _dptr(l), _dptr(b), _dptr(r)),
                     "set_stars")
+            self._n_stars = a.shape[0]
 
     @property
     def theta_count(self) -> int:
@@ -393,6 +398,47 @@ class Context:
         v = C.c_int()
         N.check(N.lib().mwsep_ctx_last_launches(self._h, C.byref(v)))
         return v.value
+
+    def separation(self, theta, seed: int = 0) -> dict:
+        """Separate the catalogue at theta (cpu/separation.c:37-254).
+
+        Returns sprob [N][S], assignment [N] (0 background, k stream k),
+        xyz [N][3] in the stripe frame, expected [S], assigned [S],
+        background_assigned, the integrals and the likelihood."""
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        if t.size != self.theta_count:
+            raise ValueError(f"theta has {t.size} values, the problem takes {self.theta_count}")
+        sm = N.mwsep_separation_summary()
+        n = self._n_stars
+        s_count = self._n_streams
+        sprob = np.zeros((n, max(s_count, 1)))
+        assign = np.zeros(n, dtype=np.int32)
+        xyz = np.zeros((n, 3))
+        N.check(N.lib().mwsep_ctx_separation(self._h, _dptr(t), C.c_ulonglong(seed), _dptr(sprob),
+                                             assign.ctypes.data_as(C.POINTER(C.c_int)), _dptr(xyz),
+                                             C.byref(sm)), "separation")
+        S = sm.number_streams
+        return {"sprob": sprob[:, :S], "assignment": assign, "xyz": xyz, "expected": list(sm.expected[:S]),
+                "assigned": list(sm.assigned[:S]), "background_assigned": sm.background_assigned,
+                "background_integral": sm.background_integral, "stream_integrals": list(sm.stream_integrals[:S]),
+                "likelihood": sm.likelihood}
+
+
+def write_separation(path: str, assignment, xyz) -> None:
+    """Write separation()'s output file: "<stream> <x> <y> <z>" per star."""
+    a = np.ascontiguousarray(assignment, dtype=np.int32)
+    x = np.ascontiguousarray(xyz, dtype=np.float64)
+    if x.shape != (a.size, 3):
+        raise ValueError("xyz must be [N][3] for N assignments")
+    N.check(N.lib().mwsep_write_separation(path.encode(), a.size, a.ctypes.data_as(C.POINTER(C.c_int)),
+                                           _dptr(x)), "write_separation")
+
+
+def stripe_transform(sgr_coordinates: int, wedge: int) -> np.ndarray:
+    """Row-major 3x3 rotation taking the stripe's normal onto the z axis."""
+    m = np.zeros(9)
+    N.check(N.lib().mwsep_stripe_transform(int(sgr_coordinates), int(wedge), _dptr(m)), "stripe_transform")
+    return m.reshape(3, 3)
 
 
 class Server:

@@ -67,6 +67,9 @@ class Oracle:
             L.so_star_densities.argtypes = [C.c_void_p, _D, _D, _D]
             L.so_gauss_legendre.argtypes = [C.c_int, _D, _D]
             L.so_gc_to_lb.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]
+            L.so_separation.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
+            L.so_stripe_transform.argtypes = [C.c_int, C.c_int, _D]
+            L.so_transform_point.argtypes = [_D, _D, _D]
             L.so_lbr_to_xyz.argtypes = [C.c_double, C.c_double, C.c_double, _D]
             cls._lib = L
         return cls._lib
@@ -158,6 +161,29 @@ class Oracle:
                                      st.ctypes.data_as(_D))
         return bg, st[: N * S].reshape(N, S)
 
+    def separation(self, theta, integrals):
+        """(sprob [N][S], xyz [N][3], expected [S]) of separation.c."""
+        N, S = self.n_stars, self.n_streams
+        sp = np.zeros(max(N * S, 1))
+        xyz = np.zeros(N * 3)
+        ex = np.zeros(max(S, 1))
+        self.lib().so_separation(self._h, _arr(theta).ctypes.data_as(_D), _arr(integrals).ctypes.data_as(_D),
+                                 sp.ctypes.data_as(_D), xyz.ctypes.data_as(_D), ex.ctypes.data_as(_D))
+        return sp[: N * S].reshape(N, S), xyz.reshape(N, 3), ex[:S]
+
+    @classmethod
+    def stripe_transform(cls, sgr, wedge):
+        m = np.zeros(9)
+        cls.lib().so_stripe_transform(sgr, wedge, m.ctypes.data_as(_D))
+        return m.reshape(3, 3)
+
+    @classmethod
+    def transform_point(cls, xyz, mat):
+        out = np.zeros(3)
+        cls.lib().so_transform_point(_arr(xyz).ctypes.data_as(_D), _arr(mat).ravel().ctypes.data_as(_D),
+                                     out.ctypes.data_as(_D))
+        return out
+
     @classmethod
     def gauss_legendre(cls, n: int):
         x = np.zeros(n)
@@ -197,6 +223,31 @@ class Reference:
             L.mwref_evaluate_files.restype = C.c_int
             cls._lib = L
         return cls._lib
+
+    @classmethod
+    def stripe_transform(cls, sgr, wedge):
+        """stripe_normal / sgr_stripe_normal + get_transform, from the
+        reference's own compiled sources."""
+        L = cls.lib()
+        n = np.zeros(3)
+        (L.sgr_stripe_normal if sgr else L.stripe_normal)(C.c_int(wedge), n.ctypes.data_as(_D))
+        rows = [np.zeros(3) for _ in range(3)]
+        mat = (_D * 3)(*[r.ctypes.data_as(_D) for r in rows])
+        t = np.array([0.0, 0.0, 1.0])
+        L.get_transform(n.ctypes.data_as(_D), t.ctypes.data_as(_D), mat)
+        return np.array(rows)
+
+    @classmethod
+    def transform_point(cls, xyz, mat):
+        """The reference's transform_point (stVector.c:155-169)."""
+        L = cls.lib()
+        rows = [np.ascontiguousarray(mat[i], dtype=np.float64) for i in range(3)]
+        cm = (_D * 3)(*[r.ctypes.data_as(_D) for r in rows])
+        p = _arr(xyz).copy()
+        sun = np.array([-8.5, 0.0, 0.0])
+        out = np.zeros(3)
+        L.transform_point(p.ctypes.data_as(_D), cm, sun.ctypes.data_as(_D), out.ctypes.data_as(_D))
+        return out
 
     @classmethod
     def evaluate(cls, param_path, star_path, theta, n_streams, n_areas, rank=0, nranks=1, repeats=1):

@@ -534,17 +534,51 @@ static void so_gc_to_sgr(double mu, double nu, int wedge, double* lamda, double*
  * Sgr->Galactic rotation as a ratio whose denominator is identically 1
  * (sums of cos^2+sin^2 products); this restatement uses the simplified
  * Euler-angle entries, which agree to a few ulp. */
+/* The Sgr -> Galactic rotation of atSurveyGeometry.c:278-290: Euler angles
+ * phi = 183.75, theta = 76.54, psi = 194.111534 degrees, each entry written
+ * as a ratio of sums of squared sines and cosines (identically one in exact
+ * arithmetic, not in doubles).  The terms are formed and summed in the
+ * reference's order so the entries carry its rounding. */
+static void so_sgr_rotation(double* r)
+{
+    const double radpdeg = 3.141592653589793 / 180;
+    const double phi = (180 + 3.75) * radpdeg;
+    const double theta = (90 - 13.46) * radpdeg;
+    const double psi = (180 + 14.111534) * radpdeg;
+    const double ct = cos(theta), st = sin(theta), cf = cos(phi), sf = sin(phi), cp = cos(psi), sp = sin(psi);
+    const double ct2 = pow(ct, 2), st2 = pow(st, 2), cf2 = pow(cf, 2), sf2 = pow(sf, 2), cp2 = pow(cp, 2),
+                 sp2 = pow(sp, 2);
+    /* the shared denominators of the 2x2 block, of r13/r23, of r31/r32 */
+    double d4 = cp2 * cf2 * ct2;
+    d4 += cp2 * cf2 * st2;
+    d4 += ct2 * sp2 * sf2;
+    d4 += sp2 * cf2 * ct2;
+    d4 += sp2 * cf2 * st2;
+    d4 += ct2 * cp2 * sf2;
+    d4 += st2 * sf2 * cp2;
+    d4 += st2 * sf2 * sp2;
+    const double d3a = ct2 * sf2 + cf2 * ct2 + cf2 * st2 + st2 * sf2;
+    const double d3b = cp2 * ct2 + sp2 * st2 + cp2 * st2 + sp2 * ct2;
+    r[0] = -(ct * sf * sp - ct2 * cf * cp - cp * st2 * cf) / d4;
+    r[1] = -(ct * sf * cp + ct2 * cf * sp + sp * st2 * cf) / d4;
+    r[2] = (st * sf) / d3a;
+    r[3] = (ct * cf * sp + ct2 * cp * sf + cp * st2 * sf) / d4;
+    r[4] = -(-ct * cf * cp + ct2 * sp * sf + sp * st2 * sf) / d4;
+    r[5] = -(st * cf) / d3a;
+    r[6] = (sp * st) / d3b;
+    r[7] = (cp * st) / d3b;
+    r[8] = ct / (ct2 + st2);
+}
+
 static void so_sgr_to_gal(double lamda, double beta, double* l, double* b)
 {
     double radpdeg = 3.141592653589793 / 180;
-    double phi = (180 + 3.75) * radpdeg;
-    double theta = (90 - 13.46) * radpdeg;
-    double psi = (180 + 14.111534) * radpdeg;
-    double cf = cos(phi), sf = sin(phi), ct = cos(theta), st = sin(theta), cp = cos(psi), sp = sin(psi);
-    double r11 = cp * cf - ct * sf * sp, r12 = -ct * sf * cp - sp * cf, r13 = st * sf;
-    double r21 = ct * cf * sp + cp * sf, r22 = ct * cf * cp - sp * sf, r23 = -st * cf;
-    double r31 = sp * st, r32 = cp * st, r33 = ct;
+    double rot[9];
     double x2 = 0.0, y2 = 0.0, z2, x1, y1, z1;
+    double r11, r12, r13, r21, r22, r23, r31, r32, r33;
+    so_sgr_rotation(rot);
+    r11 = rot[0], r12 = rot[1], r13 = rot[2], r21 = rot[3], r22 = rot[4], r23 = rot[5], r31 = rot[6],
+    r32 = rot[7], r33 = rot[8];
 
     if (beta > 90)
     {
@@ -1244,6 +1278,177 @@ int so_star_densities(so_problem* p, const double* theta, double* bg, double* st
         for (i = 0; i < S; ++i)
             st[(size_t)s * S + i] = sp[i];
     }
+    free(r_point);
+    free(r_in_mag);
+    free(r_in_mag2);
+    free(qw);
+    so_free_consts(&k);
+    return 0;
+}
+
+
+/* ------------------------------------------------------------ separation */
+
+/* stVector.c:56-103 */
+static double so_norm3(const double* v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+static double so_dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* stCoords.c:177-185 */
+static void so_lb_to_xyz(double l, double b, double* xyz)
+{
+    l = l / SO_DEG;
+    b = b / SO_DEG;
+    xyz[0] = cos(l) * cos(b);
+    xyz[1] = sin(l) * cos(b);
+    xyz[2] = sin(b);
+}
+
+/* atSurveyGeometry.c:415-441 (survey centre RA 185, Dec 32.5) */
+static void so_survey_to_eq(double slong, double slat, double* ra, double* dec)
+{
+    double anode, etaPole, x1, y1, z1;
+    slong = slong * SO_DPI / 180.0;
+    slat = slat * SO_DPI / 180.0;
+    anode = 185.0 - 90.0;
+    anode = anode * SO_DPI / 180.0;
+    etaPole = 32.5 * SO_DPI / 180.0;
+    x1 = -sin(slong);
+    y1 = cos(slat + etaPole) * cos(slong);
+    z1 = sin(slat + etaPole) * cos(slong);
+    *ra = atan2(y1, x1) + anode;
+    *dec = asin(z1);
+    *ra = *ra * 180.0 / SO_DPI;
+    *dec = *dec * 180.0 / SO_DPI;
+    so_bound2(dec, ra);
+}
+
+void so_stripe_transform(int sgr, int wedge, double* m)
+{
+    double n[3], axis[3], t[3] = {0.0, 0.0, 1.0}, angle, sin_a, x, y, z, w, an;
+    if (sgr == 0)
+    {
+        /* stCoords.c:142-150, atSurveyGeometry.c:444-459 */
+        double eta = (wedge <= 46) ? wedge * 2.5 - 57.5 : wedge * 2.5 - 57.5 - 180.0;
+        double ra, dec, l, b;
+        so_survey_to_eq(0, 90.0 + eta, &ra, &dec);
+        so_eq_to_gal(ra, dec, &l, &b);
+        so_lb_to_xyz(l, b, n);
+    }
+    else
+    {
+        /* stCoords.c:153-174 */
+        double l1, b1, l2, b2, a1[3], a2[3];
+        so_sgr_to_gal(wedge * 2.5, 0, &l1, &b1);
+        so_sgr_to_gal(wedge * 2.5, 90, &l2, &b2);
+        so_lb_to_xyz(l1, b1, a1);
+        so_lb_to_xyz(l2, b2, a2);
+        n[0] = a1[1] * a2[2] - a1[2] * a2[1];
+        n[1] = a1[2] * a2[0] - a1[0] * a2[2];
+        n[2] = a1[0] * a2[1] - a1[1] * a2[0];
+    }
+    /* stVector.c:109-137: rotation taking n onto the z axis */
+    axis[0] = n[1] * t[2] - n[2] * t[1];
+    axis[1] = n[2] * t[0] - n[0] * t[2];
+    axis[2] = n[0] * t[1] - n[1] * t[0];
+    an = so_norm3(axis);
+    axis[0] /= an;
+    axis[1] /= an;
+    axis[2] /= an;
+    angle = acos(so_dot3(n, t) / (so_norm3(n) * so_norm3(t)));
+    sin_a = sin(angle / 2);
+    x = axis[0] * sin_a;
+    y = axis[1] * sin_a;
+    z = axis[2] * sin_a;
+    w = cos(angle / 2);
+    m[0] = 1 - 2 * (y * y + z * z);
+    m[1] = 2 * (x * y - z * w);
+    m[2] = 2 * (x * z + y * w);
+    m[3] = 2 * (x * y + z * w);
+    m[4] = 1 - 2 * (x * x + z * z);
+    m[5] = 2 * (y * z - x * w);
+    m[6] = 2 * (x * z - y * w);
+    m[7] = 2 * (y * z + x * w);
+    m[8] = 1 - 2 * (x * x + y * y);
+}
+
+/* stVector.c:155-169 with stCoords.c:52-65 (xyz2lbr), :188-201 (xyz_mag,
+ * xyz2lbg): back to (l, b, r), replace r by the magnitude minus 11, to
+ * Galactic xyz again, shift by the Sun, rotate. */
+void so_transform_point(const double* point, const double* m, double* out)
+{
+    const double r0 = 8.5;
+    double lbg[3], v[3], temp, xsun;
+    xsun = point[0] + r0;
+    temp = xsun * xsun + point[1] * point[1];
+    lbg[0] = atan2(point[1], xsun) * SO_DEG;
+    lbg[1] = atan2(point[2], sqrt(temp)) * SO_DEG;
+    lbg[2] = sqrt(temp + point[2] * point[2]);
+    if (lbg[0] < 0)
+        lbg[0] += 360;
+    lbg[2] = 5.0 * (log(100.0 * lbg[2]) / log(10.0)) + 4.2 - 11.0;
+    so_lbr_to_xyz(lbg[0], lbg[1], lbg[2], v);
+    v[0] = v[0] - (-8.5);
+    v[1] = v[1] - 0.0;
+    v[2] = v[2] - 0.0;
+    out[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+    out[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+    out[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+}
+
+int so_separation(so_problem* p, const double* theta, const double* integrals, double* sprob, double* xyz,
+                  double* expected)
+{
+    so_consts k;
+    const int C = p->convolve, S = p->n_streams;
+    double *r_point, *r_in_mag, *r_in_mag2, *qw, reff, pb, ps[SO_MAX_STREAMS], eps_s[SO_MAX_STREAMS], eps_b,
+        denom, nst[SO_MAX_STREAMS], m[9];
+    int s, j;
+    so_set_theta(p, theta);
+    so_init_consts(p, &k);
+    so_stripe_transform(p->sgr, p->wedge, m);
+    /* separation.c:128-140 */
+    denom = 1.0;
+    for (j = 0; j < S; ++j)
+        denom += exp(p->st_weight[j]);
+    for (j = 0; j < S; ++j)
+    {
+        eps_s[j] = exp(p->st_weight[j]) / denom;
+        nst[j] = 0;
+    }
+    eps_b = 1.0 / denom;
+    r_point = (double*)malloc(sizeof(double) * (size_t)C);
+    r_in_mag = (double*)malloc(sizeof(double) * (size_t)C);
+    r_in_mag2 = (double*)malloc(sizeof(double) * (size_t)C);
+    qw = (double*)malloc(sizeof(double) * (size_t)C);
+    for (s = 0; s < p->n_stars; ++s)
+    {
+        const double* star = p->stars + 3 * (size_t)s;
+        double pbx, psg[SO_MAX_STREAMS], psg_sum = 0, starxyz[3];
+        so_prob_consts(p, &k, star[2], r_point, r_in_mag, r_in_mag2, qw, &reff);
+        so_probabilities(p, &k, r_point, r_in_mag, r_in_mag2, qw, reff, star, &pb, ps);
+        /* :170-196 */
+        pbx = eps_b * pb / integrals[0];
+        for (j = 0; j < S; ++j)
+            psg[j] = eps_s[j] * ps[j] / integrals[1 + j];
+        for (j = 0; j < S; ++j)
+            psg_sum += psg[j];
+        for (j = 0; j < S; ++j)
+        {
+            const double sp = psg[j] / (psg_sum + pbx);
+            if (sprob)
+                sprob[(size_t)s * S + j] = sp;
+            nst[j] += sp;
+        }
+        /* :226-227 */
+        if (xyz)
+        {
+            so_lbr_to_xyz(star[0], star[1], star[2], starxyz);
+            so_transform_point(starxyz, m, xyz + 3 * (size_t)s);
+        }
+    }
+    if (expected)
+        for (j = 0; j < S; ++j)
+            expected[j] = nst[j];
     free(r_point);
     free(r_in_mag);
     free(r_in_mag2);

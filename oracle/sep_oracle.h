@@ -74,6 +74,20 @@ int so_r_tables(so_problem* p, int area, double* irv, double* reff_xr_rp3,
  * bg[N], st[N][S]. */
 int so_star_densities(so_problem* p, const double* theta, double* bg, double* st);
 
+/* The separation output (milkyway_separation/cpu/separation.c:37-254, a
+ * program the reference no longer builds): with integrals (1+S) from an
+ * evaluation, per star the stream-membership probabilities
+ * sprob[N][S] = psg_s / (sum psg + pbx) (:128-199), and the star's position
+ * in the stripe frame xyz[N][3] (:75-116, :226-227).  expected[S] = the
+ * sequential sum of sprob over stars (:193-196).  Any output may be NULL. */
+int so_separation(so_problem* p, const double* theta, const double* integrals, double* sprob, double* xyz,
+                  double* expected);
+/* The stripe-frame rotation (stripe_normal or sgr_stripe_normal, then
+ * get_transform to the z axis): mat9 row-major. */
+void so_stripe_transform(int sgr, int wedge, double* mat9);
+/* transform_point (stVector.c:155-169) with the Sun at (-8.5, 0, 0). */
+void so_transform_point(const double* xyz, const double* mat9, double* out);
+
 /* Gauss-Legendre nodes/weights on [-1,1] (numericalIntegration.c:67-104). */
 void so_gauss_legendre(int n, double* x, double* w);
 

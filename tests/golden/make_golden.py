@@ -8,9 +8,12 @@ fixtures travel with the repository.
 
 Also records the reference's results on its own test fixtures
 (tests/astronomy_parameters-*-small.txt with the theta vectors of
-tests/CMakeLists.txt:24-41) as values only, in reference_fixtures.json.
+tests/CMakeLists.txt:24-41) as values only, in reference_fixtures.json,
+and the reference's stripe-frame transforms (stripe_normal /
+sgr_stripe_normal + get_transform, transform_point; cpu/stCoords.c,
+cpu/stVector.c) for a set of wedges and points, in transforms.json.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--transforms-only]
 """
 from __future__ import annotations
 
@@ -130,10 +133,32 @@ def reference_on_fixtures(ref_dir):
     return out
 
 
+def reference_transforms():
+    """The reference's stripe rotation for survey and Sgr wedges, and
+    transform_point of seeded Galactic points through each."""
+    rng = np.random.Generator(np.random.PCG64(4242))
+    out = []
+    for sgr, wedges in ((0, [9, 10, 11, 12, 20, 37, 46, 47, 60, 79, 82, 86]), (1, [5, 20, 79, 100, 130])):
+        for w in wedges:
+            m = orc.Reference.stripe_transform(sgr, w)
+            pts = []
+            for _ in range(4):
+                l, b, r = rng.uniform(0, 360), rng.uniform(-80, 80), rng.uniform(16, 23)
+                xyz = orc.Oracle.lbr_to_xyz(l, b, r)
+                pts.append({"lbr": [l, b, r], "xyz": [float(v) for v in xyz],
+                            "out": [float(v) for v in orc.Reference.transform_point(xyz, m)]})
+            out.append({"sgr": sgr, "wedge": w, "matrix": [float(v) for v in m.ravel()], "points": pts})
+    return out
+
+
 def main():
     orc.build(reference=True)
     if not orc.reference_available():
         sys.exit("the reference sources are needed to regenerate the goldens")
+    with open(os.path.join(HERE, "transforms.json"), "w") as f:
+        json.dump(reference_transforms(), f, indent=1)
+    if "--transforms-only" in sys.argv:
+        return
     os.makedirs(CASES, exist_ok=True)
     index = {}
     for k, (name, p, n) in enumerate(case_list()):
