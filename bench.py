@@ -361,6 +361,7 @@ def run_gb300_arm(args, ws, rank, local):
         ctx = None
         out["population_batch"] = population_batch(args)
         out["serving"] = serving(args)
+        out["catalogue_load"] = catalogue_load(args, files)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         n = min(host_cores(), 64)
         cw, kind, _ = cpu_sample(files, theta, n)
@@ -394,12 +395,39 @@ def population_batch(args):
         launches = ctx.last_launches()
         plain = ctx.evaluate_requests(reqs[:4], mw.MWSEP_PLAIN_F64)
         plain_ms = ctx.last_timings()["total_ms"]
+        # the errors() consumer: a finite-difference Hessian (2P^2+1 points) as engine batches
+        step = mw.AstronomyParameters.read(f["params"]).step()
+        P = len(step)
+        t0 = time.perf_counter()
+        ctx.hessian(wid, thetas[0], step, mw.MWSEP_MIXED_F32)
+        hess_s = time.perf_counter() - t0
     ms = statistics.median(times)
     return {"workload": "256 parameter vectors, 400x160x140 cells, convolve 60, 3 streams, 50k stars",
             "value": len(thetas) / (ms * 1e-3), "unit": "evals/s", "ms_per_batch": ms,
             "launches_per_batch": launches, "graph": True,
             "plain_f64_evals_per_s": 4 / (plain_ms * 1e-3),
-            "max_dlogL_mixed_vs_plain": max(abs(a.likelihood - b.likelihood) for a, b in zip(res[:4], plain))}
+            "max_dlogL_mixed_vs_plain": max(abs(a.likelihood - b.likelihood) for a, b in zip(res[:4], plain)),
+            "hessian": {"parameters": P, "evaluations": 2 * P * P + 1, "seconds": hess_s,
+                        "evals_per_s": (2 * P * P + 1) / hess_s, "precision": "mixed"}}
+
+
+def catalogue_load(args, files):
+    """Making the 100k-star catalogue resident: the reference's text file
+    (parse + upload + star tables) against the binary catalogue (map +
+    upload + star tables)."""
+    import milkywayathome_client_gb300 as mw
+    f = files[0]
+    binp = os.path.join(args.data_dir, "catalogue.mwsb")
+    mw.StarPoints.read(f["stars"]).write_binary(binp)
+    out = {}
+    with mw.Context(0) as ctx:
+        ctx.set_problem(mw.AstronomyParameters.read(f["params"]))
+        for kind, path in (("text", f["stars"]), ("binary", binp), ("text", f["stars"]), ("binary", binp)):
+            t0 = time.perf_counter()
+            ctx.set_stars_file(path)
+            out[kind] = (time.perf_counter() - t0) * 1e3
+    return {"stars": f["n_stars"], "text_ms": out["text"], "binary_ms": out["binary"],
+            "speedup": out["text"] / out["binary"]}
 
 
 def serving(args):

@@ -200,6 +200,12 @@ int mwsep_set_astronomy_parameters(ASTRONOMY_PARAMETERS* ap, const double* param
 /* Replaces get_search_parameters (cpu/parameters.c:365-397); out holds
  * get_optimized_parameter_count doubles. */
 int mwsep_get_search_parameters(const ASTRONOMY_PARAMETERS* ap, double* out);
+/* Replace get_step, get_min_parameters, get_max_parameters
+ * (cpu/parameters.c:399-500): the step / bounds of each optimised
+ * parameter in theta order; out holds get_optimized_parameter_count doubles. */
+int mwsep_get_step(const ASTRONOMY_PARAMETERS* ap, double* out);
+int mwsep_get_min_parameters(const ASTRONOMY_PARAMETERS* ap, double* out);
+int mwsep_get_max_parameters(const ASTRONOMY_PARAMETERS* ap, double* out);
 /* Replaces split_astronomy_parameters (cpu/parameters.c:502-522), without
  * its printf. */
 int mwsep_split_astronomy_parameters(ASTRONOMY_PARAMETERS* ap, int rank, int max_rank);
@@ -212,6 +218,34 @@ int mwsep_write_star_points(const char* path, const STAR_POINTS* sp);
 void mwsep_free_star_points(STAR_POINTS* sp);
 /* Replaces split_star_points (cpu/star_points.c:105-131). */
 int mwsep_split_star_points(STAR_POINTS* sp, int rank, int max_rank);
+
+/* Binary forms of the two input files (no reference counterpart: the
+ * reference reads text only).  A star catalogue is a 64-byte header
+ * ("MWSEPCAT", version 1, n, column offsets, file size) and three
+ * 64-byte-aligned little-endian double columns l[n], b[n], r[n]; a parameter
+ * file is "MWSEPPAR", version 1, the ASTRONOMY_PARAMETERS fields in
+ * declaration order and an FNV-1a checksum.  Malformed or truncated files
+ * give MWSEP_ERR_IO. */
+typedef struct
+{
+    int number_stars;
+    const double* l; /* degrees */
+    const double* b; /* degrees */
+    const double* r; /* kpc */
+    void* map;       /* the read-only mapping; release with mwsep_unmap_star_catalogue */
+    size_t map_bytes;
+} mwsep_star_catalogue;
+
+int mwsep_write_star_catalogue(const char* path, int n, const double* l, const double* b, const double* r);
+int mwsep_write_star_points_binary(const char* path, const STAR_POINTS* sp);
+/* Map a catalogue read-only: the columns point into the mapping. */
+int mwsep_map_star_catalogue(const char* path, mwsep_star_catalogue* out);
+int mwsep_unmap_star_catalogue(mwsep_star_catalogue* cat);
+/* Read a binary catalogue into the reference's row layout. */
+int mwsep_read_star_points_binary(const char* path, STAR_POINTS* sp);
+int mwsep_write_astronomy_parameters_binary(const char* path, const ASTRONOMY_PARAMETERS* ap);
+/* Free the result with mwsep_free_parameters. */
+int mwsep_read_astronomy_parameters_binary(const char* path, ASTRONOMY_PARAMETERS* ap);
 
 /* Replaces initialize_state (cpu/evaluation_state.c:153-176). */
 int mwsep_initialize_state(const ASTRONOMY_PARAMETERS* ap, const STAR_POINTS* sp, EVALUATION_STATE* es);
@@ -278,6 +312,10 @@ int mwsep_ctx_set_problem(mwsep_ctx* ctx, const ASTRONOMY_PARAMETERS* ap);
  * convolution tables on the device. */
 int mwsep_ctx_set_stars(mwsep_ctx* ctx, const STAR_POINTS* sp);
 int mwsep_ctx_set_stars_soa(mwsep_ctx* ctx, int n, const double* l, const double* b, const double* r);
+/* Make a catalogue file resident: a binary catalogue is mapped and its
+ * columns uploaded as they lie; anything else is read as the reference's
+ * text star file. */
+int mwsep_ctx_set_stars_file(mwsep_ctx* ctx, const char* path);
 
 /* Number of theta values the resident problem expects. */
 int mwsep_ctx_theta_count(const mwsep_ctx* ctx);
@@ -424,6 +462,34 @@ int mwsep_stripe_transform(int sgr_coordinates, int wedge, double* mat9);
 /* Write separation()'s output file (cpu/separation.c:229): one line
  * "<stream> <x> <y> <z>" per star, stream 0 for the background. */
 int mwsep_write_separation(const char* path, int n, const int* assignment, const double* xyz);
+
+/* ------------------------------------------------------------------ */
+/* Optimiser-side consumers: finite differences and parameter errors    */
+/* ------------------------------------------------------------------ */
+
+/* Central finite differences of f = likelihood (prob_sum/N - 3) of one
+ * resident wedge at theta with per-parameter steps (mwsep_get_step), all
+ * points evaluated as engine batches.  Replace get_hessian of the search
+ * library that cpu/errors.c:47 and the gradient searches of
+ * cpu/mpi_astronomy.c:96-124 call (that library is not part of the
+ * reference):
+ *   gradient[i]  = (f(x+h_i e_i) - f(x-h_i e_i)) / (2 h_i)
+ *   hessian[i*P+i] = ((f(x+h_i e_i) - f0) + (f(x-h_i e_i) - f0)) / h_i^2
+ *   hessian[i*P+j] = ((f(++) - f(+-)) - (f(-+) - f(--))) / (4 h_i h_j)
+ * 2P+1 (gradient) or 2P^2+1 (Hessian) evaluations.  Outputs may be NULL. */
+int mwsep_ctx_gradient(mwsep_ctx* ctx, int wedge, const double* theta, const double* step, int precision,
+                       double* f0, double* gradient);
+int mwsep_ctx_hessian(mwsep_ctx* ctx, int wedge, const double* theta, const double* step, int precision,
+                      double* f0, double* gradient, double* hessian);
+
+/* matrix_invert (util/matrix.c:234-319): LU with partial pivoting, one
+ * solve per unit vector; row-major n x n.  MWSEP_ERR_ARG when singular. */
+int mwsep_invert_matrix(int n, const double* a, double* inverse);
+/* errors() (cpu/errors.c:38-84): sigma = hessian^-1 / number_stars,
+ * stddev[i] = sqrt(|sigma_ii|).  Host only. */
+int mwsep_errors_from_hessian(int n, const double* hessian, int number_stars, double* sigma, double* stddev);
+/* errors()'s output file: the Hessian (" %.20lf"), SIGMA and the errors. */
+int mwsep_write_errors(const char* path, int n, const double* hessian, const double* sigma, const double* stddev);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free area integral                                        */

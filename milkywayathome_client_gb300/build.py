@@ -41,6 +41,8 @@ UNITS = [
     ("mwsep_separation.cu", ["-fmad=false"]),
     ("mwsep_io.cpp", []),
     ("mwsep_server.cpp", []),
+    ("mwsep_optimise.cpp", []),
+    ("mwsep_binary.cpp", []),
 ]
 
 

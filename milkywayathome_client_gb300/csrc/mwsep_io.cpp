@@ -399,6 +399,49 @@ extern "C" int mwsep_get_search_parameters(const ASTRONOMY_PARAMETERS* ap, doubl
     return MWSEP_OK;
 }
 
+namespace {
+
+/* The optimised entries of one per-parameter array family, in theta order
+ * (the walk of get_search_parameters). */
+int gather_optimised(const ASTRONOMY_PARAMETERS* ap, const double* bg, const double* sw, double* const* st,
+                     double* out)
+{
+    if (!ap || !out || !bg || !sw || !st) return mwsep_fail(MWSEP_ERR_ARG);
+    int k = 0;
+    for (int i = 0; i < ap->number_background_parameters; ++i)
+        if (ap->background_optimize[i]) out[k++] = bg[i];
+    for (int i = 0; i < ap->number_streams; ++i)
+    {
+        if (ap->stream_weight_optimize[i]) out[k++] = sw[i];
+        for (int j = 0; j < ap->number_stream_parameters; ++j)
+            if (ap->stream_optimize[i][j]) out[k++] = st[i][j];
+    }
+    return MWSEP_OK;
+}
+
+} // namespace
+
+/* cpu/parameters.c:399-432 */
+extern "C" int mwsep_get_step(const ASTRONOMY_PARAMETERS* ap, double* out)
+{
+    if (!ap) return mwsep_fail(MWSEP_ERR_ARG);
+    return gather_optimised(ap, ap->background_step, ap->stream_weight_step, ap->stream_step, out);
+}
+
+/* cpu/parameters.c:434-466 */
+extern "C" int mwsep_get_min_parameters(const ASTRONOMY_PARAMETERS* ap, double* out)
+{
+    if (!ap) return mwsep_fail(MWSEP_ERR_ARG);
+    return gather_optimised(ap, ap->background_min, ap->stream_weight_min, ap->stream_min, out);
+}
+
+/* cpu/parameters.c:468-500 */
+extern "C" int mwsep_get_max_parameters(const ASTRONOMY_PARAMETERS* ap, double* out)
+{
+    if (!ap) return mwsep_fail(MWSEP_ERR_ARG);
+    return gather_optimised(ap, ap->background_max, ap->stream_weight_max, ap->stream_max, out);
+}
+
 /* cpu/parameters.c:502-522 */
 extern "C" int mwsep_split_astronomy_parameters(ASTRONOMY_PARAMETERS* ap, int rank, int max_rank)
 {

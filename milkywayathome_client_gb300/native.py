@@ -159,6 +159,11 @@ class mwsep_request(C.Structure):
     _fields_ = [("wedge", C.c_int), ("theta", C.POINTER(C.c_double))]
 
 
+class mwsep_star_catalogue(C.Structure):
+    _fields_ = [("number_stars", C.c_int), ("l", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)),
+                ("r", C.POINTER(C.c_double)), ("map", C.c_void_p), ("map_bytes", C.c_size_t)]
+
+
 class mwsep_separation_summary(C.Structure):
     _fields_ = [("number_streams", C.c_int), ("likelihood", C.c_double), ("background_integral", C.c_double),
                 ("stream_integrals", C.c_double * MWSEP_MAX_STREAMS), ("expected", C.c_double * MWSEP_MAX_STREAMS),
@@ -207,6 +212,26 @@ _SIGS = {
                                        _P(C.c_double), _P(mwsep_separation_summary)]),
     "mwsep_stripe_transform": (C.c_int, [C.c_int, C.c_int, _P(C.c_double)]),
     "mwsep_write_separation": (C.c_int, [C.c_char_p, C.c_int, _P(C.c_int), _P(C.c_double)]),
+    "mwsep_get_step": (C.c_int, [_P(ASTRONOMY_PARAMETERS), _P(C.c_double)]),
+    "mwsep_write_star_catalogue": (C.c_int, [C.c_char_p, C.c_int, _P(C.c_double), _P(C.c_double),
+                                             _P(C.c_double)]),
+    "mwsep_write_star_points_binary": (C.c_int, [C.c_char_p, _P(STAR_POINTS)]),
+    "mwsep_map_star_catalogue": (C.c_int, [C.c_char_p, _P(mwsep_star_catalogue)]),
+    "mwsep_unmap_star_catalogue": (C.c_int, [_P(mwsep_star_catalogue)]),
+    "mwsep_read_star_points_binary": (C.c_int, [C.c_char_p, _P(STAR_POINTS)]),
+    "mwsep_write_astronomy_parameters_binary": (C.c_int, [C.c_char_p, _P(ASTRONOMY_PARAMETERS)]),
+    "mwsep_read_astronomy_parameters_binary": (C.c_int, [C.c_char_p, _P(ASTRONOMY_PARAMETERS)]),
+    "mwsep_ctx_set_stars_file": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "mwsep_get_min_parameters": (C.c_int, [_P(ASTRONOMY_PARAMETERS), _P(C.c_double)]),
+    "mwsep_get_max_parameters": (C.c_int, [_P(ASTRONOMY_PARAMETERS), _P(C.c_double)]),
+    "mwsep_ctx_gradient": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double), C.c_int,
+                                     _P(C.c_double), _P(C.c_double)]),
+    "mwsep_ctx_hessian": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double), C.c_int,
+                                    _P(C.c_double), _P(C.c_double), _P(C.c_double)]),
+    "mwsep_invert_matrix": (C.c_int, [C.c_int, _P(C.c_double), _P(C.c_double)]),
+    "mwsep_errors_from_hessian": (C.c_int, [C.c_int, _P(C.c_double), C.c_int, _P(C.c_double),
+                                            _P(C.c_double)]),
+    "mwsep_write_errors": (C.c_int, [C.c_char_p, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double)]),
     "mwsep_ctx_add_wedge": (C.c_int, [C.c_void_p, _P(ASTRONOMY_PARAMETERS), _P(STAR_POINTS), _P(C.c_int)]),
     "mwsep_ctx_wedge_theta_count": (C.c_int, [C.c_void_p, C.c_int]),
     "mwsep_ctx_wedge_bytes": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_size_t)]),

@@ -50,6 +50,18 @@ class AstronomyParameters:
         N.check(N.lib().mwsep_write_astronomy_parameters(str(path).encode(), C.byref(self._s)),
                 f"writing {path}")
 
+    @classmethod
+    def read_binary(cls, path: str) -> "AstronomyParameters":
+        ap = cls()
+        N.check(N.lib().mwsep_read_astronomy_parameters_binary(str(path).encode(), C.byref(ap._s)),
+                f"reading {path}")
+        ap._owned = True
+        return ap
+
+    def write_binary(self, path: str) -> None:
+        N.check(N.lib().mwsep_write_astronomy_parameters_binary(str(path).encode(), C.byref(self._s)),
+                f"writing {path}")
+
     def close(self) -> None:
         if self._owned:
             N.lib().mwsep_free_parameters(C.byref(self._s))
@@ -91,6 +103,20 @@ class AstronomyParameters:
         out = np.zeros(self.optimized_parameter_count)
         N.check(N.lib().mwsep_get_search_parameters(C.byref(self._s), _dptr(out)))
         return out
+
+    def step(self) -> np.ndarray:
+        """get_step: the step of each optimised parameter."""
+        out = np.zeros(self.optimized_parameter_count)
+        N.check(N.lib().mwsep_get_step(C.byref(self._s), _dptr(out)))
+        return out
+
+    def bounds(self):
+        """(get_min_parameters, get_max_parameters)."""
+        lo = np.zeros(self.optimized_parameter_count)
+        hi = np.zeros(self.optimized_parameter_count)
+        N.check(N.lib().mwsep_get_min_parameters(C.byref(self._s), _dptr(lo)))
+        N.check(N.lib().mwsep_get_max_parameters(C.byref(self._s), _dptr(hi)))
+        return lo, hi
 
     def split(self, rank: int, max_rank: int) -> None:
         N.check(N.lib().mwsep_split_astronomy_parameters(C.byref(self._s), rank, max_rank))
@@ -134,6 +160,16 @@ class StarPoints:
 
     def write(self, path: str) -> None:
         N.check(N.lib().mwsep_write_star_points(str(path).encode(), C.byref(self._s)), f"writing {path}")
+
+    @classmethod
+    def read_binary(cls, path: str) -> "StarPoints":
+        sp = cls()
+        N.check(N.lib().mwsep_read_star_points_binary(str(path).encode(), C.byref(sp._s)), f"reading {path}")
+        sp._owned = True
+        return sp
+
+    def write_binary(self, path: str) -> None:
+        N.check(N.lib().mwsep_write_star_points_binary(str(path).encode(), C.byref(self._s)), f"writing {path}")
 
     def to_array(self) -> np.ndarray:
         n = self._s.number_stars
@@ -317,6 +353,20 @@ class Context:
                     "set_stars")
             self._n_stars = a.shape[0]
 
+    def set_stars_file(self, path: str) -> None:
+        """A binary catalogue (mapped) or the reference's text star file."""
+        N.check(N.lib().mwsep_ctx_set_stars_file(self._h, str(path).encode()), "set_stars_file")
+        self._n_stars = self._probe_stars(path)
+
+    @staticmethod
+    def _probe_stars(path: str) -> int:
+        with open(path, "rb") as f:
+            head = f.read(24)
+        if head[:8] == b"MWSEPCAT":
+            return int.from_bytes(head[16:24], "little")
+        with open(path) as f:
+            return int(f.readline().split()[0])
+
     @property
     def theta_count(self) -> int:
         return N.lib().mwsep_ctx_theta_count(self._h)
@@ -399,6 +449,31 @@ class Context:
         N.check(N.lib().mwsep_ctx_last_launches(self._h, C.byref(v)))
         return v.value
 
+    def gradient(self, wedge: int, theta, step, precision: int = N.MWSEP_PLAIN_F64):
+        """(f0, gradient) by central differences, one engine batch."""
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        h = np.ascontiguousarray(step, dtype=np.float64)
+        if t.size != h.size:
+            raise ValueError("theta and step differ in length")
+        f0 = C.c_double()
+        g = np.zeros(t.size)
+        N.check(N.lib().mwsep_ctx_gradient(self._h, wedge, _dptr(t), _dptr(h), precision, C.byref(f0), _dptr(g)),
+                "gradient")
+        return f0.value, g
+
+    def hessian(self, wedge: int, theta, step, precision: int = N.MWSEP_PLAIN_F64):
+        """(f0, gradient, hessian) by central differences (2P^2+1 evaluations)."""
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        h = np.ascontiguousarray(step, dtype=np.float64)
+        if t.size != h.size:
+            raise ValueError("theta and step differ in length")
+        f0 = C.c_double()
+        g = np.zeros(t.size)
+        H = np.zeros((t.size, t.size))
+        N.check(N.lib().mwsep_ctx_hessian(self._h, wedge, _dptr(t), _dptr(h), precision, C.byref(f0), _dptr(g),
+                                          _dptr(H)), "hessian")
+        return f0.value, g, H
+
     def separation(self, theta, seed: int = 0) -> dict:
         """Separate the catalogue at theta (cpu/separation.c:37-254).
 
@@ -422,6 +497,70 @@ class Context:
                 "assigned": list(sm.assigned[:S]), "background_assigned": sm.background_assigned,
                 "background_integral": sm.background_integral, "stream_integrals": list(sm.stream_integrals[:S]),
                 "likelihood": sm.likelihood}
+
+
+class StarCatalogue:
+    """A binary star catalogue mapped read-only; l, b, r are views into the
+    mapping (valid until close)."""
+
+    def __init__(self, path: str):
+        self._c = N.mwsep_star_catalogue()
+        N.check(N.lib().mwsep_map_star_catalogue(str(path).encode(), C.byref(self._c)), f"mapping {path}")
+        n = self._c.number_stars
+        self.number_stars = n
+        self.l = np.ctypeslib.as_array(self._c.l, shape=(n,)) if n else np.zeros(0)
+        self.b = np.ctypeslib.as_array(self._c.b, shape=(n,)) if n else np.zeros(0)
+        self.r = np.ctypeslib.as_array(self._c.r, shape=(n,)) if n else np.zeros(0)
+
+    @staticmethod
+    def write(path: str, lbr) -> None:
+        a = np.asarray(lbr, dtype=np.float64)
+        cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+        N.check(N.lib().mwsep_write_star_catalogue(str(path).encode(), a.shape[0], *[_dptr(c) for c in cols]),
+                f"writing {path}")
+
+    def close(self) -> None:
+        if self._c.map:
+            self.l = self.b = self.r = None
+            N.lib().mwsep_unmap_star_catalogue(C.byref(self._c))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def invert_matrix(a) -> np.ndarray:
+    """matrix_invert of util/matrix.c (LU with partial pivoting)."""
+    m = np.ascontiguousarray(a, dtype=np.float64)
+    out = np.zeros_like(m)
+    N.check(N.lib().mwsep_invert_matrix(m.shape[0], _dptr(m), _dptr(out)), "invert_matrix")
+    return out
+
+
+def errors_from_hessian(hessian, number_stars: int):
+    """errors() of cpu/errors.c: (sigma = H^-1 / N, sqrt|sigma_ii|)."""
+    H = np.ascontiguousarray(hessian, dtype=np.float64)
+    n = H.shape[0]
+    sigma = np.zeros((n, n))
+    sd = np.zeros(n)
+    N.check(N.lib().mwsep_errors_from_hessian(n, _dptr(H), int(number_stars), _dptr(sigma), _dptr(sd)),
+            "errors_from_hessian")
+    return sigma, sd
+
+
+def write_errors(path: str, hessian, sigma, stddev) -> None:
+    H = np.ascontiguousarray(hessian, dtype=np.float64)
+    S = np.ascontiguousarray(sigma, dtype=np.float64)
+    d = np.ascontiguousarray(stddev, dtype=np.float64)
+    N.check(N.lib().mwsep_write_errors(path.encode(), H.shape[0], _dptr(H), _dptr(S), _dptr(d)), "write_errors")
 
 
 def write_separation(path: str, assignment, xyz) -> None:

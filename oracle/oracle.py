@@ -250,6 +250,22 @@ class Reference:
         return out
 
     @classmethod
+    def invert_matrix(cls, a):
+        """The reference's matrix_invert (util/matrix.c:298-319)."""
+        L = cls.lib()
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        n = a.shape[0]
+        rows_in = [np.ascontiguousarray(a[i]) for i in range(n)]
+        rows_out = [np.zeros(n) for _ in range(n)]
+        pin = (_D * n)(*[r.ctypes.data_as(_D) for r in rows_in])
+        pout = (_D * n)(*[r.ctypes.data_as(_D) for r in rows_out])
+        L.matrix_invert.argtypes = [C.POINTER(_D), C.c_int, C.c_int, C.POINTER(_D)]
+        L.matrix_invert.restype = C.c_int
+        if L.matrix_invert(pin, n, n, pout) != 0:
+            raise ValueError("singular matrix")
+        return np.array(rows_out)
+
+    @classmethod
     def evaluate(cls, param_path, star_path, theta, n_streams, n_areas, rank=0, nranks=1, repeats=1):
         t = _arr(theta)
         bg = C.c_double()

@@ -9,11 +9,13 @@ fixtures travel with the repository.
 Also records the reference's results on its own test fixtures
 (tests/astronomy_parameters-*-small.txt with the theta vectors of
 tests/CMakeLists.txt:24-41) as values only, in reference_fixtures.json,
-and the reference's stripe-frame transforms (stripe_normal /
+the reference's stripe-frame transforms (stripe_normal /
 sgr_stripe_normal + get_transform, transform_point; cpu/stCoords.c,
-cpu/stVector.c) for a set of wedges and points, in transforms.json.
+cpu/stVector.c) for a set of wedges and points, in transforms.json, and the
+reference's matrix_invert (util/matrix.c) of seeded matrices, in
+matrix_invert.json.
 
-    python tests/golden/make_golden.py [--transforms-only]
+    python tests/golden/make_golden.py [--aux-only]
 """
 from __future__ import annotations
 
@@ -151,13 +153,29 @@ def reference_transforms():
     return out
 
 
+def reference_inversions():
+    """matrix_invert of seeded well-conditioned matrices (Hessian-like:
+    symmetric negative definite, sizes 1..23) and of a general one."""
+    rng = np.random.Generator(np.random.PCG64(777))
+    out = []
+    for n in (1, 2, 3, 5, 8, 13, 23):
+        a = rng.standard_normal((n, n))
+        h = -(a @ a.T + n * np.eye(n)) * 10.0 ** rng.uniform(-2, 4)
+        out.append({"a": h.ravel().tolist(), "n": n, "inverse": orc.Reference.invert_matrix(h).ravel().tolist()})
+    g = rng.standard_normal((6, 6))
+    out.append({"a": g.ravel().tolist(), "n": 6, "inverse": orc.Reference.invert_matrix(g).ravel().tolist()})
+    return out
+
+
 def main():
     orc.build(reference=True)
     if not orc.reference_available():
         sys.exit("the reference sources are needed to regenerate the goldens")
     with open(os.path.join(HERE, "transforms.json"), "w") as f:
         json.dump(reference_transforms(), f, indent=1)
-    if "--transforms-only" in sys.argv:
+    with open(os.path.join(HERE, "matrix_invert.json"), "w") as f:
+        json.dump(reference_inversions(), f, indent=1)
+    if "--aux-only" in sys.argv:
         return
     os.makedirs(CASES, exist_ok=True)
     index = {}
