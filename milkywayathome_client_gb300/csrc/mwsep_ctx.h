@@ -108,6 +108,7 @@ struct Tune
     int lk_grid = 0;
     int tile_items = 0; /* engine: items per integral tile */
     int tile_stars = 0; /* engine: stars per likelihood tile */
+    int warp_items = 0; /* integral items are warp tiles (compensated form) */
     bool tuned = false; /* chosen by the autotuner */
 };
 
@@ -187,7 +188,9 @@ int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap);
 int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r);
 int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp);
 void wedge_release(mwsep_ctx* c, Wedge& w);
-void set_chunking(mwsep_area_dev& v, int k_chunk);
+void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items);
+/* r-bins per warp tile that make a tile's points whole lane groups. */
+int warp_tile_kstep(int convolve, int n_streams);
 void default_tune(mwsep_ctx* c, Wedge& w);
 /* One evaluation (or a batch) of wedge 0 through the grid-stride kernels;
  * leaves the integrals in c->d_out after the area block. */

@@ -94,7 +94,7 @@ int ensure_descriptors(mwsep_ctx* c)
             for (int p = 0; p < 2; ++p)
             {
                 mwsep_area_dev v = wd.areas[a].view;
-                set_chunking(v, wd.tune[p].k_chunk);
+                set_chunking(v, wd.tune[p].k_chunk, wd.tune[p].warp_items);
                 ha[e.area_base[w] + 2 * a + p] = v;
             }
     }
@@ -136,7 +136,7 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
         for (int a = 0; a < w.prob.n_areas; ++a)
         {
             mwsep_area_dev v = w.areas[a].view;
-            set_chunking(v, t.k_chunk);
+            set_chunking(v, t.k_chunk, t.warp_items);
             nit[cls] += (v.n_items + t.tile_items - 1) / t.tile_items;
         }
         if (with_likelihood) nlt[cls] += (w.n_stars + t.tile_stars - 1) / t.tile_stars;
@@ -198,7 +198,7 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
         for (int a = 0; a < w.prob.n_areas; ++a)
         {
             mwsep_area_dev v = w.areas[a].view;
-            set_chunking(v, t.k_chunk);
+            set_chunking(v, t.k_chunk, t.warp_items);
             q.area_slot[a] = (int)it_pos[cls];
             for (long long b = 0; b < v.n_items; b += t.tile_items)
             {
@@ -545,23 +545,38 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
     const int waves = 6;
     const long long resident = (long long)c->sm_count * blocks_per_sm(precision, 0, cls);
     std::vector<int> kcs;
-    for (int d = 1; d <= 64 && (R + d - 1) / d >= 1; d *= 2)
+    if (saved.warp_items)
     {
-        const int kc = (R + d - 1) / d;
-        if (kcs.empty() || kcs.back() != kc) kcs.push_back(kc);
-        if (kc == 1) break;
+        /* warp tiles: r-chunks of whole lane groups, and the default */
+        const int ks = warp_tile_kstep(C, w.prob.n_streams);
+        for (int m : {1, 2, 3, 4, 6, 8})
+        {
+            const int kc = std::min(R, ks * m);
+            if (std::find(kcs.begin(), kcs.end(), kc) == kcs.end()) kcs.push_back(kc);
+        }
+        if (std::find(kcs.begin(), kcs.end(), saved.k_chunk) == kcs.end()) kcs.push_back(saved.k_chunk);
     }
+    else
+        for (int d = 1; d <= 64 && (R + d - 1) / d >= 1; d *= 2)
+        {
+            const int kc = (R + d - 1) / d;
+            if (kcs.empty() || kcs.back() != kc) kcs.push_back(kc);
+            if (kc == 1) break;
+        }
+    /* items per engine tile: thread items per block thread, or warp tiles
+     * per warp of a block */
     const int tile_mult[3] = {2, 8, 32};
+    const int warp_mult[3] = {1, 4, 16};
     double best = 1e300;
     Tune best_t = saved;
     for (int kc : kcs)
     {
-        for (int tm : tile_mult)
+        for (int mi = 0; mi < 3; ++mi)
         {
             Tune& t = w.tune[precision];
             t = saved;
             t.k_chunk = kc;
-            t.tile_items = t.block * tm;
+            t.tile_items = saved.warp_items ? (t.block / 32) * warp_mult[mi] : t.block * tile_mult[mi];
             ++w.tune_gen;
             c->eng.desc_dirty = true;
             int rc = ensure_descriptors(c);
@@ -569,10 +584,14 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
             BatchShape shape;
             rc = build_batch(c, 1, &rq, precision, resident * waves, false, shape);
             if (rc) return rc;
-            /* items in the timed prefix */
+            /* items in the timed prefix (of the first area) and the
+             * columns an item covers */
+            mwsep_area_dev v0 = w.areas[0].view;
+            set_chunking(v0, t.k_chunk, t.warp_items);
             const long long items = std::min<long long>(
-                (long long)(shape.it_end[cls] - shape.it_begin[cls]) * t.tile_items, cols * ((R + kc - 1) / kc));
+                (long long)(shape.it_end[cls] - shape.it_begin[cls]) * t.tile_items, v0.n_items);
             if (items <= 0) continue;
+            const double cols_per_item = t.warp_items ? (double)cols / ((double)v0.n_items / v0.n_kchunks) : 1.0;
             double ms = 1e300;
             for (int rep = 0; rep < 2; ++rep)
             {
@@ -581,7 +600,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
                 ms = std::min(ms, c->last_ms[4]);
             }
             /* ms per convolution point of the prefix -> a full evaluation */
-            const double points = (double)items * kc * C;
+            const double points = (double)items * cols_per_item * kc * C;
             const double full_points = 0.0 + (double)cols * R * C;
             const double pred = ms / points * full_points;
             if (pred < best)

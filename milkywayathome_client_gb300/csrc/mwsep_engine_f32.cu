@@ -27,29 +27,45 @@ __device__ __forceinline__ void load_area(mwsep_area_dev& dst, const mwsep_area_
     for (int i = threadIdx.x; i < (int)(sizeof(mwsep_area_dev) / 8); i += blockDim.x) d[i] = s[i];
 }
 
+/* cs: the block's column-constant scratch, kTileCols * ColWords<S>::N floats
+ * per warp (used by warp-tile items). */
 template <int S, int FORM>
 __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const mwsep_itile& t,
-                                      double* red, double2* out)
+                                      double* red, float* cs, double2* out)
 {
     double acc[1 + S];
 #pragma unroll
     for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
     const BgConsts bc = bg_consts(th);
-    for (long long item = t.item_begin + threadIdx.x; item < t.item_end; item += blockDim.x)
-        integral_item<S, FORM>(A, th, bc, item, acc);
+    if (A.warp_items)
+    {
+        const int warp = threadIdx.x >> 5;
+        constexpr int CW = PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N;
+        float* mine = cs + warp * mwsep::kTileCols * CW;
+        for (long long wt = t.item_begin + warp; wt < t.item_end; wt += blockDim.x >> 5)
+        {
+            if constexpr (PackedTile<S>::ok)
+                warp_tile2<S, FORM>(A, th, bc, wt, mine, acc);
+            else
+                warp_tile<S, FORM>(A, th, bc, wt, mine, acc);
+        }
+    }
+    else
+        for (long long item = t.item_begin + threadIdx.x; item < t.item_end; item += blockDim.x)
+            integral_item<S, FORM>(A, th, bc, item, acc);
     reduce_and_store<1 + S>(acc, 1 + th.n_streams, red, out);
 }
 
 template <int S>
 __device__ __forceinline__ void itile_form(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                           const mwsep_itile& t, double* red, double2* out)
+                                           const mwsep_itile& t, double* red, float* cs, double2* out)
 {
     switch (mwsep_bg_form(&th))
     {
-    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, t, red, out); break;
-    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, t, red, out); break;
-    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, t, red, out); break;
-    default: itile<S, BG_NONE>(A, th, t, red, out); break;
+    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, t, red, cs, out); break;
+    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, t, red, cs, out); break;
+    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, t, red, cs, out); break;
+    default: itile<S, BG_NONE>(A, th, t, red, cs, out); break;
     }
 }
 
@@ -59,6 +75,8 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
     __shared__ double red[2 * (CLS == 0 ? 5 : MWSEP_ENG_ICOMP) * 32];
+    __shared__ __align__(16) float cs[(kBlock / 32) * mwsep::kTileCols *
+                                      (CLS == 0 ? PackedTile<4>::W : ColWords<8>::N)];
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * CLS + 2];
     for (;;)
@@ -73,15 +91,15 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
         __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
         if (CLS == 1)
-            itile_form<8>(A, th, tile, red, out);
+            itile_form<8>(A, th, tile, red, cs, out);
         else
             switch (th.n_streams)
             {
-            case 0: itile_form<0>(A, th, tile, red, out); break;
-            case 1: itile_form<1>(A, th, tile, red, out); break;
-            case 2: itile_form<2>(A, th, tile, red, out); break;
-            case 3: itile_form<3>(A, th, tile, red, out); break;
-            default: itile_form<4>(A, th, tile, red, out); break;
+            case 0: itile_form<0>(A, th, tile, red, cs, out); break;
+            case 1: itile_form<1>(A, th, tile, red, cs, out); break;
+            case 2: itile_form<2>(A, th, tile, red, cs, out); break;
+            case 3: itile_form<3>(A, th, tile, red, cs, out); break;
+            default: itile_form<4>(A, th, tile, red, cs, out); break;
             }
         __syncthreads();
     }

@@ -46,6 +46,40 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32_kernel(co
                             partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams));
 }
 
+/* The same integral over warp tiles (A.warp_items == 1): each warp takes
+ * tiles wt = warp, warp + warps, ... of the grid. */
+template <int S, int FORM>
+__global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(const mwsep_area_dev A,
+                                                                  const mwsep_theta_consts* __restrict__ thetas,
+                                                                  double2* __restrict__ partials,
+                                                                  long long theta_stride)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ double red[2 * (1 + S) * 32];
+    constexpr int CW = PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N;
+    __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * CW];
+    load_theta(th, thetas + blockIdx.y);
+    __syncthreads();
+    if (mwsep_bg_form(&th) != FORM) return;
+
+    double acc[1 + S];
+#pragma unroll
+    for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
+
+    const BgConsts bc = bg_consts(th);
+    const int warp = threadIdx.x >> 5;
+    const long long warps = (long long)gridDim.x * (kBlock / 32);
+    for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
+    {
+        if constexpr (PackedTile<S>::ok)
+            warp_tile2<S, FORM>(A, th, bc, wt, cs[warp], acc);
+        else
+            warp_tile<S, FORM>(A, th, bc, wt, cs[warp], acc);
+    }
+    reduce_and_store<1 + S>(acc, 1 + th.n_streams, red,
+                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams));
+}
+
 /* calculate_likelihood per star (cpu/evaluation_optimized.c:665-717); the
  * density sums in FP32, everything after them in FP64. */
 template <int S>
@@ -82,15 +116,26 @@ int launch_integral(const mwsep_area_dev* A, const mwsep_theta_consts* th, const
     const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
     double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
-    switch (form)
-    {
-    case BG_HERNQUIST: integral_f32_kernel<S, BG_HERNQUIST><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
-    case BG_HERNQUIST_AUX:
-        integral_f32_kernel<S, BG_HERNQUIST_AUX><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
-        break;
-    case BG_GENERAL: integral_f32_kernel<S, BG_GENERAL><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
-    default: integral_f32_kernel<S, BG_NONE><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
-    }
+    if (A->warp_items)
+        switch (form)
+        {
+        case BG_HERNQUIST: integral_f32w_kernel<S, BG_HERNQUIST><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        case BG_HERNQUIST_AUX:
+            integral_f32w_kernel<S, BG_HERNQUIST_AUX><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
+            break;
+        case BG_GENERAL: integral_f32w_kernel<S, BG_GENERAL><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        default: integral_f32w_kernel<S, BG_NONE><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        }
+    else
+        switch (form)
+        {
+        case BG_HERNQUIST: integral_f32_kernel<S, BG_HERNQUIST><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        case BG_HERNQUIST_AUX:
+            integral_f32_kernel<S, BG_HERNQUIST_AUX><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
+            break;
+        case BG_GENERAL: integral_f32_kernel<S, BG_GENERAL><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        default: integral_f32_kernel<S, BG_NONE><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride); break;
+        }
     return (int)cudaGetLastError();
 }
 
@@ -106,20 +151,31 @@ int launch_likelihood(const mwsep_stars_dev* St, const mwsep_theta_consts* th, c
 
 } // namespace
 
+namespace {
+
+template <int S>
+cudaError_t f32_occupancy(int* b, int warp_items)
+{
+    return warp_items ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_f32w_kernel<S, BG_HERNQUIST>, kBlock, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_f32_kernel<S, BG_HERNQUIST>, kBlock, 0);
+}
+
+} // namespace
+
 /* Resident blocks per SM of the compensated integral kernel for S streams
- * (sizes the persistent grid). */
-extern "C" int mwsep_integral_f32_blocks_per_sm(int n_streams)
+ * (sizes the persistent grid); warp_items selects the warp-tile kernel. */
+extern "C" int mwsep_integral_f32_blocks_per_sm(int n_streams, int warp_items)
 {
     int b = 0;
     cudaError_t e;
     switch (n_streams)
     {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<0, BG_HERNQUIST>, kBlock, 0); break;
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<1, BG_HERNQUIST>, kBlock, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<2, BG_HERNQUIST>, kBlock, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<3, BG_HERNQUIST>, kBlock, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<4, BG_HERNQUIST>, kBlock, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, integral_f32_kernel<8, BG_HERNQUIST>, kBlock, 0); break;
+    case 0: e = f32_occupancy<0>(&b, warp_items); break;
+    case 1: e = f32_occupancy<1>(&b, warp_items); break;
+    case 2: e = f32_occupancy<2>(&b, warp_items); break;
+    case 3: e = f32_occupancy<3>(&b, warp_items); break;
+    case 4: e = f32_occupancy<4>(&b, warp_items); break;
+    default: e = f32_occupancy<8>(&b, warp_items); break;
     }
     if (e != cudaSuccess)
     {

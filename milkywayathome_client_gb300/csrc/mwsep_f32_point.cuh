@@ -109,7 +109,13 @@ struct Col
     float k2[SArr<S>::N], k2dl[SArr<S>::N], k0c[SArr<S>::N], d_hi[SArr<S>::N];
 };
 
-template <int S>
+/* FROM_HI = true gives the constants of the packed form, where t is
+ * measured from the float rb_hi (t' = r - rb_hi = t + rb_lo):
+ *   background  B2 (t' - rb_lo)^2 + Db = t' (B2 t' + L) + D,
+ *               L = -2 B2 rb_lo (kept in the rb_lo slot), D = Db + B2 rb_lo^2;
+ *   streams     offsets d = rb_hi - rs.
+ * The same quadratics, with the small rb_lo folded into the constants. */
+template <int S, bool FROM_HI = false>
 __device__ __forceinline__ void column_consts(const double* g, const mwsep_theta_consts& th, Col<S>& cc)
 {
     const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
@@ -117,10 +123,20 @@ __device__ __forceinline__ void column_consts(const double* g, const mwsep_theta
     const double iq2 = 1.0 / (th.q * th.q);
     const double perp = u1 * u1 + u2 * u2 * iq2;
     const double B2 = u0 * u0 + perp;
-    const double rb = MW_LBR_R * u0 / B2;
+    const double rb_exact = MW_LBR_R * u0 / B2;
+    const double Db = (MW_LBR_R * MW_LBR_R) * perp / B2;
     cc.B2 = (float)B2;
-    cc.Db = (float)((MW_LBR_R * MW_LBR_R) * perp / B2);
-    split(rb, cc.rb_hi, cc.rb_lo);
+    split(rb_exact, cc.rb_hi, cc.rb_lo);
+    double rb = rb_exact;
+    if (FROM_HI)
+    {
+        const double dl = rb_exact - (double)cc.rb_hi;
+        cc.rb_lo = (float)(-2.0 * B2 * dl);
+        cc.Db = (float)(Db + B2 * dl * dl);
+        rb = (double)cc.rb_hi;
+    }
+    else
+        cc.Db = (float)Db;
 #pragma unroll
     for (int s = 0; s < S; ++s)
     {
@@ -161,6 +177,39 @@ struct BgConsts
     float r0, aux_a, aux_b, aux_c, alpha, ad3;
 };
 
+/* One convolution point v = {r_hi, r_lo, weight, g}: adds its weighted
+ * background and stream densities into bgacc and sacc[]. */
+template <int S, int FORM>
+__device__ __forceinline__ void point(const float4 v, const Col<S>& cc, const BgConsts& bc, float& bgacc,
+                                      float (&sacc)[SArr<S>::N])
+{
+    const float t = (v.x - cc.rb_hi) + (v.y - cc.rb_lo);
+    if (FORM == BG_HERNQUIST || FORM == BG_HERNQUIST_AUX)
+    {
+        const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
+        const float y = rsqa(rg2);           /* 1 / rg */
+        const float rs = fmaf(rg2, y, bc.r0); /* rg + r0 */
+        const float den = rs * rs * rs;
+        bgacc = fmaf(v.z * y, rcpa(den), bgacc);
+        if (FORM == BG_HERNQUIST_AUX)
+            bgacc = fmaf(v.z, fmaf(fmaf(bc.aux_a, v.w, bc.aux_b), v.w, bc.aux_c), bgacc);
+    }
+    else if (FORM == BG_GENERAL)
+    {
+        const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
+        const float rg = rg2 * rsqa(rg2);
+        const float l2 = fmaf(bc.alpha, lg2a(rg), bc.ad3 * lg2a(rg + bc.r0));
+        bgacc = fmaf(v.z, ex2a(-l2), bgacc);
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        const float u = t + cc.d_hi[s];
+        const float arg = fmaf(u, fmaf(cc.k2[s], u, cc.k2dl[s]), cc.k0c[s]);
+        sacc[s] = fmaf(v.z, ex2a(arg), sacc[s]);
+    }
+}
+
 /* The density sums of one cell (or star) over its C convolution points:
  * points at p[n * stride], {r_hi, r_lo, weight, g}.  Plain FP32 sums in two
  * interleaved halves (more independent chains, smaller rounding). */
@@ -172,34 +221,7 @@ __device__ __forceinline__ void convolve(const float4* __restrict__ p, int strid
     float sa[SArr<S>::N], sb[SArr<S>::N];
 #pragma unroll
     for (int s = 0; s < S; ++s) sa[s] = sb[s] = 0.f;
-
-    auto point = [&](const float4 v, float& bgacc, float (&sacc)[SArr<S>::N]) {
-        const float t = (v.x - cc.rb_hi) + (v.y - cc.rb_lo);
-        if (FORM == BG_HERNQUIST || FORM == BG_HERNQUIST_AUX)
-        {
-            const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
-            const float y = rsqa(rg2);           /* 1 / rg */
-            const float rs = fmaf(rg2, y, bc.r0); /* rg + r0 */
-            const float den = rs * rs * rs;
-            bgacc = fmaf(v.z * y, rcpa(den), bgacc);
-            if (FORM == BG_HERNQUIST_AUX)
-                bgacc = fmaf(v.z, fmaf(fmaf(bc.aux_a, v.w, bc.aux_b), v.w, bc.aux_c), bgacc);
-        }
-        else if (FORM == BG_GENERAL)
-        {
-            const float rg2 = fmaf(cc.B2 * t, t, cc.Db);
-            const float rg = rg2 * rsqa(rg2);
-            const float l2 = fmaf(bc.alpha, lg2a(rg), bc.ad3 * lg2a(rg + bc.r0));
-            bgacc = fmaf(v.z, ex2a(-l2), bgacc);
-        }
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-        {
-            const float u = t + cc.d_hi[s];
-            const float arg = fmaf(u, fmaf(cc.k2[s], u, cc.k2dl[s]), cc.k0c[s]);
-            sacc[s] = fmaf(v.z, ex2a(arg), sacc[s]);
-        }
-    };
+    auto pt = [&](const float4 v, float& bgacc, float (&sacc)[SArr<S>::N]) { point<S, FORM>(v, cc, bc, bgacc, sacc); };
 
     /* four points per trip, loads issued before any arithmetic */
     int n = 0;
@@ -209,12 +231,12 @@ __device__ __forceinline__ void convolve(const float4* __restrict__ p, int strid
         const float4 v1 = p[(size_t)(n + 1) * stride];
         const float4 v2 = p[(size_t)(n + 2) * stride];
         const float4 v3 = p[(size_t)(n + 3) * stride];
-        point(v0, bga, sa);
-        point(v1, bgb, sb);
-        point(v2, bga, sa);
-        point(v3, bgb, sb);
+        pt(v0, bga, sa);
+        pt(v1, bgb, sb);
+        pt(v2, bga, sa);
+        pt(v3, bgb, sb);
     }
-    for (; n < C; ++n) point(p[(size_t)n * stride], bga, sa);
+    for (; n < C; ++n) pt(p[(size_t)n * stride], bga, sa);
     bg = bga + bgb;
 #pragma unroll
     for (int s = 0; s < S; ++s) st[s] = sa[s] + sb[s];
@@ -293,6 +315,347 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     acc[0] += kb.value() * idsj;
 #pragma unroll
     for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * idsj;
+}
+
+/* ---- warp tiles ----
+ * A warp tile is 32 mu-columns at one nu (one ids factor) and a run of
+ * r-bins.  The tile's convolution points, in the table's own (k, n) order,
+ * are dealt to the lanes in groups of 32 P: lane l holds points
+ * g + 32 i + l (i < P) of a group in registers, and the warp walks the
+ * tile's columns with each column's constants broadcast from shared memory.
+ * Every point is then evaluated against every column with no load in the
+ * inner loop.  The column constants are computed once per tile, one column
+ * per lane, in FP64. */
+template <int S>
+struct ColWords
+{
+    static constexpr int N = ((4 + 4 * S) + 3) / 4 * 4; /* floats, whole float4s */
+};
+
+template <int S>
+__device__ __forceinline__ void store_col(float* dst, const Col<S>& cc)
+{
+    dst[0] = cc.B2;
+    dst[1] = cc.Db;
+    dst[2] = cc.rb_hi;
+    dst[3] = cc.rb_lo;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        dst[4 + s] = cc.k2[s];
+        dst[4 + S + s] = cc.k2dl[s];
+        dst[4 + 2 * S + s] = cc.k0c[s];
+        dst[4 + 3 * S + s] = cc.d_hi[s];
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void load_col(const float* src, Col<S>& cc)
+{
+    constexpr int N = ColWords<S>::N;
+    float w[N];
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q)
+    {
+        const float4 x = reinterpret_cast<const float4*>(src)[q];
+        w[4 * q] = x.x;
+        w[4 * q + 1] = x.y;
+        w[4 * q + 2] = x.z;
+        w[4 * q + 3] = x.w;
+    }
+    cc.B2 = w[0];
+    cc.Db = w[1];
+    cc.rb_hi = w[2];
+    cc.rb_lo = w[3];
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        cc.k2[s] = w[4 + s];
+        cc.k2dl[s] = w[4 + S + s];
+        cc.k0c[s] = w[4 + 2 * S + s];
+        cc.d_hi[s] = w[4 + 3 * S + s];
+    }
+}
+
+/* One warp tile of an integral, called by all 32 lanes of a warp.  cs is
+ * this warp's shared scratch of mwsep::kTileCols * ColWords<S>::N floats (16-byte
+ * aligned).  Adds the tile's integrals (each lane its share, FP64) into
+ * acc. */
+template <int S, int FORM>
+__device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_theta_consts& th,
+                                          const BgConsts& bc, long long wt, float* __restrict__ cs,
+                                          double (&acc)[1 + S])
+{
+    constexpr int P = mwsep::TileP<S>::P;
+    constexpr int CW = ColWords<S>::N;
+    const int lane = threadIdx.x & 31;
+    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
+    const long long rest = wt / nmb;
+    const int mb = (int)(wt - rest * nmb);
+    const int kc = (int)(rest / A.nu_steps);
+    const int nu = (int)(rest - (long long)kc * A.nu_steps);
+    const int mu0 = mb * mwsep::kTileCols;
+    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+    if (lane < ncols)
+    {
+        Col<S> cc;
+        column_consts<S>(A.geom + 4 * ((size_t)(mu0 + lane) * A.nu_steps + nu), th, cc);
+        store_col<S>(cs + lane * CW, cc);
+    }
+    __syncwarp();
+    const int C = A.convolve;
+    const int k0 = kc * A.k_chunk;
+    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int nf = (k1 - k0) * C;
+    const float4* __restrict__ base = A.pts + (size_t)k0 * C;
+    const double idsv = A.ids[nu];
+    for (int g0 = 0; g0 < nf; g0 += 32 * P)
+    {
+        /* this lane's points of the group; past the tile's end a copy of its
+         * first point with zero weight */
+        float4 v[P];
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+        {
+            const int f = g0 + 32 * i + lane;
+            v[i] = base[f < nf ? f : 0];
+            if (f >= nf) v[i].z = 0.f;
+        }
+        float gb0 = 0.f, gb1 = 0.f, gs0[SArr<S>::N], gs1[SArr<S>::N];
+#pragma unroll
+        for (int s = 0; s < S; ++s) gs0[s] = gs1[s] = 0.f;
+        for (int j = 0; j < ncols; ++j)
+        {
+            Col<S> cc;
+            load_col<S>(cs + j * CW, cc);
+#pragma unroll
+            for (int i = 0; i < P; i += 2)
+            {
+                point<S, FORM>(v[i], cc, bc, gb0, gs0);
+                if (i + 1 < P) point<S, FORM>(v[i + 1], cc, bc, gb1, gs1);
+            }
+        }
+        if (FORM != BG_NONE) acc[0] += (double)(gb0 + gb1) * idsv;
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs0[s] + gs1[s]) * idsv;
+    }
+    /* q == 0: every cell's background is -irv[k] (times ids, not reff;
+     * :213-216, :504), the same for all the tile's columns */
+    if (FORM == BG_NONE && lane == 0)
+    {
+        double sum = 0.0;
+        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[k]);
+        acc[0] += sum * (double)ncols * idsv;
+    }
+    __syncwarp();
+}
+
+/* ---- packed warp tiles (FP32x2) ----
+ * The same warp tile with each lane's points taken two at a time in float2
+ * registers, so the FP32 arithmetic runs as packed f32x2 FMA/ADD/MUL
+ * (__ffma2_rn, __fadd2_rn, __fmul2_rn): half the FP32 instructions.  The
+ * column constants are kept duplicated ({c, c} pairs) in shared memory so
+ * they load as ready pairs.  The Hernquist reciprocal is shared by four
+ * points: with P2 = (d1 d3, d2 d4), i = 1 / (P2.x P2.y) and
+ * Q = (i P2.y, i P2.x) = (1/(d1 d3), 1/(d2 d4)), 1/d1 = Q.x d3 and so on --
+ * one SFU reciprocal and five multiplies instead of four reciprocals, which
+ * moves work from the SFU (the bound of this kernel) to the FMA pipe.  The
+ * product is clamped at FLT_MIN (a scale radius below ~1e-3 kpc would
+ * otherwise flush it). */
+typedef float2 f2;
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ f2 dup2(float a) { return make_float2(a, a); }
+
+/* Packed tiles are used up to 4 streams (their constants fit the registers). */
+template <int S>
+struct PackedTile
+{
+    static constexpr bool ok = S <= 4;
+    static constexpr int W = 2 * (4 + 4 * S); /* floats per column: every constant twice */
+    static constexpr int P = mwsep::TileP<S>::P; /* points per lane per group */
+};
+
+template <int S>
+struct Col2
+{
+    f2 B2, D, nrb_hi, L; /* column_consts<S, true>: D and L of t' (B2 t' + L) + D */
+    f2 k2[SArr<S>::N], k2dl[SArr<S>::N], k0c[SArr<S>::N], d_hi[SArr<S>::N];
+};
+
+template <int S>
+__device__ __forceinline__ void store_col2(float* dst, const Col<S>& cc)
+{
+    auto put = [&](int i, float v) {
+        dst[2 * i] = v;
+        dst[2 * i + 1] = v;
+    };
+    put(0, cc.B2);
+    put(1, cc.Db);
+    put(2, -cc.rb_hi);
+    put(3, cc.rb_lo);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        put(4 + 4 * s, cc.k2[s]);
+        put(5 + 4 * s, cc.k2dl[s]);
+        put(6 + 4 * s, cc.k0c[s]);
+        put(7 + 4 * s, cc.d_hi[s]);
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void load_col2(const float* src, Col2<S>& c)
+{
+    const float4* q = reinterpret_cast<const float4*>(src);
+    float4 x = q[0];
+    c.B2 = make_float2(x.x, x.y);
+    c.D = make_float2(x.z, x.w);
+    x = q[1];
+    c.nrb_hi = make_float2(x.x, x.y);
+    c.L = make_float2(x.z, x.w);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        x = q[2 + 2 * s];
+        c.k2[s] = make_float2(x.x, x.y);
+        c.k2dl[s] = make_float2(x.z, x.w);
+        x = q[3 + 2 * s];
+        c.k0c[s] = make_float2(x.x, x.y);
+        c.d_hi[s] = make_float2(x.z, x.w);
+    }
+}
+
+/* Two pairs of points (four points) against one column. */
+template <int S, int FORM>
+__device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, const f2 GA, const f2 XB, const f2 YB,
+                                        const f2 WB, const f2 GB, const Col2<S>& c, const BgConsts& bc, f2& bg,
+                                        f2 (&st)[SArr<S>::N])
+{
+    /* t' = (r_hi - rb_hi) + r_lo */
+    const f2 tA = add2(add2(XA, c.nrb_hi), YA);
+    const f2 tB = add2(add2(XB, c.nrb_hi), YB);
+    if (FORM == BG_HERNQUIST || FORM == BG_HERNQUIST_AUX)
+    {
+        const f2 r0 = dup2(bc.r0);
+        const f2 gA = fma2(tA, fma2(c.B2, tA, c.L), c.D);
+        const f2 gB = fma2(tB, fma2(c.B2, tB, c.L), c.D);
+        const f2 yA = make_float2(rsqa(gA.x), rsqa(gA.y));
+        const f2 yB = make_float2(rsqa(gB.x), rsqa(gB.y));
+        const f2 sA = fma2(gA, yA, r0);
+        const f2 sB = fma2(gB, yB, r0);
+        const f2 dA = mul2(mul2(sA, sA), sA);
+        const f2 dB = mul2(mul2(sB, sB), sB);
+        const f2 p2 = mul2(dA, dB);
+        const float i = rcpa(fmaxf(p2.x * p2.y, 1.17549435e-38f));
+        const f2 q = make_float2(i * p2.y, i * p2.x);
+        bg = fma2(mul2(WA, yA), mul2(q, dB), bg);
+        bg = fma2(mul2(WB, yB), mul2(q, dA), bg);
+        if (FORM == BG_HERNQUIST_AUX)
+        {
+            const f2 a = dup2(bc.aux_a), b = dup2(bc.aux_b), cc = dup2(bc.aux_c);
+            bg = fma2(WA, fma2(fma2(a, GA, b), GA, cc), bg);
+            bg = fma2(WB, fma2(fma2(a, GB, b), GB, cc), bg);
+        }
+    }
+    else if (FORM == BG_GENERAL)
+    {
+        const f2 r0 = dup2(bc.r0), al = dup2(bc.alpha), ad = dup2(bc.ad3);
+        const f2 gA = fma2(tA, fma2(c.B2, tA, c.L), c.D);
+        const f2 gB = fma2(tB, fma2(c.B2, tB, c.L), c.D);
+        const f2 rA = mul2(gA, make_float2(rsqa(gA.x), rsqa(gA.y)));
+        const f2 rB = mul2(gB, make_float2(rsqa(gB.x), rsqa(gB.y)));
+        const f2 sA = add2(rA, r0), sB = add2(rB, r0);
+        const f2 lA = fma2(al, make_float2(lg2a(rA.x), lg2a(rA.y)), mul2(ad, make_float2(lg2a(sA.x), lg2a(sA.y))));
+        const f2 lB = fma2(al, make_float2(lg2a(rB.x), lg2a(rB.y)), mul2(ad, make_float2(lg2a(sB.x), lg2a(sB.y))));
+        bg = fma2(WA, make_float2(ex2a(-lA.x), ex2a(-lA.y)), bg);
+        bg = fma2(WB, make_float2(ex2a(-lB.x), ex2a(-lB.y)), bg);
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        const f2 uA = add2(tA, c.d_hi[s]);
+        const f2 uB = add2(tB, c.d_hi[s]);
+        const f2 aA = fma2(uA, fma2(c.k2[s], uA, c.k2dl[s]), c.k0c[s]);
+        const f2 aB = fma2(uB, fma2(c.k2[s], uB, c.k2dl[s]), c.k0c[s]);
+        st[s] = fma2(WA, make_float2(ex2a(aA.x), ex2a(aA.y)), st[s]);
+        st[s] = fma2(WB, make_float2(ex2a(aB.x), ex2a(aB.y)), st[s]);
+    }
+}
+
+/* warp_tile with packed arithmetic; cs holds kTileCols * PackedTile<S>::W
+ * floats for this warp. */
+template <int S, int FORM>
+__device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_theta_consts& th,
+                                           const BgConsts& bc, long long wt, float* __restrict__ cs,
+                                           double (&acc)[1 + S])
+{
+    constexpr int P = PackedTile<S>::P;
+    constexpr int NP = P / 2;
+    constexpr int CW = PackedTile<S>::W;
+    static_assert(NP % 2 == 0, "pairs are taken two at a time");
+    const int lane = threadIdx.x & 31;
+    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
+    const long long rest = wt / nmb;
+    const int mb = (int)(wt - rest * nmb);
+    const int kc = (int)(rest / A.nu_steps);
+    const int nu = (int)(rest - (long long)kc * A.nu_steps);
+    const int mu0 = mb * mwsep::kTileCols;
+    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+    if (lane < ncols)
+    {
+        Col<S> cc;
+        column_consts<S, true>(A.geom + 4 * ((size_t)(mu0 + lane) * A.nu_steps + nu), th, cc);
+        store_col2<S>(cs + lane * CW, cc);
+    }
+    __syncwarp();
+    const int C = A.convolve;
+    const int k0 = kc * A.k_chunk;
+    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int nf = (k1 - k0) * C;
+    const float4* __restrict__ base = A.pts + (size_t)k0 * C;
+    const double idsv = A.ids[nu];
+    for (int g0 = 0; g0 < nf; g0 += 32 * P)
+    {
+        /* pair m = this lane's points g0 + 64 m + lane and g0 + 64 m + 32 + lane;
+         * past the tile's end a copy of its first point with zero weight */
+        f2 X[NP], Y[NP], Wt[NP], G[NP];
+#pragma unroll
+        for (int m = 0; m < NP; ++m)
+        {
+            const int fa = g0 + 64 * m + lane, fb = fa + 32;
+            float4 a = base[fa < nf ? fa : 0];
+            float4 b = base[fb < nf ? fb : 0];
+            if (fa >= nf) a.z = 0.f;
+            if (fb >= nf) b.z = 0.f;
+            X[m] = make_float2(a.x, b.x);
+            Y[m] = make_float2(a.y, b.y);
+            Wt[m] = make_float2(a.z, b.z);
+            G[m] = make_float2(a.w, b.w);
+        }
+        f2 gb = make_float2(0.f, 0.f), gs[SArr<S>::N];
+#pragma unroll
+        for (int s = 0; s < S; ++s) gs[s] = make_float2(0.f, 0.f);
+        for (int j = 0; j < ncols; ++j)
+        {
+            Col2<S> c;
+            load_col2<S>(cs + j * CW, c);
+#pragma unroll
+            for (int m = 0; m < NP; m += 2)
+                points4<S, FORM>(X[m], Y[m], Wt[m], G[m], X[m + 1], Y[m + 1], Wt[m + 1], G[m + 1], c, bc, gb, gs);
+        }
+        if (FORM != BG_NONE) acc[0] += (double)(gb.x + gb.y) * idsv;
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs[s].x + gs[s].y) * idsv;
+    }
+    if (FORM == BG_NONE && lane == 0)
+    {
+        double sum = 0.0;
+        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[k]);
+        acc[0] += sum * (double)ncols * idsv;
+    }
+    __syncwarp();
 }
 
 /* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717):

@@ -344,9 +344,34 @@ void default_tune(mwsep_ctx* c, Wedge& w)
     {
         Tune& t = w.tune[prec];
         t.block = 256;
+        t.warp_items = (prec == MWSEP_MIXED_F32 && env_long("MWSEP_F32_WARP_TILES", 1) != 0) ? 1 : 0;
         const int per_sm = prec == MWSEP_PLAIN_F64 ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
-                                                   : mwsep_integral_f32_blocks_per_sm(p.n_streams);
+                                                   : mwsep_integral_f32_blocks_per_sm(p.n_streams, t.warp_items);
         const long long threads = (long long)c->sm_count * per_sm * t.block;
+        if (t.warp_items)
+        {
+            /* warp tiles: ~32 per warp, r-chunks of whole lane groups */
+            long long tiles_per_chunk = 0;
+            for (int a = 0; a < p.n_areas; ++a)
+                tiles_per_chunk = std::max(tiles_per_chunk,
+                                           mwsep::warp_tile_count(p.area[a].mu_steps, p.area[a].nu_steps, 1));
+            const long long want = threads / 32 * 32;
+            long long nk = (want + tiles_per_chunk - 1) / std::max<long long>(tiles_per_chunk, 1);
+            nk = std::max<long long>(1, std::min<long long>(nk, max_r));
+            int kc = (int)((max_r + nk - 1) / nk);
+            const int ks = warp_tile_kstep(p.convolve, p.n_streams);
+            if (kc >= ks) kc = kc / ks * ks;
+            t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", kc);
+            long long g = (long long)c->sm_count * per_sm;
+            g = env_long("MWSEP_TUNE_GRID_F32", g);
+            t.grid = (int)std::max<long long>(1, g);
+            t.lk_block = 256;
+            t.lk_grid = occupancy_grid(c, t.lk_block, std::max(w.n_stars, 1));
+            t.tile_items = 8 * 4; /* engine: 4 warp tiles per warp of a block */
+            t.tile_stars = 1024;
+            t.tuned = false;
+            continue;
+        }
         const long long want_items = threads * 48;
         long long chunks = (want_items + max_cols - 1) / std::max<long long>(max_cols, 1);
         chunks = std::max<long long>(1, std::min<long long>(chunks, max_r));
@@ -457,11 +482,26 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
 
 } // namespace
 
-void set_chunking(mwsep_area_dev& v, int k_chunk)
+void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items)
 {
     v.k_chunk = std::max(1, std::min(k_chunk, v.r_steps));
     v.n_kchunks = (v.r_steps + v.k_chunk - 1) / v.k_chunk;
-    v.n_items = (long long)v.n_cols * v.n_kchunks;
+    v.warp_items = warp_items ? 1 : 0;
+    v.n_items = warp_items ? mwsep::warp_tile_count(v.mu_steps, v.nu_steps, v.n_kchunks)
+                           : (long long)v.n_cols * v.n_kchunks;
+}
+
+int warp_tile_kstep(int convolve, int n_streams)
+{
+    const int group = 32 * (n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
+    int a = group, b = std::max(convolve, 1);
+    while (b)
+    {
+        const int t = a % b;
+        a = b;
+        b = t;
+    }
+    return group / a;
 }
 
 int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r)
@@ -639,7 +679,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     for (int a = 0; a < A; ++a)
     {
         mwsep_area_dev v = w.areas[a].view;
-        set_chunking(v, t.k_chunk);
+        set_chunking(v, t.k_chunk, t.warp_items);
         sh.area_index = a;
         if (precision == MWSEP_PLAIN_F64)
         {

@@ -54,10 +54,12 @@ typedef struct
 {
     int mu_steps, nu_steps, r_steps, convolve;
     int n_cols;          /* mu_steps * nu_steps */
-    int k_chunk;         /* r-bins per thread */
+    int k_chunk;         /* r-bins per item */
     int n_kchunks;       /* ceil(r_steps / k_chunk) */
-    int pad0;
-    long long n_items;   /* n_cols * n_kchunks */
+    int warp_items;      /* 0: an item is (column, r-chunk), one thread;
+                            1: an item is a warp tile (32 mu-columns at one nu, r-chunk) */
+    long long n_items;   /* thread items: n_cols * n_kchunks;
+                            warp tiles: n_kchunks * nu_steps * ceil(mu_steps / 32) */
     const double* geom;      /* [mu][nu] x 4: bsin, bcos, lsin, lcos */
     const double* r_point;   /* [R][C] */
     const double* qw;        /* [R][C]  qw_r3_N */
@@ -86,6 +88,26 @@ typedef struct
     const double* b;
     const double* r;
 } mwsep_stars_dev;
+
+#ifdef __cplusplus
+namespace mwsep {
+/* Warp tiles of the compensated integral: 32 mu-columns at one nu and a run
+ * of r-bins; lanes hold P convolution points each per group. */
+constexpr int kTileCols = 32;
+#ifndef MWSEP_F32_TILE_P
+#define MWSEP_F32_TILE_P 12 /* a multiple of 4 (pairs are taken two at a time) */
+#endif
+template <int S>
+struct TileP
+{
+    static constexpr int P = S <= 4 ? MWSEP_F32_TILE_P : 6;
+};
+MWSEP_HD inline long long warp_tile_count(int mu_steps, int nu_steps, int n_kchunks)
+{
+    return (long long)n_kchunks * nu_steps * ((mu_steps + kTileCols - 1) / kTileCols);
+}
+} // namespace mwsep
+#endif
 
 /* Per-evaluation likelihood sums written by the reduction kernels:
  * [0] sum of log10 p (prob_sum), [1] zero-probability count, [2] bg-only
@@ -212,7 +234,7 @@ int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_con
                                 const mwsep_launch_shape* shape, const double* integrals,
                                 double2* partials, void* stream);
 /* Resident blocks per SM of the integral kernels (persistent-grid sizing). */
-int mwsep_integral_f32_blocks_per_sm(int n_streams);
+int mwsep_integral_f32_blocks_per_sm(int n_streams, int warp_items);
 int mwsep_integral_f64_blocks_per_sm(int n_streams, int block);
 /* Reduce per-block compensated partials of every area into area integrals
  * and subtract the cut areas (cpu/evaluation_optimized.c:584-593):

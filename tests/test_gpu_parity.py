@@ -152,3 +152,23 @@ def test_c_client_matches_reference(built_library, mixed):
     if not mixed:
         # printed with %.20lf: compare at the printed precision
         assert abs(bg - g["background_integral"]) <= max(1e-12 * abs(g["background_integral"]), 1e-20)
+
+
+@pytest.mark.parametrize("name", ["three_streams", "cut_area"])
+def test_q_zero_background_integral(gpu_ctx, oracle_built, name):
+    """q == 0: every cell's background is -1 times its volume, no density
+    (cpu/evaluation_optimized.c:213-216).  Only the background integral is
+    comparable (the reference's stream terms then read stale coordinates)."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    ap = mw.AstronomyParameters.read(pf)
+    theta = list(g["theta"])
+    assert ap.struct.background_optimize[1]  # q is theta[0] in these cases
+    theta[0] = 0.0
+    _setup(gpu_ctx, name)
+    want = oracle_built.Oracle(pf, sf).integrals(theta)[0][0]
+    r64 = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_F64)
+    r32 = gpu_ctx.evaluate(theta, mw.MWSEP_MIXED_F32)
+    assert _close_rel(r64.background_integral, want, REL_INT_F64), (r64.background_integral, want)
+    # the compensated form sums the volumes rounded to FP32 once each
+    assert _close_rel(r32.background_integral, want, 1e-6), (r32.background_integral, want)
