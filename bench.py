@@ -316,19 +316,27 @@ def run_gb300_arm(args, ws, rank, local):
     e2e_value = ws / e2e_step
     e2e_logl = v - 3.0
 
-    # roofline of the dominant kernel (the compensated integral)
+    # roofline of the dominant kernel (the compensated integral, packed warp
+    # tiles).  Per convolution point it issues 11.25 + 4S FP32 lane-ops
+    # (t 2, halo quadratic 2, rg + r0 1, cube 2, w/rg 1, the reciprocal shared
+    # by four points 2.25, accumulate 1; per stream offset, two-FMA exponent,
+    # accumulate) and 1.25 + S SFU ops (rsqrt, a quarter rcp, S ex2).  Its
+    # peak is the point rate of the slower of the two pipes at the rates the
+    # library's microbenchmark measures on this GPU.
     cell_pts, star_pts = points_per_eval(files)
-    mufu_per_point = 2 + S  # rsqrt + rcp for the halo, one ex2 per stream
+    fp32_ops = 11.25 + 4 * S
+    sfu_s_per_point = 1.0 / (peaks.rsqrt_gops * 1e9) + 0.25 / (peaks.rcp_gops * 1e9) + S / (peaks.ex2_gops * 1e9)
+    fma_s_per_point = fp32_ops / (peaks.fp32_fma_tflops * 1e12 / 2.0)
+    peak = 1.0 / max(sfu_s_per_point, fma_s_per_point) / 1e9
     integ_s = statistics.median(integ_ms) * 1e-3
-    achieved = cell_pts * mufu_per_point / integ_s / 1e9
-    # peak for this op mix: the SFU time of one point at the measured rates
-    peak = mufu_per_point / (1.0 / peaks.rsqrt_gops + 1.0 / peaks.rcp_gops + S / peaks.ex2_gops)
-    traffic = traffic_from_profiles("integral_f32_config1")
-    roofline = {"bound": "sfu", "achieved": achieved, "peak": peak, "unit": "Gop/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "integral_f32_kernel",
-                "peak_source": "measured (project pipe microbenchmark, mwsep_measure_pipe_peaks): "
-                               "rsqrt, rcp and ex2 rates weighted by this kernel's op mix",
-                "work_per_point": f"{mufu_per_point} SFU ops (rsqrt, rcp, {S} ex2)",
+    achieved = cell_pts / integ_s / 1e9
+    traffic = traffic_from_profiles("integral_f32w_config1")
+    roofline = {"bound": "fma+sfu", "achieved": achieved, "peak": peak, "unit": "Gpoint/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "integral_f32w_kernel (packed warp tiles)",
+                "peak_source": "measured (project pipe microbenchmark, mwsep_measure_pipe_peaks): FP32 FMA, "
+                               "rsqrt, rcp and ex2 rates, at this kernel's per-point op mix",
+                "work_per_point": f"{fp32_ops} FP32 lane-ops + {1.25 + S} SFU ops",
+                "binding_pipe": "fma" if fma_s_per_point >= sfu_s_per_point else "sfu",
                 "points_per_launch": cell_pts}
 
     out = {
