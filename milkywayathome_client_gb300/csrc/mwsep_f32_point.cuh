@@ -455,13 +455,12 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
  * registers, so the FP32 arithmetic runs as packed f32x2 FMA/ADD/MUL
  * (__ffma2_rn, __fadd2_rn, __fmul2_rn): half the FP32 instructions.  The
  * column constants are kept duplicated ({c, c} pairs) in shared memory so
- * they load as ready pairs.  The Hernquist reciprocal is shared by four
- * points: with P2 = (d1 d3, d2 d4), i = 1 / (P2.x P2.y) and
- * Q = (i P2.y, i P2.x) = (1/(d1 d3), 1/(d2 d4)), 1/d1 = Q.x d3 and so on --
- * one SFU reciprocal and five multiplies instead of four reciprocals, which
- * moves work from the SFU (the bound of this kernel) to the FMA pipe.  The
- * product is clamped at FLT_MIN (a scale radius below ~1e-3 kpc would
- * otherwise flush it). */
+ * they load as ready pairs.  The four Hernquist terms w_i / (rg_i d_i),
+ * d_i = (rg_i + r0)^3, of two pairs are added as one fraction
+ *   N / D,  N = (wy1 d2 + wy2 d1) D34 + (wy3 d4 + wy4 d3) D12,  D = D12 D34,
+ * with one SFU reciprocal instead of four, which moves work from the SFU to
+ * the FMA pipe (the two are the bound of this kernel).  D is clamped at
+ * FLT_MIN (a scale radius below ~1e-3 kpc would otherwise flush it). */
 typedef float2 f2;
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
@@ -531,7 +530,7 @@ __device__ __forceinline__ void load_col2(const float* src, Col2<S>& c)
 template <int S, int FORM>
 __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, const f2 GA, const f2 XB, const f2 YB,
                                         const f2 WB, const f2 GB, const Col2<S>& c, const BgConsts& bc, f2& bg,
-                                        f2 (&st)[SArr<S>::N])
+                                        f2 (&stA)[SArr<S>::N], f2 (&stB)[SArr<S>::N])
 {
     /* t' = (r_hi - rb_hi) + r_lo */
     const f2 tA = add2(add2(XA, c.nrb_hi), YA);
@@ -547,11 +546,13 @@ __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, c
         const f2 sB = fma2(gB, yB, r0);
         const f2 dA = mul2(mul2(sA, sA), sA);
         const f2 dB = mul2(mul2(sB, sB), sB);
-        const f2 p2 = mul2(dA, dB);
-        const float i = rcpa(fmaxf(p2.x * p2.y, 1.17549435e-38f));
-        const f2 q = make_float2(i * p2.y, i * p2.x);
-        bg = fma2(mul2(WA, yA), mul2(q, dB), bg);
-        bg = fma2(mul2(WB, yB), mul2(q, dA), bg);
+        /* sum_i w_i y_i / d_i over the four points as one fraction N / D:
+         * one reciprocal and one accumulation per four points */
+        const f2 wyA = mul2(WA, yA), wyB = mul2(WB, yB);
+        const float nA = fmaf(wyA.x, dA.y, wyA.y * dA.x), DA = dA.x * dA.y;
+        const float nB = fmaf(wyB.x, dB.y, wyB.y * dB.x), DB = dB.x * dB.y;
+        const float num = fmaf(nA, DB, nB * DA);
+        bg.x = fmaf(num, rcpa(fmaxf(DA * DB, 1.17549435e-38f)), bg.x);
         if (FORM == BG_HERNQUIST_AUX)
         {
             const f2 a = dup2(bc.aux_a), b = dup2(bc.aux_b), cc = dup2(bc.aux_c);
@@ -579,8 +580,8 @@ __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, c
         const f2 uB = add2(tB, c.d_hi[s]);
         const f2 aA = fma2(uA, fma2(c.k2[s], uA, c.k2dl[s]), c.k0c[s]);
         const f2 aB = fma2(uB, fma2(c.k2[s], uB, c.k2dl[s]), c.k0c[s]);
-        st[s] = fma2(WA, make_float2(ex2a(aA.x), ex2a(aA.y)), st[s]);
-        st[s] = fma2(WB, make_float2(ex2a(aB.x), ex2a(aB.y)), st[s]);
+        stA[s] = fma2(WA, make_float2(ex2a(aA.x), ex2a(aA.y)), stA[s]);
+        stB[s] = fma2(WB, make_float2(ex2a(aB.x), ex2a(aB.y)), stB[s]);
     }
 }
 
@@ -637,14 +638,20 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
         f2 gb = make_float2(0.f, 0.f), gs[SArr<S>::N];
 #pragma unroll
         for (int s = 0; s < S; ++s) gs[s] = make_float2(0.f, 0.f);
+        f2 gs2[SArr<S>::N]; /* the B pairs' stream sums: two independent chains */
+#pragma unroll
+        for (int s = 0; s < S; ++s) gs2[s] = make_float2(0.f, 0.f);
         for (int j = 0; j < ncols; ++j)
         {
             Col2<S> c;
             load_col2<S>(cs + j * CW, c);
 #pragma unroll
             for (int m = 0; m < NP; m += 2)
-                points4<S, FORM>(X[m], Y[m], Wt[m], G[m], X[m + 1], Y[m + 1], Wt[m + 1], G[m + 1], c, bc, gb, gs);
+                points4<S, FORM>(X[m], Y[m], Wt[m], G[m], X[m + 1], Y[m + 1], Wt[m + 1], G[m + 1], c, bc, gb, gs,
+                                 gs2);
         }
+#pragma unroll
+        for (int s = 0; s < S; ++s) gs[s] = add2(gs[s], gs2[s]);
         if (FORM != BG_NONE) acc[0] += (double)(gb.x + gb.y) * idsv;
 #pragma unroll
         for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs[s].x + gs[s].y) * idsv;
