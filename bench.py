@@ -317,14 +317,14 @@ def run_gb300_arm(args, ws, rank, local):
     e2e_logl = v - 3.0
 
     # roofline of the dominant kernel (the compensated integral, packed warp
-    # tiles).  Per convolution point it issues 11.25 + 4S FP32 lane-ops
-    # (t 2, halo quadratic 2, rg + r0 1, cube 2, w/rg 1, the reciprocal shared
-    # by four points 2.25, accumulate 1; per stream offset, two-FMA exponent,
-    # accumulate) and 1.25 + S SFU ops (rsqrt, a quarter rcp, S ex2).  Its
+    # tiles).  Per convolution point it issues 10.5 + 4S FP32 lane-ops
+    # (t 2, halo quadratic 2, rg + r0 1, cube 2, the four-point fraction
+    # sum 3.5; per stream offset, two-FMA exponent, accumulate) and 1.25 + S
+    # SFU ops (rsqrt, a quarter rcp, S ex2).  Its
     # peak is the point rate of the slower of the two pipes at the rates the
     # library's microbenchmark measures on this GPU.
     cell_pts, star_pts = points_per_eval(files)
-    fp32_ops = 11.25 + 4 * S
+    fp32_ops = 10.5 + 4 * S
     sfu_s_per_point = 1.0 / (peaks.rsqrt_gops * 1e9) + 0.25 / (peaks.rcp_gops * 1e9) + S / (peaks.ex2_gops * 1e9)
     fma_s_per_point = fp32_ops / (peaks.fp32_fma_tflops * 1e12 / 2.0)
     peak = 1.0 / max(sfu_s_per_point, fma_s_per_point) / 1e9
