@@ -180,6 +180,13 @@ const char* mwsep_status_string(int status);
 int mwsep_last_error(void);
 /* Library build/version string. */
 const char* mwsep_version(void);
+/* Device-side index checks of a debug build (compiled with
+ * -DMWSEP_DEVICE_CHECKS=1): *enabled says whether this library has them;
+ * *failures counts table indices found out of range since the last call
+ * (each was redirected to element 0 instead of being read) and *first is
+ * the first one as (tag << 48 | index).  Reading resets the counters.  No
+ * reference counterpart. */
+int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, unsigned long long* first);
 
 /* ------------------------------------------------------------------ */
 /* Problem I/O, same file formats and semantics as the reference        */

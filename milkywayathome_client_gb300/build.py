@@ -96,7 +96,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(u[0], list(u[1]) + list(extra_flags), verbose, build_dir), UNITS))
     tmp = lib_path + ".tmp"
-    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lpthread"]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lpthread", "-ldl"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

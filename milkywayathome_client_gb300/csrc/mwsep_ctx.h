@@ -10,6 +10,7 @@
 #define MWSEP_CTX_H
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -45,6 +46,15 @@
     } while (0)
 
 namespace mwsep {
+
+/* An NVTX range over a host-side phase (a no-op unless a profiler listens). */
+struct Range
+{
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 /* A grow-only device buffer; `total` tracks the context's device bytes. */
 struct DevBuf

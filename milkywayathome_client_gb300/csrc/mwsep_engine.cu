@@ -252,6 +252,8 @@ mwsep_engine_args engine_args(mwsep_ctx* c)
     a.lpart = e.d_lpart.as<double2>();
     a.out = e.d_out.as<double>();
     a.counters = e.d_counters.as<int>();
+    a.n_area_desc = e.n_area_desc;
+    a.n_star_desc = e.n_star_desc;
     return a;
 }
 
@@ -300,6 +302,7 @@ int issue(mwsep_ctx* c, int precision, bool has_i[2], bool has_l[2], bool with_l
  * matches, otherwise capture a new one. */
 int run_batch(mwsep_ctx* c, int precision, const BatchShape& shape, bool with_likelihood, bool use_graph)
 {
+    mwsep::Range nvtx_range("mwsep.engine_batch");
     EngineState& e = c->eng;
     /* counters: per class next/end for integral and likelihood tiles */
     int* cnt = e.h_counters.as<int>();
@@ -510,6 +513,7 @@ extern "C" int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* c, int id, int precis
  * evaluation from the time per convolution point, and keep the fastest. */
 extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* predicted_ms)
 {
+    mwsep::Range nvtx_range("mwsep.autotune");
     if (!c || id < 0 || id >= (int)c->wedges.size()) return mwsep_fail(MWSEP_ERR_ARG);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
     Wedge& w = *c->wedges[id];

@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
         const int t = s_tile;
         if (t >= n_tiles) break;
         const mwsep_itile tile = a.itiles[t];
-        load_theta(th, a.thetas + tile.req);
-        load_area(A, a.areas + tile.area_desc);
+        load_theta(th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10));
+        load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
         __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
         if (CLS == 1)
@@ -132,9 +132,10 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
         const int t = s_tile;
         if (t >= n_tiles) break;
         const mwsep_ltile tile = a.ltiles[t];
-        load_theta(th, a.thetas + tile.req);
+        load_theta(th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10));
         __syncthreads();
-        const mwsep_stars_dev St = a.stars[a.reqs[tile.req].stars];
+        const mwsep_stars_dev St =
+            a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
         if (CLS == 1)
@@ -179,3 +180,5 @@ extern "C" int mwsep_engine_f32_blocks_per_sm(int phase, int cls)
     }
     return b > 0 ? b : 1;
 }
+
+MWSEP_CHECKS_READER(mwsep_checks_engine_f32)

@@ -217,3 +217,5 @@ extern "C" int mwsep_launch_likelihood_f32(const mwsep_stars_dev* stars, const m
     default: return launch_likelihood<8>(stars, th_dev, sh, integrals, partials, st);
     }
 }
+
+MWSEP_CHECKS_READER(mwsep_checks_f32)

@@ -29,6 +29,7 @@
 #include <math.h>
 #include "mwsep_internal.h"
 #include "mwsep_reduce.cuh"
+#include "mwsep_checks.cuh"
 
 namespace mwsep {
 namespace f32 {
@@ -292,7 +293,7 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const int kc = (int)(item / A.n_cols);
     const int col = (int)(item - (long long)kc * A.n_cols);
     Col<S> cc;
-    column_consts<S>(A.geom + 4 * (size_t)col, th, cc);
+    column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1), th, cc);
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
     fkahan kb, ks[SArr<S>::N];
@@ -302,16 +303,16 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     for (int k = k0; k < k1; ++k)
     {
         float bg, st[SArr<S>::N];
-        convolve<S, FORM>(A.pts + (size_t)k * C, 1, C, cc, bc, bg, st);
+        convolve<S, FORM>(A.pts + (size_t)MWSEP_IDX(k, A.r_steps, 2) * C, 1, C, cc, bc, bg, st);
         /* q == 0: bg = -1, times V but not reff (:213-216, :504) */
-        if (FORM == BG_NONE) bg = -(float)A.irv[k];
+        if (FORM == BG_NONE) bg = -(float)A.irv[MWSEP_IDX(k, A.r_steps, 4)];
         kb.add(bg);
 #pragma unroll
         for (int s = 0; s < S; ++s) ks[s].add(st[s]);
     }
     /* the table weights carry reff*irv; the nu-slab factor ids[j] and the
      * hand-off to FP64 happen once per item */
-    const double idsj = A.ids[col % A.nu_steps];
+    const double idsj = A.ids[MWSEP_IDX(col % A.nu_steps, A.nu_steps, 3)];
     acc[0] += kb.value() * idsj;
 #pragma unroll
     for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * idsj;
@@ -399,7 +400,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
     if (lane < ncols)
     {
         Col<S> cc;
-        column_consts<S>(A.geom + 4 * ((size_t)(mu0 + lane) * A.nu_steps + nu), th, cc);
+        column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1), th, cc);
         store_col<S>(cs + lane * CW, cc);
     }
     __syncwarp();
@@ -407,8 +408,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
     const int nf = (k1 - k0) * C;
-    const float4* __restrict__ base = A.pts + (size_t)k0 * C;
-    const double idsv = A.ids[nu];
+    const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
     {
         /* this lane's points of the group; past the tile's end a copy of its
@@ -418,7 +418,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
         for (int i = 0; i < P; ++i)
         {
             const int f = g0 + 32 * i + lane;
-            v[i] = base[f < nf ? f : 0];
+            v[i] = A.pts[MWSEP_IDX((size_t)k0 * C + (f < nf ? f : 0), (size_t)A.r_steps * C, 2)];
             if (f >= nf) v[i].z = 0.f;
         }
         float gb0 = 0.f, gb1 = 0.f, gs0[SArr<S>::N], gs1[SArr<S>::N];
@@ -444,7 +444,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
     if (FORM == BG_NONE && lane == 0)
     {
         double sum = 0.0;
-        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[k]);
+        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[MWSEP_IDX(k, A.r_steps, 4)]);
         acc[0] += sum * (double)ncols * idsv;
     }
     __syncwarp();
@@ -607,7 +607,8 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     if (lane < ncols)
     {
         Col<S> cc;
-        column_consts<S, true>(A.geom + 4 * ((size_t)(mu0 + lane) * A.nu_steps + nu), th, cc);
+        column_consts<S, true>(A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1),
+                               th, cc);
         store_col2<S>(cs + lane * CW, cc);
     }
     __syncwarp();
@@ -615,8 +616,7 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
     const int nf = (k1 - k0) * C;
-    const float4* __restrict__ base = A.pts + (size_t)k0 * C;
-    const double idsv = A.ids[nu];
+    const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
     {
         /* pair m = this lane's points g0 + 64 m + lane and g0 + 64 m + 32 + lane;
@@ -626,8 +626,8 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
         for (int m = 0; m < NP; ++m)
         {
             const int fa = g0 + 64 * m + lane, fb = fa + 32;
-            float4 a = base[fa < nf ? fa : 0];
-            float4 b = base[fb < nf ? fb : 0];
+            float4 a = A.pts[MWSEP_IDX((size_t)k0 * C + (fa < nf ? fa : 0), (size_t)A.r_steps * C, 2)];
+            float4 b = A.pts[MWSEP_IDX((size_t)k0 * C + (fb < nf ? fb : 0), (size_t)A.r_steps * C, 2)];
             if (fa >= nf) a.z = 0.f;
             if (fb >= nf) b.z = 0.f;
             X[m] = make_float2(a.x, b.x);
@@ -659,7 +659,7 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     if (FORM == BG_NONE && lane == 0)
     {
         double sum = 0.0;
-        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[k]);
+        for (int k = k0; k < k1; ++k) sum += (double)(-(float)A.irv[MWSEP_IDX(k, A.r_steps, 4)]);
         acc[0] += sum * (double)ncols * idsv;
     }
     __syncwarp();
@@ -675,6 +675,7 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     const int NS = th.n_streams;
     const int N = St.n_stars;
     Col<S> cc;
+    s0 = (int)MWSEP_IDX(s0, N, 7);
     column_consts<S>(St.geom + 4 * (size_t)s0, th, cc);
     float bgf = 0.f, stf[SArr<S>::N];
     switch (mwsep_bg_form(&th))

@@ -151,3 +151,5 @@ extern "C" int mwsep_launch_likelihood_f64(const mwsep_stars_dev* stars, const m
     if (sh->n_streams <= 4) return launch_likelihood<4>(stars, th_dev, sh, integrals, partials, st);
     return launch_likelihood<8>(stars, th_dev, sh, integrals, partials, st);
 }
+
+MWSEP_CHECKS_READER(mwsep_checks_f64)

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include "mwsep_internal.h"
+#include "mwsep_checks.cuh"
 #include "mwsep_reduce.cuh"
 
 namespace mwsep {
@@ -105,19 +106,19 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const int kc = (int)(item / A.n_cols);
     const int col = (int)(item - (long long)kc * A.n_cols);
     const int j = col % A.nu_steps;
-    const double* g = A.geom + 4 * (size_t)col;
+    const double* g = A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1);
     const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
-    const double idsj = A.ids[j];
+    const double idsj = A.ids[MWSEP_IDX(j, A.nu_steps, 3)];
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
     for (int k = k0; k < k1; ++k)
     {
-        const double V = A.irv[k] * idsj;
+        const double V = A.irv[MWSEP_IDX(k, A.r_steps, 4)] * idsj;
         double bg, st[SMAX];
-        const size_t row = (size_t)k * C;
+        const size_t row = (size_t)MWSEP_IDX(k, A.r_steps, 5) * C;
         convolve_f64<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, 1, C, bsin, bcos,
                            lsin, lcos, th, bg, st);
-        const double rf = A.reff[k];
+        const double rf = A.reff[MWSEP_IDX(k, A.r_steps, 6)];
         if (th.bg_mode != 2) bg *= rf;
         bg *= V;
         acc[0].add(bg);
@@ -143,6 +144,7 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
 {
     const int S = th.n_streams;
     const int N = St.n_stars;
+    s0 = (int)MWSEP_IDX(s0, N, 7);
     const double* g = St.geom + 4 * (size_t)s0;
     double bg, st[SMAX];
     convolve_f64<SMAX>(St.r_point + s0, St.qw + s0, St.r_in_mag + s0, St.r_in_mag2 + s0, (size_t)N, St.convolve,

@@ -30,6 +30,7 @@
 #include "mwsep_ctx.h"
 #include "mwsep_geometry.cuh"
 #include "mwsep_internal.h"
+#include "mwsep_checks.cuh"
 #include "mwsep_status.h"
 
 /* ---------------------------------------------------------------- status */
@@ -43,6 +44,36 @@ extern "C" int mwsep_fail(int status)
 }
 
 extern "C" int mwsep_last_error(void) { return tl_last_error; }
+
+#if MWSEP_DEVICE_CHECKS
+extern "C" int mwsep_checks_f32(unsigned long long*, unsigned long long*);
+extern "C" int mwsep_checks_f64(unsigned long long*, unsigned long long*);
+extern "C" int mwsep_checks_engine_f32(unsigned long long*, unsigned long long*);
+extern "C" int mwsep_checks_engine_f64(unsigned long long*, unsigned long long*);
+extern "C" int mwsep_checks_separation(unsigned long long*, unsigned long long*);
+#endif
+
+extern "C" int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, unsigned long long* first)
+{
+    if (!enabled || !failures || !first) return mwsep_fail(MWSEP_ERR_ARG);
+    *failures = 0;
+    *first = 0;
+#if MWSEP_DEVICE_CHECKS
+    *enabled = 1;
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return mwsep_fail(MWSEP_ERR_CUDA);
+    int rc = 0;
+    rc |= mwsep_checks_f32(failures, first);
+    rc |= mwsep_checks_f64(failures, first);
+    rc |= mwsep_checks_engine_f32(failures, first);
+    rc |= mwsep_checks_engine_f64(failures, first);
+    rc |= mwsep_checks_separation(failures, first);
+    return rc ? mwsep_fail(MWSEP_ERR_CUDA) : MWSEP_OK;
+#else
+    (void)device;
+    *enabled = 0;
+    return MWSEP_OK;
+#endif
+}
 
 extern "C" const char* mwsep_status_string(int s)
 {
@@ -506,6 +537,7 @@ int warp_tile_kstep(int convolve, int n_streams)
 
 int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r)
 {
+    mwsep::Range nvtx_range("mwsep.set_stars");
     if (!w.has_problem) return mwsep_fail(MWSEP_ERR_STATE);
     if (n < 1) return mwsep_fail(MWSEP_ERR_ARG);
     const int C = w.prob.convolve;
@@ -578,6 +610,7 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp)
 
 int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap)
 {
+    mwsep::Range nvtx_range("mwsep.set_problem");
     int rc = check_problem(ap);
     if (rc) return mwsep_fail(rc);
     const int old_convolve = w.has_problem ? w.prob.convolve : -1;
@@ -629,6 +662,7 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
 
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out)
 {
+    mwsep::Range nvtx_range("mwsep.evaluate");
     if (c->wedges.empty() || !c->wedges[0]->has_problem || !c->wedges[0]->has_stars)
         return mwsep_fail(MWSEP_ERR_STATE);
     Wedge& w = *c->wedges[0];

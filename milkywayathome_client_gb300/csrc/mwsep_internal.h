@@ -202,6 +202,8 @@ typedef struct
     double2* lpart;                       /* [ltiles][LCOMP] */
     double* out;                          /* [requests][OUT_STRIDE] */
     int* counters;
+    int n_area_desc;                      /* descriptors in areas / stars */
+    int n_star_desc;
 } mwsep_engine_args;
 
 #ifdef __cplusplus

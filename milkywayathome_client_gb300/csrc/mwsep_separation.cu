@@ -81,11 +81,12 @@ __global__ void __launch_bounds__(256) separation_kernel(const mwsep_stars_dev S
     const int N = St.n_stars;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
     {
-        const double* g = St.geom + 4 * (size_t)s0;
+        const int si = (int)MWSEP_IDX(s0, N, 7);
+        const double* g = St.geom + 4 * (size_t)si;
         double bg, st[SMAX];
-        f64::convolve_f64<SMAX>(St.r_point + s0, St.qw + s0, St.r_in_mag + s0, St.r_in_mag2 + s0, (size_t)N,
+        f64::convolve_f64<SMAX>(St.r_point + si, St.qw + si, St.r_in_mag + si, St.r_in_mag2 + si, (size_t)N,
                                 St.convolve, g[0], g[1], g[2], g[3], th, bg, st);
-        const double rf = St.reff[s0];
+        const double rf = St.reff[si];
         if (th.bg_mode != 2) bg *= rf;
         const double pbx = sc.eps_b * bg / I[0];
         double psg[SMAX], sum = 0.0;
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256) separation_kernel(const mwsep_stars_dev S
         if (xyz)
         {
             double p[3];
-            mwsep::lbr_to_xyz(St.l[s0], St.b[s0], St.r[s0], p);
+            mwsep::lbr_to_xyz(St.l[si], St.b[si], St.r[si], p);
             transform_point(p, sc.m, xyz + 3 * (size_t)s0);
         }
     }
@@ -208,6 +209,7 @@ extern "C" int mwsep_stripe_transform(int sgr_coordinates, int wedge, double* ma
 extern "C" int mwsep_ctx_separation(mwsep_ctx* c, const double* theta, unsigned long long seed, double* sprob,
                                     int* assignment, double* xyz, mwsep_separation_summary* summary)
 {
+    mwsep::Range nvtx_range("mwsep.separation");
     if (!c || !theta) return mwsep_fail(MWSEP_ERR_ARG);
     if (c->wedges.empty() || !c->wedges[0]->has_problem || !c->wedges[0]->has_stars)
         return mwsep_fail(MWSEP_ERR_STATE);
@@ -299,3 +301,5 @@ extern "C" int mwsep_ctx_separation(mwsep_ctx* c, const double* theta, unsigned 
     }
     return MWSEP_OK;
 }
+
+MWSEP_CHECKS_READER(mwsep_checks_separation)
