@@ -126,10 +126,10 @@ struct Wedge
 {
     bool has_problem = false;
     ProblemHost prob;
-    std::vector<double> gl_x, gl_w, dx;
+    std::vector<double> gl_x, gl_w, dx, nfac;
     double coeff = 0.0;
     AreaDev areas[MWSEP_MAX_AREAS];
-    DevBuf d_dx, d_glw;
+    DevBuf d_dx, d_glw, d_nfac; /* per convolution point: dx, gl_w, star-table factors */
 
     bool has_stars = false;
     int n_stars = 0;

@@ -38,10 +38,16 @@ __global__ void geometry_kernel(double mu_min, double mu_step, int mu_steps, con
 }
 
 /* Per-star tables: cpu/evaluation_optimized.c:159-188 applied to the
- * star's distance, plus its sines/cosines (:205-208).  Tables are [C][N]. */
+ * star's distance, plus its sines/cosines (:205-208).  Tables are [C][N].
+ * The per-point pow and exp separate into a per-star and a per-point factor:
+ *   r_point = 10^((g' - M)/5 + 1) / 1000 * 10^(dx_n / 5),
+ *   qw_r3_N = (gl_w_n coeff e^{-dx_n^2 / 2 sigma^2}) r_point^3,
+ * with nfac = {10^(dx_n/5)} then {gl_w_n coeff e^{-dx_n^2/2 sigma^2}} built
+ * once per problem on the host: one multiply per point instead of a pow and
+ * an exp, equal to the reference's values within a few ulp. */
 __global__ void star_tables_kernel(int n, const double* __restrict__ l, const double* __restrict__ b,
                                    const double* __restrict__ r, int C, const double* __restrict__ dx,
-                                   const double* __restrict__ gl_w, double coeff, double* __restrict__ geom,
+                                   const double* __restrict__ nfac, double* __restrict__ geom,
                                    double* __restrict__ r_point, double* __restrict__ qw,
                                    double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
                                    double* __restrict__ reff, float4* __restrict__ pts)
@@ -51,10 +57,12 @@ __global__ void star_tables_kernel(int n, const double* __restrict__ l, const do
         double gPrime, rf;
         mwsep::prob_consts_head(r[s], gPrime, rf);
         reff[s] = rf;
+        const double base = pow(10.0, (gPrime - MW_ABSM) / 5.0 + 1.0) / 1000.0;
         for (int i = 0; i < C; ++i)
         {
-            double g, rp, q;
-            mwsep::prob_consts_point(gPrime, dx[i], gl_w[i], coeff, g, rp, q);
+            const double g = gPrime + dx[i];
+            const double rp = base * nfac[i];
+            const double q = nfac[C + i] * (rp * rp * rp);
             const size_t o = (size_t)i * n + s;
             r_in_mag[o] = g;
             r_in_mag2[o] = g * g;
@@ -86,14 +94,14 @@ extern "C" int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps
 }
 
 extern "C" int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
-                                        const double* dx, const double* gl_w, double coeff, double* geom,
-                                        double* r_point, double* qw, double* r_in_mag, double* r_in_mag2,
-                                        double* reff, float4* pts, void* stream)
+                                        const double* dx, const double* nfac, double* geom, double* r_point,
+                                        double* qw, double* r_in_mag, double* r_in_mag2, double* reff, float4* pts,
+                                        void* stream)
 {
     if (n <= 0) return 0;
     int grid = (n + 127) / 128;
     if (grid > 152 * 32) grid = 152 * 32;
-    star_tables_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(n, l, b, r, convolve, dx, gl_w, coeff, geom,
-                                                               r_point, qw, r_in_mag, r_in_mag2, reff, pts);
+    star_tables_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(n, l, b, r, convolve, dx, nfac, geom, r_point, qw,
+                                                               r_in_mag, r_in_mag2, reff, pts);
     return (int)cudaGetLastError();
 }

@@ -562,7 +562,7 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     CU(h2d(c, w.s_b.p, b, (size_t)n * 8));
     CU(h2d(c, w.s_r.p, r, (size_t)n * 8));
     CK(mwsep_launch_star_tables(n, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(), C,
-                                w.d_dx.as<double>(), w.d_glw.as<double>(), w.coeff, w.s_geom.as<double>(),
+                                w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
                                 w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
                                 w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
     mwsep_stars_dev& v = w.stars_view;
@@ -608,11 +608,46 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp)
     return MWSEP_OK;
 }
 
+namespace {
+
+/* The device tables of a wedge depend on these fields only (never on the
+ * parameter values): equal fields give the same tables. */
+bool same_tables(const ProblemHost& a, const ProblemHost& b)
+{
+    if (a.convolve != b.convolve || a.wedge != b.wedge || a.sgr != b.sgr || a.n_areas != b.n_areas ||
+        a.n_streams != b.n_streams)
+        return false;
+    for (int i = 0; i < a.n_areas; ++i)
+    {
+        const AreaHost &x = a.area[i], &y = b.area[i];
+        if (x.mu_steps != y.mu_steps || x.nu_steps != y.nu_steps || x.r_steps != y.r_steps ||
+            x.mu_min != y.mu_min || x.mu_max != y.mu_max || x.nu_min != y.nu_min || x.nu_max != y.nu_max ||
+            x.r_min != y.r_min || x.r_max != y.r_max || x.mu_step != y.mu_step || x.nu_step != y.nu_step ||
+            x.r_step != y.r_step)
+            return false;
+    }
+    return true;
+}
+
+} // namespace
+
 int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap)
 {
     mwsep::Range nvtx_range("mwsep.set_problem");
     int rc = check_problem(ap);
     if (rc) return mwsep_fail(rc);
+    if (w.has_problem)
+    {
+        /* the same grids, convolution, wedge and frame: the resident tables
+         * (and the wedge's tuned shape) stand; only the values change */
+        ProblemHost next;
+        copy_problem(ap, next);
+        if (same_tables(next, w.prob))
+        {
+            w.prob = next;
+            return MWSEP_OK;
+        }
+    }
     const int old_convolve = w.has_problem ? w.prob.convolve : -1;
     copy_problem(ap, w.prob);
     w.has_problem = false;
@@ -624,11 +659,20 @@ int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap)
     for (int i = 0; i < C; ++i) w.dx[i] = 3 * MW_STDEV * w.gl_x[i]; /* evaluation_optimized.c:131 */
     w.coeff = 1 / (MW_STDEV * sqrt(2 * MW_PI));                      /* :84 */
     const size_t before = c->dev_bytes;
-    if (w.d_dx.ensure((size_t)C * 8, c->dev_bytes) || w.d_glw.ensure((size_t)C * 8, c->dev_bytes))
+    if (w.d_dx.ensure((size_t)C * 8, c->dev_bytes) || w.d_glw.ensure((size_t)C * 8, c->dev_bytes) ||
+        w.d_nfac.ensure((size_t)C * 16, c->dev_bytes))
         return mwsep_fail(MWSEP_ERR_NOMEM);
     w.bytes += c->dev_bytes - before;
+    /* star-table factors (the separable form of set_probability_constants) */
+    w.nfac.assign((size_t)2 * C, 0.0);
+    for (int i = 0; i < C; ++i)
+    {
+        w.nfac[(size_t)i] = pow(10.0, w.dx[i] / 5.0);
+        w.nfac[(size_t)C + i] = w.gl_w[i] * (w.coeff * exp(-(w.dx[i] * w.dx[i]) / (2 * MW_STDEV * MW_STDEV)));
+    }
     CU(h2d(c, w.d_dx.p, w.dx.data(), (size_t)C * 8));
     CU(h2d(c, w.d_glw.p, w.gl_w.data(), (size_t)C * 8));
+    CU(h2d(c, w.d_nfac.p, w.nfac.data(), (size_t)C * 16));
     for (int a = 0; a < w.prob.n_areas; ++a)
     {
         rc = build_area(c, w, a);
@@ -652,7 +696,7 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
                           &D.ids, &D.nus, &D.pts};
         for (DevBuf* b : bufs) b->release(t);
     }
-    DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
+    DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.d_nfac, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
                       &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts};
     for (DevBuf* b : bufs) b->release(t);
     w.h_stars.release();
