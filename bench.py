@@ -338,6 +338,15 @@ def run_gb300_arm(args, ws, rank, local):
                 "work_per_point": f"{fp32_ops} FP32 lane-ops + {1.25 + S} SFU ops",
                 "binding_pipe": "fma" if fma_s_per_point >= sfu_s_per_point else "sfu",
                 "points_per_launch": cell_pts}
+    # the same throughput in the reference's own operation count: F(S) = 18 + 23 S
+    # flops per density point (every +, -, x, /, sqrt, exp counted once)
+    F = 18 + 23 * S
+    pts_eval = cell_pts + star_pts
+    algorithmic = {"flops_per_point": F, "points_per_eval": pts_eval,
+                   "mixed_tflops": pts_eval * F * value / 1e12,
+                   "plain_f64_tflops": pts_eval * F * plain_value / 1e12,
+                   "note": "reference operation count; divide, sqrt and exp expand to many pipe "
+                           "instructions, so the pipe roofline above is the binding one"}
 
     out = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
@@ -358,6 +367,7 @@ def run_gb300_arm(args, ws, rank, local):
                 "d2h_bytes_per_step": d2h.value, "api": "mwsep_evaluate_mixed (EvalFunc, host structs)"},
         "gpu_launches": launches,
         "roofline": roofline,
+        "roofline_algorithmic": algorithmic,
         "pipe_peaks": {"fp64_tflops": peaks.fp64_fma_tflops, "fp32_tflops": peaks.fp32_fma_tflops,
                        "ex2_gops": peaks.ex2_gops, "rsqrt_gops": peaks.rsqrt_gops, "rcp_gops": peaks.rcp_gops},
         "wall_s_timed": wall,
@@ -442,7 +452,7 @@ def serving(args):
     """Poisson arrivals over the 6 mixed-size wedges, compensated FP32."""
     from milkywayathome_client_gb300 import native as N
     from milkywayathome_client_gb300 import serve_bench
-    res = serve_bench.run([50.0, 200.0], 3.0, N.MWSEP_MIXED_F32, 2, 256,
+    res = serve_bench.run([50.0, 200.0, 800.0], 2.0, N.MWSEP_MIXED_F32, 2, 256,
                           os.path.join(args.data_dir, "serving"))
     return {"workload": "Poisson arrivals over 6 resident wedges (log-uniform sizes), wedge chosen by star count",
             "lanes": 2, "precision": "mixed", "results": res}

@@ -28,6 +28,19 @@ static double now_s(void)
     return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+/* The library's binary files start with an 8-byte magic; anything else is
+ * read as the reference's text format. */
+static int has_magic(const char* path, const char* magic)
+{
+    char buf[8];
+    FILE* f = fopen(path, "rb");
+    size_t got;
+    if (!f) return 0;
+    got = fread(buf, 1, 8, f);
+    fclose(f);
+    return got == 8 && memcmp(buf, magic, 8) == 0;
+}
+
 int main(int argc, char** argv)
 {
     const char* pfile = NULL;
@@ -55,14 +68,15 @@ int main(int argc, char** argv)
     }
     memset(&ap, 0, sizeof(ap));
     memset(&sp, 0, sizeof(sp));
-    rc = mwsep_read_astronomy_parameters(pfile, &ap);
+    rc = has_magic(pfile, "MWSEPPAR") ? mwsep_read_astronomy_parameters_binary(pfile, &ap)
+                                      : mwsep_read_astronomy_parameters(pfile, &ap);
     if (rc)
     {
         fprintf(stderr, "APP: error reading astronomy parameters from file %s: %s\n", pfile,
                 mwsep_status_string(rc));
         return 1;
     }
-    rc = mwsep_read_star_points(sfile, &sp);
+    rc = has_magic(sfile, "MWSEPCAT") ? mwsep_read_star_points_binary(sfile, &sp) : mwsep_read_star_points(sfile, &sp);
     if (rc)
     {
         fprintf(stderr, "APP: error reading star points from file %s: %s\n", sfile, mwsep_status_string(rc));

@@ -26,3 +26,24 @@ def test_binary_catalogue_gives_identical_results(gpu_ctx, tmp_path, name):
         assert t.likelihood == b.likelihood
         assert t.integrals == b.integrals
         assert t.prob_sum == b.prob_sum
+
+
+def test_c_client_reads_binary_files(built_library, tmp_path):
+    """The C client takes the binary forms in place of the text files and
+    prints the same result lines."""
+    import subprocess
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import build
+    pf, sf, g = load_case("three_streams")
+    bp, bs = str(tmp_path / "p.mwsp"), str(tmp_path / "s.mwsb")
+    mw.AstronomyParameters.read(pf).write_binary(bp)
+    mw.StarPoints.read(sf).write_binary(bs)
+    theta = [repr(float(x)) for x in g["theta"]]
+    outs = []
+    for a, p in ((pf, sf), (bp, bs)):
+        r = subprocess.run([build.CLIENT_PATH, "-a", a, "-p", p, *theta], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        outs.append([ln for ln in r.stderr.splitlines() if ln.startswith("<") and "seconds" not in ln
+                     and "search_application" not in ln])
+    assert outs[0] == outs[1] and len(outs[0]) >= 3
