@@ -95,6 +95,100 @@ __device__ __forceinline__ void convolve_f64(const double* __restrict__ rp, cons
     }
 }
 
+/* Per-column constants of the integral's density in completed-square form,
+ * in FP64.  With u = (cos b cos l, cos b sin l, sin b) the column's unit
+ * vector, a point at distance r sits at x = r u - (R, 0, 0)
+ * (cpu/evaluation_optimized.c:222-227), and
+ *   background  x0^2 + x1^2 + x2^2/q^2 = B2 (r - rb)^2 + Db,
+ *   stream s    |x - c - ((x - c).a) a|^2 = A2 (r - rs)^2 + Ds,
+ * both sums of non-negative terms (no cancellation), so the stream exponent
+ * -|.|^2 / sigma2_s is k2 (r - rs)^2 + k0.  The same quantities as the
+ * reference's x0, x1, x2 and perpendicular-distance arithmetic, in about
+ * half the FP64 operations (no per-point divide by q^2 or sigma2). */
+template <int SMAX>
+struct ColF64
+{
+    double B2, rb, Db;
+    double rs[SMAX], k2[SMAX], k0[SMAX];
+};
+
+template <int SMAX>
+__device__ __forceinline__ void column_consts_f64(double bsin, double bcos, double lsin, double lcos,
+                                                  const mwsep_theta_consts& th, ColF64<SMAX>& cc)
+{
+    const double u0 = bcos * lcos, u1 = bcos * lsin, u2 = bsin;
+    const double perp = u1 * u1 + u2 * u2 / (th.q * th.q);
+    cc.B2 = u0 * u0 + perp;
+    cc.rb = MW_LBR_R * u0 / cc.B2;
+    cc.Db = (MW_LBR_R * MW_LBR_R) * perp / cc.B2;
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s)
+    {
+        cc.rs[s] = 0.0;
+        cc.k2[s] = 0.0;
+        cc.k0[s] = 0.0;
+        if (s < th.n_streams && th.stream_on[s])
+        {
+            const double a0 = th.a[s][0], a1 = th.a[s][1], a2 = th.a[s][2];
+            /* c' = c + (R, 0, 0) so that x - c = r u - c' */
+            const double c0 = th.c[s][0] + MW_LBR_R, c1 = th.c[s][1], c2 = th.c[s][2];
+            const double au = a0 * u0 + a1 * u1 + a2 * u2;
+            const double p0 = u0 - au * a0, p1 = u1 - au * a1, p2 = u2 - au * a2;
+            const double ac = a0 * c0 + a1 * c1 + a2 * c2;
+            const double q0 = c0 - ac * a0, q1 = c1 - ac * a1, q2 = c2 - ac * a2;
+            const double A2 = p0 * p0 + p1 * p1 + p2 * p2;
+            const double rs = (A2 > 1e-300) ? (p0 * q0 + p1 * q1 + p2 * q2) / A2 : 0.0;
+            const double e0 = q0 - rs * p0, e1 = q1 - rs * p1, e2 = q2 - rs * p2;
+            const double Ds = e0 * e0 + e1 * e1 + e2 * e2;
+            const double f = -1.0 / th.sigma_sq2[s];
+            cc.rs[s] = rs;
+            cc.k2[s] = A2 * f;
+            cc.k0[s] = Ds * f;
+        }
+    }
+}
+
+/* One cell's convolution with the completed-square constants (the
+ * integral's counterpart of convolve_f64). */
+template <int SMAX>
+__device__ __forceinline__ void convolve_f64_cs(const double* __restrict__ rp, const double* __restrict__ qwt,
+                                                const double* __restrict__ gm, const double* __restrict__ gm2,
+                                                int C, const ColF64<SMAX>& cc, const mwsep_theta_consts& th,
+                                                double& bg, double (&st)[SMAX])
+{
+    const int S = th.n_streams;
+    bg = (th.bg_mode == 2) ? -1.0 : 0.0;
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) st[s] = 0.0;
+    for (int n = 0; n < C; ++n)
+    {
+        const double r = rp[n];
+        const double qw = qwt[n];
+        if (th.bg_mode != 2)
+        {
+            const double t = r - cc.rb;
+            const double rg = sqrt(cc.B2 * t * t + cc.Db);
+            if (th.bg_mode == 0)
+            {
+                const double rs = rg + th.r0;
+                bg += qw / (rg * rs * rs * rs);
+                if (th.aux) bg += qw * (th.bg_a * gm2[n] + th.bg_b * gm[n] + th.bg_c);
+            }
+            else
+                bg += qw / (pow(rg, th.alpha) * pow(rg + th.r0, th.alpha_delta3));
+        }
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s)
+        {
+            if (s < S && th.stream_on[s])
+            {
+                const double u = r - cc.rs[s];
+                st[s] += qw * exp(cc.k2[s] * u * u + cc.k0[s]);
+            }
+        }
+    }
+}
+
 /* One item of an integral (a column and its run of r-bins): Kahan-adds
  * each cell's bg*V and st*V into acc (cpu/evaluation_optimized.c:498-520). */
 template <int SMAX>
@@ -107,7 +201,8 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const int col = (int)(item - (long long)kc * A.n_cols);
     const int j = col % A.nu_steps;
     const double* g = A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1);
-    const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
+    ColF64<SMAX> cc;
+    column_consts_f64<SMAX>(g[0], g[1], g[2], g[3], th, cc);
     const double idsj = A.ids[MWSEP_IDX(j, A.nu_steps, 3)];
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
@@ -116,8 +211,7 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
         const double V = A.irv[MWSEP_IDX(k, A.r_steps, 4)] * idsj;
         double bg, st[SMAX];
         const size_t row = (size_t)MWSEP_IDX(k, A.r_steps, 5) * C;
-        convolve_f64<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, 1, C, bsin, bcos,
-                           lsin, lcos, th, bg, st);
+        convolve_f64_cs<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, C, cc, th, bg, st);
         const double rf = A.reff[MWSEP_IDX(k, A.r_steps, 6)];
         if (th.bg_mode != 2) bg *= rf;
         bg *= V;
