@@ -109,6 +109,13 @@ def case_list():
     # the shape of config 0 at full size (80 x 40 x 70, convolve 30), 10k stars
     c0 = syn.config(0)
     cases.append(("config0", c0["problems"][0], 10_000))
+
+    # the library's maximum sizes: 8 streams, 8 integral areas (a wedge and
+    # 7 cuts), convolve 512, on a small grid
+    p = P(convolve=512, areas=[_wedge((310.0, 340.0, 8), (-1.25, 1.25, 4), (16.0, 22.5, 6))] +
+          [_wedge((311.0 + 3.5 * i, 313.0 + 3.5 * i, 2), (-1.25, 1.25, 2), (16.0, 22.5, 6)) for i in range(7)])
+    p.streams = syn.draw_streams(rng, 8, 310.0, 340.0)
+    cases.append(("max_limits", p, 64))
     return cases
 
 
