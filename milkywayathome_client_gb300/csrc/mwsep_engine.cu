@@ -2,7 +2,7 @@
  *
  * Evaluates a batch of requests, each naming a resident wedge and a
  * parameter vector, with one persistent launch per phase (integrals, then
- * likelihood) for all requests of a stream-count class:
+ * likelihood) for all requests of a stream-count group:
  *
  *   H2D counters, constants, requests, tile lists
  *   -> integral tiles (persistent, dynamic tile counter)
@@ -13,7 +13,7 @@
  * The sequence is captured once as a CUDA graph and replayed: tile and
  * request counts live in device memory, copies are of the buffers' full
  * capacity, so any batch that fits the current capacities replays the same
- * graph (re-captured only when a buffer grows or the set of kernel classes
+ * graph (re-captured only when a buffer grows or the set of kernel groups
  * changes).
  *
  * Tiles are cut from each request's items by its wedge's tile shape
@@ -39,15 +39,18 @@ using namespace mwsep;
 
 namespace {
 
-int stream_class(int S) { return S <= 4 ? 0 : 1; }
+constexpr int NG = MWSEP_ENG_GROUPS;
+
+/* The kernel group of a stream count: S itself up to 4, 5 for 5..8. */
+int stream_group(int S) { return S <= 4 ? S : 5; }
 
 /* Grow-only capacity with headroom. */
 size_t grow(size_t need) { return need + need / 2 + 64; }
 
-int blocks_per_sm(int precision, int phase, int cls)
+int blocks_per_sm(int precision, int phase, int group)
 {
-    return precision == MWSEP_PLAIN_F64 ? mwsep_engine_f64_blocks_per_sm(phase, cls)
-                                        : mwsep_engine_f32_blocks_per_sm(phase, cls);
+    return precision == MWSEP_PLAIN_F64 ? mwsep_engine_f64_blocks_per_sm(phase, group)
+                                        : mwsep_engine_f32_blocks_per_sm(phase, group);
 }
 
 void invalidate_graph(EngineState& e)
@@ -110,13 +113,13 @@ int ensure_descriptors(mwsep_ctx* c)
     return MWSEP_OK;
 }
 
-/* Tile ranges of one batch, per kernel class: [begin, end) in the tile
- * arrays (class 0 first). */
+/* Tile ranges of one batch, per kernel group: [begin, end) in the tile
+ * arrays (group 0 first). */
 struct BatchShape
 {
     int n_req = 0;
-    int it_begin[2] = {0, 0}, it_end[2] = {0, 0};
-    int lt_begin[2] = {0, 0}, lt_end[2] = {0, 0};
+    int it_begin[NG] = {}, it_end[NG] = {};
+    int lt_begin[NG] = {}, lt_end[NG] = {};
 };
 
 /* Build the host side of one batch into the pinned staging buffers.
@@ -127,12 +130,12 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
 {
     EngineState& e = c->eng;
     /* count tiles first */
-    long long nit[2] = {0, 0}, nlt[2] = {0, 0};
+    long long nit[NG] = {}, nlt[NG] = {};
     for (int i = 0; i < n; ++i)
     {
         const Wedge& w = *c->wedges[reqs[i].wedge];
         const Tune& t = w.tune[precision];
-        const int cls = stream_class(w.prob.n_streams);
+        const int cls = stream_group(w.prob.n_streams);
         for (int a = 0; a < w.prob.n_areas; ++a)
         {
             mwsep_area_dev v = w.areas[a].view;
@@ -141,7 +144,13 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
         }
         if (with_likelihood) nlt[cls] += (w.n_stars + t.tile_stars - 1) / t.tile_stars;
     }
-    const long long total_it = nit[0] + nit[1], total_lt = std::max<long long>(1, nlt[0] + nlt[1]);
+    long long total_it = 0, total_lt = 0;
+    for (int g = 0; g < NG; ++g)
+    {
+        total_it += nit[g];
+        total_lt += nlt[g];
+    }
+    total_lt = std::max<long long>(1, total_lt);
     if (total_it > (1LL << 30) || total_lt > (1LL << 30)) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
 
     /* capacities (grow-only); any reallocation invalidates the graph.  The
@@ -182,13 +191,19 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
     mwsep_req_dev* hq = e.h_reqs.as<mwsep_req_dev>();
     mwsep_itile* hit = e.h_itiles.as<mwsep_itile>();
     mwsep_ltile* hlt = e.h_ltiles.as<mwsep_ltile>();
-    long long it_pos[2] = {0, nit[0]}, lt_pos[2] = {0, nlt[0]};
+    long long it_pos[NG], lt_pos[NG];
+    it_pos[0] = lt_pos[0] = 0;
+    for (int g = 1; g < NG; ++g)
+    {
+        it_pos[g] = it_pos[g - 1] + nit[g - 1];
+        lt_pos[g] = lt_pos[g - 1] + nlt[g - 1];
+    }
     for (int i = 0; i < n; ++i)
     {
         const int wi = reqs[i].wedge;
         const Wedge& w = *c->wedges[wi];
         const Tune& t = w.tune[precision];
-        const int cls = stream_class(w.prob.n_streams);
+        const int cls = stream_group(w.prob.n_streams);
         theta_consts(w.prob, reqs[i].theta, hth[i]);
         mwsep_req_dev& q = hq[i];
         memset(&q, 0, sizeof(q));
@@ -223,17 +238,19 @@ int build_batch(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision, l
         q.lk_slot1 = (int)lt_pos[cls];
     }
     shape.n_req = n;
-    shape.it_begin[0] = 0;
-    shape.it_end[0] = (int)nit[0];
-    shape.it_begin[1] = (int)nit[0];
-    shape.it_end[1] = (int)(nit[0] + nit[1]);
-    shape.lt_begin[0] = 0;
-    shape.lt_end[0] = (int)nlt[0];
-    shape.lt_begin[1] = (int)nlt[0];
-    shape.lt_end[1] = (int)(nlt[0] + nlt[1]);
+    long long ib = 0, lb = 0;
+    for (int g = 0; g < NG; ++g)
+    {
+        shape.it_begin[g] = (int)ib;
+        shape.it_end[g] = (int)(ib + nit[g]);
+        shape.lt_begin[g] = (int)lb;
+        shape.lt_end[g] = (int)(lb + nlt[g]);
+        ib += nit[g];
+        lb += nlt[g];
+    }
     if (max_itiles >= 0)
-        /* timing runs: keep only the first tiles of each class */
-        for (int k = 0; k < 2; ++k)
+        /* timing runs: keep only the first tiles of each group */
+        for (int k = 0; k < NG; ++k)
             shape.it_end[k] = (int)std::min<long long>(shape.it_end[k], shape.it_begin[k] + max_itiles);
     return MWSEP_OK;
 }
@@ -258,7 +275,7 @@ mwsep_engine_args engine_args(mwsep_ctx* c)
 }
 
 /* Issue (or capture) the launch sequence of one batch. */
-int issue(mwsep_ctx* c, int precision, bool has_i[2], bool has_l[2], bool with_likelihood, int* launches)
+int issue(mwsep_ctx* c, int precision, const bool* has_i, const bool* has_l, bool with_likelihood, int* launches)
 {
     EngineState& e = c->eng;
     cudaStream_t st = c->stream;
@@ -269,7 +286,7 @@ int issue(mwsep_ctx* c, int precision, bool has_i[2], bool has_l[2], bool with_l
     CU(h2d(c, e.d_itiles.p, e.h_itiles.p, e.d_itiles.bytes));
     if (with_likelihood) CU(h2d(c, e.d_ltiles.p, e.h_ltiles.p, e.d_ltiles.bytes));
     int n = 0;
-    for (int cls = 0; cls < 2; ++cls)
+    for (int cls = 0; cls < NG; ++cls)
     {
         if (!has_i[cls]) continue;
         const int g = c->sm_count * blocks_per_sm(precision, 0, cls);
@@ -282,7 +299,7 @@ int issue(mwsep_ctx* c, int precision, bool has_i[2], bool has_l[2], bool with_l
     ++n;
     if (with_likelihood)
     {
-        for (int cls = 0; cls < 2; ++cls)
+        for (int cls = 0; cls < NG; ++cls)
         {
             if (!has_l[cls]) continue;
             const int g = c->sm_count * blocks_per_sm(precision, 1, cls);
@@ -298,16 +315,16 @@ int issue(mwsep_ctx* c, int precision, bool has_i[2], bool has_l[2], bool with_l
     return MWSEP_OK;
 }
 
-/* Run a built batch: replay the captured graph when the shape class
+/* Run a built batch: replay the captured graph when the shape group
  * matches, otherwise capture a new one. */
 int run_batch(mwsep_ctx* c, int precision, const BatchShape& shape, bool with_likelihood, bool use_graph)
 {
     mwsep::Range nvtx_range("mwsep.engine_batch");
     EngineState& e = c->eng;
-    /* counters: per class next/end for integral and likelihood tiles */
+    /* counters: per group next/end for integral and likelihood tiles */
     int* cnt = e.h_counters.as<int>();
     memset(cnt, 0, sizeof(int) * MWSEP_ENG_COUNTERS);
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < NG; ++k)
     {
         cnt[4 * k + 0] = shape.it_begin[k];
         cnt[4 * k + 1] = shape.lt_begin[k];
@@ -315,17 +332,22 @@ int run_batch(mwsep_ctx* c, int precision, const BatchShape& shape, bool with_li
         cnt[4 * k + 3] = shape.lt_end[k];
     }
     cnt[MWSEP_ENG_NREQ] = shape.n_req;
-    bool has_i[2] = {shape.it_end[0] > shape.it_begin[0], shape.it_end[1] > shape.it_begin[1]};
-    bool has_l[2] = {with_likelihood && shape.lt_end[0] > shape.lt_begin[0],
-                     with_likelihood && shape.lt_end[1] > shape.lt_begin[1]};
+    bool has_i[NG], has_l[NG];
+    long long imask = 0, lmask = 0;
+    for (int k = 0; k < NG; ++k)
+    {
+        has_i[k] = shape.it_end[k] > shape.it_begin[k];
+        has_l[k] = with_likelihood && shape.lt_end[k] > shape.lt_begin[k];
+        imask |= (long long)has_i[k] << k;
+        lmask |= (long long)has_l[k] << k;
+    }
 
     cudaStream_t st = c->stream;
     int launches = 0;
     CU(cudaEventRecord(c->ev[0], st));
     if (use_graph)
     {
-        const long long key[5] = {precision, (long long)has_i[0] | ((long long)has_i[1] << 1),
-                                  (long long)has_l[0] | ((long long)has_l[1] << 1), (long long)with_likelihood,
+        const long long key[5] = {precision, imask, lmask, (long long)with_likelihood,
                                   (long long)e.d_ipart.bytes};
         if (!e.graph || memcmp(key, e.graph_key, sizeof(key)) != 0)
         {
@@ -545,7 +567,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
     }
     const int C = w.prob.convolve;
     const Tune saved = w.tune[precision];
-    const int cls = stream_class(w.prob.n_streams);
+    const int cls = stream_group(w.prob.n_streams);
     const int waves = 6;
     const long long resident = (long long)c->sm_count * blocks_per_sm(precision, 0, cls);
     std::vector<int> kcs;

@@ -69,19 +69,28 @@ __device__ __forceinline__ void itile_form(const mwsep_area_dev& A, const mwsep_
     }
 }
 
-template <int CLS>
+/* Streams handled by a kernel of group G: exactly G up to 4, 8 (with
+ * guards) for group 5. */
+template <int G>
+struct GroupS
+{
+    static constexpr int S = G <= 4 ? G : 8;
+};
+
+template <int G>
 __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mwsep_engine_args a)
 {
+    constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
-    __shared__ double red[2 * (CLS == 0 ? 5 : MWSEP_ENG_ICOMP) * 32];
+    __shared__ double red[2 * (1 + S) * 32];
     __shared__ __align__(16) float cs[(kBlock / 32) * mwsep::kTileCols *
-                                      (CLS == 0 ? PackedTile<4>::W : ColWords<8>::N)];
+                                      (PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N)];
     __shared__ int s_tile;
-    const int n_tiles = a.counters[4 * CLS + 2];
+    const int n_tiles = a.counters[4 * G + 2];
     for (;;)
     {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 0], 1);
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 0], 1);
         __syncthreads();
         const int t = s_tile;
         if (t >= n_tiles) break;
@@ -90,17 +99,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
         load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
         __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
-        if (CLS == 1)
-            itile_form<8>(A, th, tile, red, cs, out);
-        else
-            switch (th.n_streams)
-            {
-            case 0: itile_form<0>(A, th, tile, red, cs, out); break;
-            case 1: itile_form<1>(A, th, tile, red, cs, out); break;
-            case 2: itile_form<2>(A, th, tile, red, cs, out); break;
-            case 3: itile_form<3>(A, th, tile, red, cs, out); break;
-            default: itile_form<4>(A, th, tile, red, cs, out); break;
-            }
+        itile_form<S>(A, th, tile, red, cs, out);
         __syncthreads();
     }
 }
@@ -118,16 +117,17 @@ __device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_the
     reduce_and_store<3 + S>(acc, 3 + th.n_streams, red, out);
 }
 
-template <int CLS>
+template <int G>
 __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const mwsep_engine_args a)
 {
+    constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (CLS == 0 ? 7 : MWSEP_ENG_LCOMP) * 32];
+    __shared__ double red[2 * (3 + S) * 32];
     __shared__ int s_tile;
-    const int n_tiles = a.counters[4 * CLS + 3];
+    const int n_tiles = a.counters[4 * G + 3];
     for (;;)
     {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 1], 1);
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 1], 1);
         __syncthreads();
         const int t = s_tile;
         if (t >= n_tiles) break;
@@ -138,41 +138,61 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
             a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
-        if (CLS == 1)
-            ltile<8>(St, th, I, tile, red, out);
-        else
-            switch (th.n_streams)
-            {
-            case 0: ltile<0>(St, th, I, tile, red, out); break;
-            case 1: ltile<1>(St, th, I, tile, red, out); break;
-            case 2: ltile<2>(St, th, I, tile, red, out); break;
-            case 3: ltile<3>(St, th, I, tile, red, out); break;
-            default: ltile<4>(St, th, I, tile, red, out); break;
-            }
+        ltile<S>(St, th, I, tile, red, out);
         __syncthreads();
     }
 }
 
 } // namespace
 
-extern "C" int mwsep_engine_f32_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream)
+namespace {
+
+template <int G>
+void launch_group(int phase, const mwsep_engine_args* a, int grid, cudaStream_t st)
+{
+    if (phase == 0)
+        engine_integral_f32_kernel<G><<<grid, kBlock, 0, st>>>(*a);
+    else
+        engine_likelihood_f32_kernel<G><<<grid, kBlock, 0, st>>>(*a);
+}
+
+template <int G>
+cudaError_t group_occupancy(int* b, int phase)
+{
+    return phase == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_integral_f32_kernel<G>, kBlock, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_likelihood_f32_kernel<G>, kBlock, 0);
+}
+
+} // namespace
+
+extern "C" int mwsep_engine_f32_launch(int phase, int group, const mwsep_engine_args* a, int grid, void* stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (phase == 0 && cls == 0) engine_integral_f32_kernel<0><<<grid, kBlock, 0, st>>>(*a);
-    else if (phase == 0) engine_integral_f32_kernel<1><<<grid, kBlock, 0, st>>>(*a);
-    else if (cls == 0) engine_likelihood_f32_kernel<0><<<grid, kBlock, 0, st>>>(*a);
-    else engine_likelihood_f32_kernel<1><<<grid, kBlock, 0, st>>>(*a);
+    switch (group)
+    {
+    case 0: launch_group<0>(phase, a, grid, st); break;
+    case 1: launch_group<1>(phase, a, grid, st); break;
+    case 2: launch_group<2>(phase, a, grid, st); break;
+    case 3: launch_group<3>(phase, a, grid, st); break;
+    case 4: launch_group<4>(phase, a, grid, st); break;
+    default: launch_group<5>(phase, a, grid, st); break;
+    }
     return (int)cudaGetLastError();
 }
 
-extern "C" int mwsep_engine_f32_blocks_per_sm(int phase, int cls)
+extern "C" int mwsep_engine_f32_blocks_per_sm(int phase, int group)
 {
     int b = 0;
     cudaError_t e;
-    if (phase == 0 && cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f32_kernel<0>, kBlock, 0);
-    else if (phase == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f32_kernel<1>, kBlock, 0);
-    else if (cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f32_kernel<0>, kBlock, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f32_kernel<1>, kBlock, 0);
+    switch (group)
+    {
+    case 0: e = group_occupancy<0>(&b, phase); break;
+    case 1: e = group_occupancy<1>(&b, phase); break;
+    case 2: e = group_occupancy<2>(&b, phase); break;
+    case 3: e = group_occupancy<3>(&b, phase); break;
+    case 4: e = group_occupancy<4>(&b, phase); break;
+    default: e = group_occupancy<5>(&b, phase); break;
+    }
     if (e != cudaSuccess)
     {
         cudaGetLastError();

@@ -44,17 +44,26 @@ __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta
     store_partial<1 + SMAX>(acc, 1 + th.n_streams, red, out);
 }
 
-template <int CLS>
+/* The FP64 kernels are specialised on a bound of the stream count: group G
+ * (the stream count up to 4, or 5 for 5..8) runs with SMAX = 1, 1, 2, 4, 4, 8. */
+template <int G>
+struct GroupSmax
+{
+    static constexpr int S = G <= 1 ? 1 : G == 2 ? 2 : G <= 4 ? 4 : 8;
+};
+
+template <int G>
 __global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep_engine_args a)
 {
+    constexpr int SMAX = GroupSmax<G>::S;
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
-    __shared__ double red[2 * (CLS == 0 ? 5 : MWSEP_ENG_ICOMP) * 32];
+    __shared__ double red[2 * (1 + SMAX) * 32];
     __shared__ int s_tile;
-    const int n_tiles = a.counters[4 * CLS + 2];
+    const int n_tiles = a.counters[4 * G + 2];
     for (;;)
     {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 0], 1);
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 0], 1);
         __syncthreads();
         const int t = s_tile;
         if (t >= n_tiles) break;
@@ -63,10 +72,7 @@ __global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep
         load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
         __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
-        if (CLS == 1) itile<8>(A, th, tile, red, out);
-        else if (th.n_streams <= 1) itile<1>(A, th, tile, red, out);
-        else if (th.n_streams <= 2) itile<2>(A, th, tile, red, out);
-        else itile<4>(A, th, tile, red, out);
+        itile<SMAX>(A, th, tile, red, out);
         __syncthreads();
     }
 }
@@ -83,16 +89,17 @@ __device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_the
     store_partial<3 + SMAX>(acc, 3 + th.n_streams, red, out);
 }
 
-template <int CLS>
+template <int G>
 __global__ void __launch_bounds__(kBlock) engine_likelihood_f64_kernel(const mwsep_engine_args a)
 {
+    constexpr int SMAX = GroupSmax<G>::S;
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (CLS == 0 ? 7 : MWSEP_ENG_LCOMP) * 32];
+    __shared__ double red[2 * (3 + SMAX) * 32];
     __shared__ int s_tile;
-    const int n_tiles = a.counters[4 * CLS + 3];
+    const int n_tiles = a.counters[4 * G + 3];
     for (;;)
     {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * CLS + 1], 1);
+        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 1], 1);
         __syncthreads();
         const int t = s_tile;
         if (t >= n_tiles) break;
@@ -103,34 +110,61 @@ __global__ void __launch_bounds__(kBlock) engine_likelihood_f64_kernel(const mws
             a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
-        if (CLS == 1) ltile<8>(St, th, I, tile, red, out);
-        else if (th.n_streams <= 1) ltile<1>(St, th, I, tile, red, out);
-        else if (th.n_streams <= 2) ltile<2>(St, th, I, tile, red, out);
-        else ltile<4>(St, th, I, tile, red, out);
+        ltile<SMAX>(St, th, I, tile, red, out);
         __syncthreads();
     }
 }
 
 } // namespace
 
-extern "C" int mwsep_engine_f64_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream)
+namespace {
+
+template <int G>
+void launch_group(int phase, const mwsep_engine_args* a, int grid, cudaStream_t st)
+{
+    if (phase == 0)
+        engine_integral_f64_kernel<G><<<grid, kBlock, 0, st>>>(*a);
+    else
+        engine_likelihood_f64_kernel<G><<<grid, kBlock, 0, st>>>(*a);
+}
+
+template <int G>
+cudaError_t group_occupancy(int* b, int phase)
+{
+    return phase == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_integral_f64_kernel<G>, kBlock, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_likelihood_f64_kernel<G>, kBlock, 0);
+}
+
+} // namespace
+
+extern "C" int mwsep_engine_f64_launch(int phase, int group, const mwsep_engine_args* a, int grid, void* stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (phase == 0 && cls == 0) engine_integral_f64_kernel<0><<<grid, kBlock, 0, st>>>(*a);
-    else if (phase == 0) engine_integral_f64_kernel<1><<<grid, kBlock, 0, st>>>(*a);
-    else if (cls == 0) engine_likelihood_f64_kernel<0><<<grid, kBlock, 0, st>>>(*a);
-    else engine_likelihood_f64_kernel<1><<<grid, kBlock, 0, st>>>(*a);
+    switch (group)
+    {
+    case 0: launch_group<0>(phase, a, grid, st); break;
+    case 1: launch_group<1>(phase, a, grid, st); break;
+    case 2: launch_group<2>(phase, a, grid, st); break;
+    case 3: launch_group<3>(phase, a, grid, st); break;
+    case 4: launch_group<4>(phase, a, grid, st); break;
+    default: launch_group<5>(phase, a, grid, st); break;
+    }
     return (int)cudaGetLastError();
 }
 
-extern "C" int mwsep_engine_f64_blocks_per_sm(int phase, int cls)
+extern "C" int mwsep_engine_f64_blocks_per_sm(int phase, int group)
 {
     int b = 0;
     cudaError_t e;
-    if (phase == 0 && cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f64_kernel<0>, kBlock, 0);
-    else if (phase == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_integral_f64_kernel<1>, kBlock, 0);
-    else if (cls == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f64_kernel<0>, kBlock, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, engine_likelihood_f64_kernel<1>, kBlock, 0);
+    switch (group)
+    {
+    case 0: e = group_occupancy<0>(&b, phase); break;
+    case 1: e = group_occupancy<1>(&b, phase); break;
+    case 2: e = group_occupancy<2>(&b, phase); break;
+    case 3: e = group_occupancy<3>(&b, phase); break;
+    case 4: e = group_occupancy<4>(&b, phase); break;
+    default: e = group_occupancy<5>(&b, phase); break;
+    }
     if (e != cudaSuccess)
     {
         cudaGetLastError();

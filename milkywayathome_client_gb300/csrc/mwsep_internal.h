@@ -181,14 +181,15 @@ typedef struct
     int pad0;
 } mwsep_ltile;
 
-/* Requests are split into two kernel classes: up to 4 streams (class 0,
- * the common case, specialised per stream count) and 5..8 streams
- * (class 1).  Device-side counters of one engine launch, per class c:
- * [4c+0] next integral tile, [4c+1] next likelihood tile, [4c+2] end of the
- * class's integral tiles, [4c+3] end of its likelihood tiles; [8] requests.
- * A class's tiles are contiguous and start where its "next" counters start. */
-#define MWSEP_ENG_COUNTERS 12
-#define MWSEP_ENG_NREQ 8
+/* Requests are split into kernel groups by stream count: group g = S for
+ * S <= 4 (each kernel specialised on its exact S), group 5 for 5..8 streams.
+ * Device-side counters of one engine launch, per group g: [4g+0] next
+ * integral tile, [4g+1] next likelihood tile, [4g+2] end of the group's
+ * integral tiles, [4g+3] end of its likelihood tiles; [24] requests.  A
+ * group's tiles are contiguous and start where its "next" counters start. */
+#define MWSEP_ENG_GROUPS 6
+#define MWSEP_ENG_COUNTERS 28
+#define MWSEP_ENG_NREQ 24
 
 typedef struct
 {
@@ -210,11 +211,11 @@ typedef struct
 extern "C" {
 #endif
 /* Engine launchers: persistent grids (grid = resident blocks x SMs). */
-/* phase 0: integrals, 1: likelihood; cls: 0 (<= 4 streams) or 1 (5..8) */
-int mwsep_engine_f32_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream);
-int mwsep_engine_f64_launch(int phase, int cls, const mwsep_engine_args* a, int grid, void* stream);
-int mwsep_engine_f32_blocks_per_sm(int phase, int cls);
-int mwsep_engine_f64_blocks_per_sm(int phase, int cls);
+/* phase 0: integrals, 1: likelihood; group: the stream count (0..4) or 5 (5..8 streams) */
+int mwsep_engine_f32_launch(int phase, int group, const mwsep_engine_args* a, int grid, void* stream);
+int mwsep_engine_f64_launch(int phase, int group, const mwsep_engine_args* a, int grid, void* stream);
+int mwsep_engine_f32_blocks_per_sm(int phase, int group);
+int mwsep_engine_f64_blocks_per_sm(int phase, int group);
 /* per-request fixed-order reductions: phase 0 integrals (+ cut
  * subtraction), phase 1 likelihood */
 int mwsep_engine_reduce(int phase, const mwsep_engine_args* a, int grid, void* stream);
