@@ -89,3 +89,37 @@ def test_cancel_and_timeout(served):
             assert srv.wait(fresh, 300).likelihood == srv.wait(ids[0], 300).likelihood
         for i in ids[1:-1]:
             srv.wait(i, 300)
+
+
+def test_lane_budget_refuses_and_server_keeps_serving(served):
+    """A lane whose device-memory share cannot hold even one request reports
+    MWSEP_ERR_BUDGET for it (admission by HBM footprint) and stays usable."""
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    ctx, wedges = served
+    w, base = wedges[0]
+    with mw.Server(ctx, lanes=1, max_batch=8, lane_hbm_bytes=1) as srv:
+        ids = [srv.submit(w, base, mw.MWSEP_MIXED_F32) for _ in range(3)]
+        for i in ids:
+            st, res = srv.try_wait(i, 300)
+            assert st == N.MWSEP_ERR_BUDGET and res is None
+        s = srv.stats()
+        assert s["failed"] == 3 and s["completed"] == 0
+
+
+def test_destroy_with_queued_requests_returns(served):
+    """Destroying a server with work queued cancels the queue, lets the
+    running batch finish, and returns."""
+    import time
+    import milkywayathome_client_gb300 as mw
+    ctx, wedges = served
+    w, base = wedges[2]
+    srv = mw.Server(ctx, lanes=1, max_batch=1)
+    for _ in range(50):
+        srv.submit(w, base, mw.MWSEP_PLAIN_F64)
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 120
+    # the context still evaluates afterwards
+    r = ctx.evaluate_requests([(w, base)], mw.MWSEP_PLAIN_F64)[0]
+    assert r.likelihood == r.likelihood
