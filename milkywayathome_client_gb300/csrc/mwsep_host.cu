@@ -391,6 +391,11 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             nk = std::max<long long>(1, std::min<long long>(nk, max_r));
             int kc = (int)((max_r + nk - 1) / nk);
             const int ks = warp_tile_kstep(p.convolve, p.n_streams);
+            /* at least four lane groups of points per column of a tile, so
+             * the column prologue and the last group's padding stay small */
+            const int group = 32 * (p.n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
+            const int kmin = std::min(max_r, ((4 * group + p.convolve - 1) / p.convolve + ks - 1) / ks * ks);
+            kc = std::max(kc, kmin);
             if (kc >= ks) kc = kc / ks * ks;
             t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", kc);
             long long g = (long long)c->sm_count * per_sm;
