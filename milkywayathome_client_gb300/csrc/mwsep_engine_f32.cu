@@ -105,15 +105,15 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
 }
 
 template <int S>
-__device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_theta_consts& th, const double* I,
-                                      const mwsep_ltile& t, double* red, double2* out)
+__device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
+                                      const LkScale<S>& ks, const mwsep_ltile& t, double* red, double2* out)
 {
     double acc[3 + S];
 #pragma unroll
     for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
     const BgConsts bc = bg_consts(th);
     for (int s0 = t.star_begin + threadIdx.x; s0 < t.star_end; s0 += blockDim.x)
-        likelihood_star<S>(St, th, bc, I, s0, acc);
+        likelihood_star<S>(St, th, bc, ks, s0, acc);
     reduce_and_store<3 + S>(acc, 3 + th.n_streams, red, out);
 }
 
@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
     constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (3 + S) * 32];
+    __shared__ LkScale<S> ks;
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * G + 3];
     for (;;)
@@ -137,8 +138,10 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
         const mwsep_stars_dev St =
             a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
+        if (threadIdx.x == 0) lk_scale<S>(th, I, ks);
+        __syncthreads();
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
-        ltile<S>(St, th, I, tile, red, out);
+        ltile<S>(St, th, ks, tile, red, out);
         __syncthreads();
     }
 }

@@ -91,10 +91,12 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
 {
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (3 + S) * 32];
+    __shared__ LkScale<S> ks;
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     const int NS = th.n_streams;
-    const double* I = integrals + (size_t)blockIdx.y * (1 + NS);
+    if (threadIdx.x == 0) lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
+    __syncthreads();
     const BgConsts bc = bg_consts(th);
 
     double acc[3 + S];
@@ -103,7 +105,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
 
     const int N = St.n_stars;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
-        likelihood_star<S>(St, th, bc, I, s0, acc);
+        likelihood_star<S>(St, th, bc, ks, s0, acc);
     reduce_and_store<3 + S>(acc, 3 + NS, red,
                             partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }

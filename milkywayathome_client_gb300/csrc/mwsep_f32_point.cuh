@@ -665,12 +665,31 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     __syncwarp();
 }
 
+/* The per-evaluation factors of the likelihood's mixture: w_b / I_b,
+ * w_s / I_s and 1 / (0.001 sum w), formed once per block so the per-star
+ * epilogue multiplies instead of dividing. */
+template <int S>
+struct LkScale
+{
+    double bg, st[SArr<S>::N], inv_sw;
+};
+
+template <int S>
+__device__ __forceinline__ void lk_scale(const mwsep_theta_consts& th, const double* I, LkScale<S>& k)
+{
+    k.bg = th.exp_bg_weight / I[0];
+#pragma unroll
+    for (int s = 0; s < S; ++s) k.st[s] = (s < th.n_streams) ? th.exp_stream_weight[s] / I[1 + s] : 0.0;
+    k.inv_sw = 1.0 / th.sum_exp_weights;
+}
+
 /* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717):
  * the density sums in FP32, everything after them in FP64.  acc slots:
  * [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
 template <int S>
 __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                                const BgConsts& bc, const double* I, int s0, double (&acc)[3 + S])
+                                                const BgConsts& bc, const LkScale<S>& ks, int s0,
+                                                double (&acc)[3 + S])
 {
     const int NS = th.n_streams;
     const int N = St.n_stars;
@@ -687,20 +706,20 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     }
     /* the star weights carry its reff_xr_rp3 */
     const double bg = (th.bg_mode == 2) ? -1.0 : (double)bgf;
-    double bg_only = (bg / I[0]) * th.exp_bg_weight;
+    double bg_only = bg * ks.bg;
     double star_prob = bg_only;
-    acc[2] += (bg_only == 0.0) ? -238.0 : log10(bg_only / th.sum_exp_weights);
+    acc[2] += (bg_only == 0.0) ? -238.0 : log10(bg_only * ks.inv_sw);
 #pragma unroll
     for (int s = 0; s < S; ++s)
     {
         if (s < NS)
         {
-            double st_only = (double)stf[s] / I[1 + s] * th.exp_stream_weight[s];
+            double st_only = (double)stf[s] * ks.st[s];
             star_prob += st_only;
-            acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only / th.sum_exp_weights);
+            acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only * ks.inv_sw);
         }
     }
-    star_prob /= th.sum_exp_weights;
+    star_prob *= ks.inv_sw;
     if (star_prob != 0.0)
         acc[0] += log10(star_prob);
     else
