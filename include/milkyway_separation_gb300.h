@@ -172,7 +172,15 @@ enum
     /* Densities and exp in FP32 (SFU) with compensated per-thread sums;
      * geometry, tables, cross-block sums, normalisation and the
      * log-likelihood in FP64.  Within 1e-7 absolute on the log-likelihood. */
-    MWSEP_MIXED_F32 = 1
+    MWSEP_MIXED_F32 = 1,
+    /* The plain form's accuracy (1e-12 relative on the integrals) computed in
+     * double-float arithmetic -- pairs of FP32 values, about 48 bits -- on
+     * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Covers the
+     * alpha = delta = 1 background without the aux profile and up to 4
+     * streams; any other problem is evaluated as MWSEP_PLAIN_F64.  Single-wedge evaluations and batches
+     * (mwsep_ctx_evaluate / _batch); the engine and the server take the
+     * other two forms. */
+    MWSEP_PLAIN_DF = 2
 };
 
 const char* mwsep_status_string(int status);

@@ -39,6 +39,7 @@ UNITS = [
     ("mwsep_engine_f32.cu", ["-fmad=true"]),
     ("mwsep_engine_f64.cu", ["-fmad=false"]),
     ("mwsep_separation.cu", ["-fmad=false"]),
+    ("mwsep_df.cu", ["-fmad=true"]),
     ("mwsep_io.cpp", []),
     ("mwsep_server.cpp", []),
     ("mwsep_optimise.cpp", []),

@@ -86,7 +86,7 @@ struct AreaHost
 
 struct AreaDev
 {
-    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, pts;
+    DevBuf geom, r_point, qw, r_in_mag, r_in_mag2, reff, irv, ids, nus, pts, ptsdf;
     mwsep_area_dev view{};
 };
 
@@ -137,7 +137,7 @@ struct Wedge
     mwsep_stars_dev stars_view{};
     HostPinned h_stars;
 
-    Tune tune[2];
+    Tune tune[3]; /* per precision: plain FP64, compensated FP32, double-float */
     unsigned tune_gen = 0; /* bumped whenever tune[] changes */
     size_t bytes = 0;      /* device bytes this wedge holds */
 };

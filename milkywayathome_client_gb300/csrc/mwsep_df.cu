@@ -1,0 +1,288 @@
+/* mwsep_df.cu -- the plain form's integral in double-float arithmetic
+ * (MWSEP_PLAIN_DF): FP64-level accuracy computed on the FP32 pipes.
+ *
+ * Same decomposition as the compensated warp tiles (32 mu-columns at one nu
+ * and a run of r-bins per warp; each lane holds DFP points of a group, the
+ * columns' constants are broadcast from shared memory), with every quantity
+ * carried as a double-float pair (mwsep_df.cuh):
+ *   t = r - rb,  rg = sqrt(B2 t^2 + Db),  bg += w / (rg (rg + r0)^3),
+ *   stream s:  st_s += w 2^(k2_s (r - rs_s)^2 + k0_s),
+ * where w = qw_r3_N * reff_xr_rp3 * irv is the table weight (as a pair), the
+ * completed-square constants are formed per column in FP64 (as in the plain
+ * FP64 kernel) and the stream exponent is in base 2.  FP32 has an exponent
+ * range of 2^+-126, so each stream's exponents are shifted by a per-tile
+ * power of two (the largest floor(k0_s) among the tile's columns; k2_s <= 0
+ * so no point exceeds its column's k0_s) and the sums are scaled back in
+ * FP64 -- tiny integrals keep their FP64 magnitude.  Terms more than 2^126
+ * below the tile's largest are dropped, far below FP64 resolution.
+ *
+ * Per lane the group sums are double-float; per group they go to FP64
+ * (times ids), across blocks the usual compensated FP64 reduction.
+ *
+ * Background forms: alpha = delta = 1 without the aux profile, up to 4
+ * streams; the host runs any other problem through the native FP64 kernel.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mwsep_checks.cuh"
+#include "mwsep_df.cuh"
+#include "mwsep_f64_point.cuh"
+#include "mwsep_internal.h"
+#include "mwsep_reduce.cuh"
+
+#ifndef MWSEP_DF_TILE_P
+#define MWSEP_DF_TILE_P 8
+#endif
+
+namespace {
+
+using mwsep::dfl::df;
+namespace D = mwsep::dfl;
+
+constexpr int kBlock = 256;
+constexpr int DFP = MWSEP_DF_TILE_P; /* points per lane per group */
+
+/* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0. */
+template <int S>
+struct ColDF
+{
+    static constexpr int W = 2 * (3 + 3 * S); /* floats */
+};
+
+/* 2^(j/64), j < 64, as pairs (host-built). */
+__constant__ float2 c_exp2_tab[64];
+
+template <int S>
+__device__ __forceinline__ void put(float* dst, int i, double v)
+{
+    const df x = D::from_double(v);
+    dst[2 * i] = x.hi;
+    dst[2 * i + 1] = x.lo;
+}
+
+template <int S>
+__device__ __forceinline__ df get(const float* src, int i)
+{
+    const float2 v = reinterpret_cast<const float2*>(src)[i];
+    return D::mk(v.x, v.y);
+}
+
+/* One warp tile of the double-float integral (all 32 lanes). */
+template <int S>
+__device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwsep_theta_consts& th, long long wt,
+                                             float* __restrict__ cs, const df* __restrict__ tab,
+                                             double (&acc)[1 + S])
+{
+    constexpr int CW = ColDF<S>::W;
+    const int lane = threadIdx.x & 31;
+    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
+    const long long rest = wt / nmb;
+    const int mb = (int)(wt - rest * nmb);
+    const int kc = (int)(rest / A.nu_steps);
+    const int nu = (int)(rest - (long long)kc * A.nu_steps);
+    const int mu0 = mb * mwsep::kTileCols;
+    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+
+    /* column constants (FP64), with each stream's exponent shifted by the
+     * tile's largest floor(k0) */
+    mwsep::f64::ColF64<(S > 0 ? S : 1)> cc;
+    double k2b[S > 0 ? S : 1], k0b[S > 0 ? S : 1];
+    int eref[S > 0 ? S : 1];
+    const bool live = lane < ncols;
+    if (live)
+    {
+        const double* g = A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1);
+        mwsep::f64::column_consts_f64<(S > 0 ? S : 1)>(g[0], g[1], g[2], g[3], th, cc);
+    }
+    constexpr double kLog2e = 1.4426950408889634073599246810018921;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        const bool on = live && s < th.n_streams && th.stream_on[s];
+        k2b[s] = on ? cc.k2[s] * kLog2e : 0.0;
+        k0b[s] = on ? cc.k0[s] * kLog2e : -1.0e300;
+        int e = on ? (int)fmax(floor(k0b[s]), -2000000000.0) : -2000000000;
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        eref[s] = e;
+    }
+    if (live)
+    {
+        float* c = cs + lane * CW;
+        put<S>(c, 0, cc.B2);
+        put<S>(c, 1, cc.rb);
+        put<S>(c, 2, cc.Db);
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            const bool on = s < th.n_streams && th.stream_on[s] && eref[s] > -2000000000;
+            put<S>(c, 3 + 3 * s, cc.rs[s]);
+            put<S>(c, 4 + 3 * s, k2b[s]);
+            put<S>(c, 5 + 3 * s, on ? k0b[s] - (double)eref[s] : -1.0e30);
+        }
+    }
+    __syncwarp();
+    double scale[S > 0 ? S : 1];
+#pragma unroll
+    for (int s = 0; s < S; ++s) scale[s] = (eref[s] > -1100) ? ldexp(1.0, eref[s]) : 0.0;
+
+    const df r0 = D::from_double(th.r0);
+    const int C = A.convolve;
+    const int k0 = kc * A.k_chunk;
+    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int nf = (k1 - k0) * C;
+    const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
+    for (int g0 = 0; g0 < nf; g0 += 32 * DFP)
+    {
+        df r[DFP], w[DFP];
+#pragma unroll
+        for (int i = 0; i < DFP; ++i)
+        {
+            const int f = g0 + 32 * i + lane;
+            /* past the tile's end: a copy of its first point with zero weight */
+            const float4 v = A.ptsdf[MWSEP_IDX((size_t)k0 * C + (f < nf ? f : 0), (size_t)A.r_steps * C, 2)];
+            r[i] = D::mk(v.x, v.y);
+            w[i] = (f < nf) ? D::mk(v.z, v.w) : D::mk(0.f, 0.f);
+        }
+        df bg = D::mk(0.f, 0.f), st[S > 0 ? S : 1];
+#pragma unroll
+        for (int s = 0; s < S; ++s) st[s] = D::mk(0.f, 0.f);
+        for (int j = 0; j < ncols; ++j)
+        {
+            const float* c = cs + j * CW;
+            const df B2 = get<S>(c, 0), nrb = D::neg(get<S>(c, 1)), Db = get<S>(c, 2);
+#pragma unroll
+            for (int i = 0; i < DFP; ++i)
+            {
+                const df t = D::add(r[i], nrb);
+                const df rg = D::sqrt(D::add_same(D::mul(B2, D::sqr(t)), Db));
+                const df sum = D::add_same(rg, r0);
+                const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
+                bg = D::add_same(bg, D::mul(w[i], D::recip(den)));
+#pragma unroll
+                for (int s = 0; s < S; ++s)
+                {
+                    const df u = D::add(r[i], D::neg(get<S>(c, 3 + 3 * s)));
+                    const df a = D::add(D::mul(get<S>(c, 4 + 3 * s), D::sqr(u)), get<S>(c, 5 + 3 * s));
+                    st[s] = D::add_same(st[s], D::mul(w[i], D::exp2(a, tab)));
+                }
+            }
+        }
+        acc[0] += ((double)bg.hi + (double)bg.lo) * idsv;
+#pragma unroll
+        for (int s = 0; s < S; ++s) acc[1 + s] += ((double)st[s].hi + (double)st[s].lo) * scale[s] * idsv;
+    }
+    __syncwarp();
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area_dev A,
+                                                                const mwsep_theta_consts* __restrict__ thetas,
+                                                                double2* __restrict__ partials, long long theta_stride)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ double red[2 * (1 + S) * 32];
+    __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * ColDF<S>::W];
+    __shared__ df tab[64];
+    mwsep::f64::load_theta(th, thetas + blockIdx.y);
+    if (threadIdx.x < 64) tab[threadIdx.x] = D::mk(c_exp2_tab[threadIdx.x].x, c_exp2_tab[threadIdx.x].y);
+    __syncthreads();
+    double acc[1 + S];
+#pragma unroll
+    for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
+    const int warp = threadIdx.x >> 5;
+    const long long warps = (long long)gridDim.x * (kBlock / 32);
+    for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
+        warp_tile_df<S>(A, th, wt, cs[warp], tab, acc);
+    /* block reduction into compensated pairs */
+    mwsep::comp_sum cacc[1 + S];
+#pragma unroll
+    for (int k = 0; k < 1 + S; ++k)
+    {
+        cacc[k].s = acc[k];
+        cacc[k].c = 0.0;
+    }
+    mwsep::block_reduce<1 + S>(cacc, red);
+    if (threadIdx.x == 0)
+    {
+        double2* out = partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams);
+#pragma unroll
+        for (int k = 0; k < 1 + S; ++k)
+            if (k < 1 + th.n_streams) out[k] = make_double2(cacc[k].s, cacc[k].c);
+    }
+}
+
+template <int S>
+int launch(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_launch_shape* sh, double2* partials,
+           cudaStream_t st)
+{
+    const long long ncomp = 1 + sh->n_streams;
+    const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
+    double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
+    dim3 g(sh->grid, sh->n_theta);
+    integral_df_kernel<S><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
+    return (int)cudaGetLastError();
+}
+
+template <int S>
+cudaError_t occupancy(int* b)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_df_kernel<S>, kBlock, 0);
+}
+
+bool g_table_ready[64] = {};
+
+} // namespace
+
+/* Upload the 2^(j/64) table to this device (once per device). */
+extern "C" int mwsep_df_prepare(int device)
+{
+    if (device < 0 || device >= 64) return 1;
+    if (g_table_ready[device]) return 0;
+    float2 t[64];
+    for (int j = 0; j < 64; ++j)
+    {
+        const mwsep::dfl::df v = mwsep::dfl::from_double(exp2((double)j / 64.0));
+        t[j] = make_float2(v.hi, v.lo);
+    }
+    if (cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t)) != cudaSuccess) return 1;
+    g_table_ready[device] = true;
+    return 0;
+}
+
+extern "C" int mwsep_integral_df_blocks_per_sm(int n_streams)
+{
+    int b = 0;
+    cudaError_t e;
+    switch (n_streams)
+    {
+    case 0: e = occupancy<0>(&b); break;
+    case 1: e = occupancy<1>(&b); break;
+    case 2: e = occupancy<2>(&b); break;
+    case 3: e = occupancy<3>(&b); break;
+    default: e = occupancy<4>(&b); break; /* 5..8 streams run in native FP64 */
+    }
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return b > 0 ? b : 1;
+}
+
+extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                        const mwsep_launch_shape* sh, double2* partials, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (sh->n_streams)
+    {
+    case 0: return launch<0>(area, th_dev, sh, partials, st);
+    case 1: return launch<1>(area, th_dev, sh, partials, st);
+    case 2: return launch<2>(area, th_dev, sh, partials, st);
+    case 3: return launch<3>(area, th_dev, sh, partials, st);
+    case 4: return launch<4>(area, th_dev, sh, partials, st);
+    default: return (int)cudaErrorInvalidValue; /* 5..8 streams run in native FP64 */
+    }
+}
+
+MWSEP_CHECKS_READER(mwsep_checks_df)

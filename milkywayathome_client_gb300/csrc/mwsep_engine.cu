@@ -482,6 +482,7 @@ extern "C" int mwsep_ctx_evaluate_requests(mwsep_ctx* c, int n, const mwsep_requ
                                            mwsep_result* out)
 {
     if (!c || !out) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision == MWSEP_PLAIN_DF) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
     int rc = check_requests(c, n, reqs);
     if (rc) return mwsep_fail(rc);
@@ -537,6 +538,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
 {
     mwsep::Range nvtx_range("mwsep.autotune");
     if (!c || id < 0 || id >= (int)c->wedges.size()) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision == MWSEP_PLAIN_DF) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
     Wedge& w = *c->wedges[id];
     if (!w.has_problem || !w.has_stars) return mwsep_fail(MWSEP_ERR_STATE);

@@ -371,13 +371,15 @@ void default_tune(mwsep_ctx* c, Wedge& w)
         max_cols = std::max<long long>(max_cols, (long long)p.area[a].mu_steps * p.area[a].nu_steps);
         max_r = std::max(max_r, p.area[a].r_steps);
     }
-    for (int prec = 0; prec < 2; ++prec)
+    for (int prec = 0; prec < 3; ++prec)
     {
         Tune& t = w.tune[prec];
         t.block = 256;
-        t.warp_items = (prec == MWSEP_MIXED_F32 && env_long("MWSEP_F32_WARP_TILES", 1) != 0) ? 1 : 0;
-        const int per_sm = prec == MWSEP_PLAIN_F64 ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
-                                                   : mwsep_integral_f32_blocks_per_sm(p.n_streams, t.warp_items);
+        t.warp_items = (prec == MWSEP_PLAIN_DF ||
+                        (prec == MWSEP_MIXED_F32 && env_long("MWSEP_F32_WARP_TILES", 1) != 0)) ? 1 : 0;
+        const int per_sm = prec == MWSEP_PLAIN_F64   ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
+                           : prec == MWSEP_PLAIN_DF ? mwsep_integral_df_blocks_per_sm(p.n_streams)
+                                                    : mwsep_integral_f32_blocks_per_sm(p.n_streams, t.warp_items);
         const long long threads = (long long)c->sm_count * per_sm * t.block;
         if (t.warp_items)
         {
@@ -390,10 +392,19 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             long long nk = (want + tiles_per_chunk - 1) / std::max<long long>(tiles_per_chunk, 1);
             nk = std::max<long long>(1, std::min<long long>(nk, max_r));
             int kc = (int)((max_r + nk - 1) / nk);
-            const int ks = warp_tile_kstep(p.convolve, p.n_streams);
+            const int group = prec == MWSEP_PLAIN_DF
+                                  ? 32 * MWSEP_DF_TILE_P
+                                  : 32 * (p.n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
+            int ks = group;
+            for (int a = group, b = std::max(p.convolve, 1); b;)
+            {
+                const int t2 = a % b;
+                a = b;
+                b = t2;
+                ks = group / a;
+            }
             /* at least four lane groups of points per column of a tile, so
              * the column prologue and the last group's padding stay small */
-            const int group = 32 * (p.n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
             const int kmin = std::min(max_r, ((4 * group + p.convolve - 1) / p.convolve + ks - 1) / ks * ks);
             kc = std::max(kc, kmin);
             if (kc >= ks) kc = kc / ks * ks;
@@ -438,7 +449,7 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
 
     /* cpu__r_constants (cpu/evaluation_optimized.c:360-422) on the host */
     std::vector<double> irv(R), reff(R), rp(RC), qw(RC), gm(RC), gm2(RC), ids(NU), nus(NU);
-    std::vector<float4> pts(RC);
+    std::vector<float4> pts(RC), ptsdf(RC);
     for (int i = 0; i < R; ++i)
     {
         const double log_r = A.r_min + (i * A.r_step);
@@ -457,6 +468,9 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
             gm2[o] = g * g;
             const float hi = (float)rp[o];
             pts[o] = make_float4(hi, (float)(rp[o] - (double)hi), (float)(qw[o] * (reff[i] * irv[i])), (float)g);
+            const double wd = qw[o] * (reff[i] * irv[i]);
+            const float whi = (float)wd;
+            ptsdf[o] = make_float4(hi, (float)(rp[o] - (double)hi), whi, (float)(wd - (double)whi));
         }
     }
     for (int j = 0; j < NU; ++j)
@@ -480,6 +494,7 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
     rc |= D.ids.ensure(NU * 8, tot);
     rc |= D.nus.ensure(NU * 8, tot);
     rc |= D.pts.ensure(RC * sizeof(float4), tot);
+    rc |= D.ptsdf.ensure(RC * sizeof(float4), tot);
     w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
 
@@ -493,6 +508,7 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
     CU(h2d(c, D.ids.p, ids.data(), NU * 8));
     CU(h2d(c, D.nus.p, nus.data(), NU * 8));
     CU(h2d(c, D.pts.p, pts.data(), RC * sizeof(float4)));
+    CU(h2d(c, D.ptsdf.p, ptsdf.data(), RC * sizeof(float4)));
     CK(mwsep_launch_geometry(A.mu_min, A.mu_step, A.mu_steps, D.nus.as<double>(), NU, p.sgr, p.wedge,
                              D.geom.as<double>(), st));
     /* the host vectors die with this frame: wait for the copies */
@@ -513,6 +529,7 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
     v.irv = D.irv.as<double>();
     v.ids = D.ids.as<double>();
     v.pts = D.pts.as<float4>();
+    v.ptsdf = D.ptsdf.as<float4>();
     return MWSEP_OK;
 }
 
@@ -585,7 +602,7 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     v.r = w.s_r.as<double>();
     w.n_stars = n;
     w.has_stars = true;
-    for (int prec = 0; prec < 2; ++prec)
+    for (int prec = 0; prec < 3; ++prec)
         w.tune[prec].lk_grid = occupancy_grid(c, w.tune[prec].lk_block, n);
     return MWSEP_OK;
 }
@@ -698,7 +715,7 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
     {
         AreaDev& D = w.areas[a];
         DevBuf* bufs[] = {&D.geom, &D.r_point, &D.qw, &D.r_in_mag, &D.r_in_mag2, &D.reff, &D.irv,
-                          &D.ids, &D.nus, &D.pts};
+                          &D.ids, &D.nus, &D.pts, &D.ptsdf};
         for (DevBuf* b : bufs) b->release(t);
     }
     DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.d_nfac, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
@@ -716,14 +733,24 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
         return mwsep_fail(MWSEP_ERR_STATE);
     Wedge& w = *c->wedges[0];
     if (B < 1 || B > 65535 || !thetas || !out) return mwsep_fail(MWSEP_ERR_ARG);
-    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
+        return mwsep_fail(MWSEP_ERR_ARG);
     const ProblemHost& p = w.prob;
     const int S = p.n_streams, A = p.n_areas, P = p.n_theta;
-    const Tune& t = w.tune[precision];
     const int ncomp = 1 + S, nslots = 3 + S;
 
     size_t& tot = c->dev_bytes;
     const size_t th_bytes = sizeof(mwsep_theta_consts) * (size_t)B;
+    if (c->h_theta.ensure(th_bytes)) return mwsep_fail(MWSEP_ERR_NOMEM);
+    mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
+    for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
+    /* the double-float integral covers the alpha = delta = 1, no-aux
+     * background with up to 4 streams; anything else runs in native FP64 */
+    if (precision == MWSEP_PLAIN_DF)
+        for (int i = 0; i < B; ++i)
+            if (mwsep_bg_form(&hth[i]) != 0 || S > 4) precision = MWSEP_PLAIN_F64;
+    if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
+    const Tune& t = w.tune[precision];
     const size_t part_bytes = sizeof(double2) * (size_t)B * A * t.grid * ncomp;
     const size_t lkpart_bytes = sizeof(double2) * (size_t)B * t.lk_grid * nslots;
     const size_t out_doubles = (size_t)B * (A * ncomp + ncomp + nslots);
@@ -732,12 +759,8 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     rc |= c->d_partials.ensure(part_bytes, tot);
     rc |= c->d_lkpartials.ensure(lkpart_bytes, tot);
     rc |= c->d_out.ensure(out_doubles * 8, tot);
-    rc |= c->h_theta.ensure(th_bytes);
     rc |= c->h_out.ensure(out_doubles * 8);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
-
-    mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
-    for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
 
     double* d_areas = c->d_out.as<double>();
     double* d_ints = d_areas + (size_t)B * A * ncomp;
@@ -770,6 +793,12 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
                                          c->d_partials.as<double2>(), st));
             ++launches;
         }
+        else if (precision == MWSEP_PLAIN_DF)
+        {
+            CK(mwsep_launch_integral_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                        c->d_partials.as<double2>(), st));
+            ++launches;
+        }
         else
         {
             for (int form = 0; form < 4; ++form)
@@ -790,7 +819,7 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     lk.block = t.lk_block;
     lk.grid = t.lk_grid;
     lk.area_index = 0;
-    if (precision == MWSEP_PLAIN_F64)
+    if (precision != MWSEP_MIXED_F32) /* plain and double-float: the FP64 likelihood */
         CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
     else

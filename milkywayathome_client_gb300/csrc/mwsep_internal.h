@@ -71,6 +71,9 @@ typedef struct
     /* compensated-FP32 table: per (k, n) {r_hi, r_lo, qw*reff*irv, g}
      * where r = r_hi + r_lo to ~2^-48 and the weight is rounded once */
     const float4* pts;       /* [R][C] */
+    /* double-float table: per (k, n) {r_hi, r_lo, w_hi, w_lo}, r and the
+     * weight qw*reff*irv each as an unevaluated FP32 pair (~2^-48) */
+    const float4* ptsdf;     /* [R][C] */
 } mwsep_area_dev;
 
 /* A resident catalogue on the device (tables are [C][N], star-minor). */
@@ -238,6 +241,14 @@ int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_con
                                 double2* partials, void* stream);
 /* Resident blocks per SM of the integral kernels (persistent-grid sizing). */
 int mwsep_integral_f32_blocks_per_sm(int n_streams, int warp_items);
+/* double-float integral (mwsep_df.cu) */
+#ifndef MWSEP_DF_TILE_P
+#define MWSEP_DF_TILE_P 8
+#endif
+int mwsep_df_prepare(int device);
+int mwsep_integral_df_blocks_per_sm(int n_streams);
+int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                             const mwsep_launch_shape* sh, double2* partials, void* stream);
 int mwsep_integral_f64_blocks_per_sm(int n_streams, int block);
 /* Reduce per-block compensated partials of every area into area integrals
  * and subtract the cut areas (cpu/evaluation_optimized.c:584-593):

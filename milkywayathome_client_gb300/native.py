@@ -33,6 +33,7 @@ MWSEP_MAX_AREAS = 8
 
 MWSEP_PLAIN_F64 = 0
 MWSEP_MIXED_F32 = 1
+MWSEP_PLAIN_DF = 2
 
 
 class INTEGRAL(C.Structure):

@@ -1,0 +1,86 @@
+"""GPU: the double-float form (MWSEP_PLAIN_DF) against the reference's own
+outputs at the plain form's tolerances (1e-12 relative on every integral,
+1e-12 absolute on the log-likelihood), against the native FP64 kernel at
+full size, batch == single, and its limits (other background forms and more
+than 4 streams run in native FP64; the engine refuses it)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_case
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+ABS_LOGL = 1e-12
+
+
+def _close_rel(a, b, tol):
+    if math.isnan(a) or math.isnan(b):
+        return math.isnan(a) and math.isnan(b)
+    if b == 0.0:
+        return a == 0.0
+    return abs(a - b) <= tol * abs(b)
+
+
+def _setup(ctx, name):
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    ctx.set_problem(mw.AstronomyParameters.read(pf))
+    ctx.set_stars(mw.StarPoints.read(sf))
+    return g
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_double_float_matches_reference(gpu_ctx, name):
+    import milkywayathome_client_gb300 as mw
+    g = _setup(gpu_ctx, name)
+    r = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+    for a, (got, want) in enumerate(zip(r.area_integrals, g["area_integrals"])):
+        for k, (x, y) in enumerate(zip(got, want)):
+            assert _close_rel(x, y, REL), f"area {a} comp {k}: {x!r} vs {y!r}"
+    assert _close_rel(r.background_integral, g["background_integral"], REL)
+    for x, y in zip(r.stream_integrals, g["stream_integrals"]):
+        assert _close_rel(x, y, REL), (x, y)
+    if not math.isnan(g["likelihood"]):
+        assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL, (r.likelihood, g["likelihood"])
+    assert r.num_zero == g["num_zero"]
+
+
+def test_double_float_batch_equals_single(gpu_ctx):
+    import milkywayathome_client_gb300 as mw
+    g = _setup(gpu_ctx, "three_streams")
+    base = np.asarray(g["theta"])
+    thetas = [base * (1 + 1e-3 * k) for k in range(5)]
+    single = [gpu_ctx.evaluate(t, mw.MWSEP_PLAIN_DF) for t in thetas]
+    batch = gpu_ctx.evaluate_batch(thetas, mw.MWSEP_PLAIN_DF)
+    for a, b in zip(single, batch):
+        assert a.likelihood == b.likelihood and a.integrals == b.integrals
+
+
+def test_double_float_matches_native_fp64_at_full_size(gpu_ctx):
+    """Config 0 at full size (80 x 40 x 70 cells, convolve 30)."""
+    import milkywayathome_client_gb300 as mw
+    g = _setup(gpu_ctx, "config0")
+    a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+    for x, y in zip(b.integrals, a.integrals):
+        assert _close_rel(x, y, REL), (x, y)
+    assert abs(a.likelihood - b.likelihood) <= ABS_LOGL
+
+
+def test_double_float_limits(gpu_ctx):
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    for name in ("aux_profile", "six_streams"):  # run in native FP64: identical bits
+        g = _setup(gpu_ctx, name)
+        a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+        b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+        assert a.integrals == b.integrals and a.likelihood == b.likelihood
+    pf, sf, g = load_case("basic_1stream")
+    with mw.Context(0) as ctx:
+        w = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
+        with pytest.raises(mw.MwsepError) as e:
+            ctx.evaluate_requests([(w, g["theta"])], mw.MWSEP_PLAIN_DF)
+        assert e.value.status == N.MWSEP_ERR_UNSUPPORTED
