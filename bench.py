@@ -10,6 +10,8 @@ milkywayathome_client_gb300/synthetic.py).  A step is one evaluation
              catalogue resident in HBM (device time from CUDA events on the
              library's stream; L2 flushed between steps)
   plain_f64  the same for the plain FP64 drop-in form
+  plain_double_float  the same for the double-float form (plain-form
+             accuracy, 1e-12, computed in pairs of FP32 values)
   e2e        evaluations/s through the reference-facing EvalFunc C-ABI call
              (mwsep_evaluate_mixed) with host structs: every step uploads the
              catalogue, rebuilds the wedge and star tables, evaluates and
@@ -301,6 +303,20 @@ def run_gb300_arm(args, ws, rank, local):
     f64_ms_step = allreduce_max(ws, sum(f64_ms)) / args.plain_steps
     plain_value = ws / (f64_ms_step * 1e-3)
 
+    # the double-float form: plain-form accuracy (1e-12) on the FP32 pipes
+    step(N.MWSEP_PLAIN_DF)
+    df_ms = []
+    for _ in range(args.plain_steps):
+        rdf, t, _ = step(N.MWSEP_PLAIN_DF)
+        df_ms.append(t["total_ms"])
+    df_ms_step = allreduce_max(ws, sum(df_ms)) / args.plain_steps
+    double_float = {"value": ws / (df_ms_step * 1e-3), "unit": "evals/s", "ms_per_step": df_ms_step,
+                    "dtype": "f32 pairs (double-float)",
+                    "speedup_vs_plain_f64": f64_ms_step / df_ms_step,
+                    "dlogL_vs_plain_f64": rdf.likelihood - r64.likelihood,
+                    "max_integral_rel_err_vs_plain_f64": max(abs(a - b) / abs(b) if b else 0.0
+                                                             for a, b in zip(rdf.integrals, r64.integrals))}
+
     # e2e through the EvalFunc C ABI with host buffers
     es = mw.EvaluationState(ap, sp)
     mw.evaluate_mixed(theta, ap, es, sp)  # warm-up (creates the library's default context)
@@ -356,6 +372,7 @@ def run_gb300_arm(args, ws, rank, local):
                        parallelism="replicas" if ws > 1 else "single GPU"),
         "impl": "gb300",
         "plain_f64": {"value": plain_value, "unit": "evals/s", "ms_per_step": f64_ms_step, "dtype": "f64"},
+        "plain_double_float": double_float,
         "speedup_mixed_vs_plain": value / plain_value,
         "dlogL_mixed_vs_plain": r32.likelihood - r64.likelihood,
         "integral_rel_err_mixed_vs_plain": [(a - b) / b if b else 0.0 for a, b in zip(r32.integrals,

@@ -10,11 +10,14 @@
  * where w = qw_r3_N * reff_xr_rp3 * irv is the table weight (as a pair), the
  * completed-square constants are formed per column in FP64 (as in the plain
  * FP64 kernel) and the stream exponent is in base 2.  FP32 has an exponent
- * range of 2^+-126, so each stream's exponents are shifted by a per-tile
- * power of two (the largest floor(k0_s) among the tile's columns; k2_s <= 0
- * so no point exceeds its column's k0_s) and the sums are scaled back in
- * FP64 -- tiny integrals keep their FP64 magnitude.  Terms more than 2^126
- * below the tile's largest are dropped, far below FP64 resolution.
+ * range of 2^+-126, so before each lane group the warp finds, in FP32, the
+ * largest stream exponent over the group's points and the tile's columns
+ * (a cheap pass: 4 operations per point, column and stream), and each column
+ * writes its k0 shifted by floor of that maximum, formed in FP64.  The
+ * group's largest term is then about 1 and its sums are scaled back in FP64,
+ * so integrals far below FP32 range keep their FP64 magnitude; terms more
+ * than 2^126 below the group's largest are dropped, far below FP64
+ * resolution of the sum.
  *
  * Per lane the group sums are double-float; per group they go to FP64
  * (times ids), across blocks the usual compensated FP64 reduction.
@@ -43,15 +46,16 @@ namespace D = mwsep::dfl;
 constexpr int kBlock = 256;
 constexpr int DFP = MWSEP_DF_TILE_P; /* points per lane per group */
 
-/* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0. */
+/* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0 - eref. */
 template <int S>
 struct ColDF
 {
     static constexpr int W = 2 * (3 + 3 * S); /* floats */
 };
+__host__ __device__ constexpr int kSP(int S) { return S > 0 ? S : 1; }
 
-/* 2^(j/64), j < 64, as pairs (host-built). */
-__constant__ float2 c_exp2_tab[64];
+/* 2^(j/1024) as pairs (host-built). */
+__constant__ float2 c_exp2_tab[D::kExp2Table];
 
 template <int S>
 __device__ __forceinline__ void put(float* dst, int i, double v)
@@ -71,8 +75,8 @@ __device__ __forceinline__ df get(const float* src, int i)
 /* One warp tile of the double-float integral (all 32 lanes). */
 template <int S>
 __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwsep_theta_consts& th, long long wt,
-                                             float* __restrict__ cs, const df* __restrict__ tab,
-                                             double (&acc)[1 + S])
+                                             float* __restrict__ cs, float* __restrict__ kf,
+                                             const float2* __restrict__ tab, double (&acc)[1 + S])
 {
     constexpr int CW = ColDF<S>::W;
     const int lane = threadIdx.x & 31;
@@ -84,30 +88,15 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     const int mu0 = mb * mwsep::kTileCols;
     const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
 
-    /* column constants (FP64), with each stream's exponent shifted by the
-     * tile's largest floor(k0) */
-    mwsep::f64::ColF64<(S > 0 ? S : 1)> cc;
-    double k2b[S > 0 ? S : 1], k0b[S > 0 ? S : 1];
-    int eref[S > 0 ? S : 1];
+    /* column constants (FP64); the stream exponents in base 2 */
+    mwsep::f64::ColF64<kSP(S)> cc;
+    double k0b[kSP(S)];
     const bool live = lane < ncols;
     if (live)
     {
         const double* g = A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1);
-        mwsep::f64::column_consts_f64<(S > 0 ? S : 1)>(g[0], g[1], g[2], g[3], th, cc);
-    }
-    constexpr double kLog2e = 1.4426950408889634073599246810018921;
-#pragma unroll
-    for (int s = 0; s < S; ++s)
-    {
-        const bool on = live && s < th.n_streams && th.stream_on[s];
-        k2b[s] = on ? cc.k2[s] * kLog2e : 0.0;
-        k0b[s] = on ? cc.k0[s] * kLog2e : -1.0e300;
-        int e = on ? (int)fmax(floor(k0b[s]), -2000000000.0) : -2000000000;
-        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-        eref[s] = e;
-    }
-    if (live)
-    {
+        mwsep::f64::column_consts_f64<kSP(S)>(g[0], g[1], g[2], g[3], th, cc);
+        constexpr double kLog2e = 1.4426950408889634073599246810018921;
         float* c = cs + lane * CW;
         put<S>(c, 0, cc.B2);
         put<S>(c, 1, cc.rb);
@@ -115,16 +104,15 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
 #pragma unroll
         for (int s = 0; s < S; ++s)
         {
-            const bool on = s < th.n_streams && th.stream_on[s] && eref[s] > -2000000000;
+            const bool on = s < th.n_streams && th.stream_on[s];
+            k0b[s] = on ? cc.k0[s] * kLog2e : -1.0e300;
             put<S>(c, 3 + 3 * s, cc.rs[s]);
-            put<S>(c, 4 + 3 * s, k2b[s]);
-            put<S>(c, 5 + 3 * s, on ? k0b[s] - (double)eref[s] : -1.0e30);
+            put<S>(c, 4 + 3 * s, on ? cc.k2[s] * kLog2e : 0.0);
+            put<S>(c, 5 + 3 * s, -1.0e30); /* set per group */
+            kf[lane * kSP(S) + s] = on ? (float)fmax(k0b[s], -1.0e30) : -1.0e30f;
         }
     }
     __syncwarp();
-    double scale[S > 0 ? S : 1];
-#pragma unroll
-    for (int s = 0; s < S; ++s) scale[s] = (eref[s] > -1100) ? ldexp(1.0, eref[s]) : 0.0;
 
     const df r0 = D::from_double(th.r0);
     const int C = A.convolve;
@@ -144,7 +132,45 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
             r[i] = D::mk(v.x, v.y);
             w[i] = (f < nf) ? D::mk(v.z, v.w) : D::mk(0.f, 0.f);
         }
-        df bg = D::mk(0.f, 0.f), st[S > 0 ? S : 1];
+        /* the group's largest stream exponent (FP32 estimate, error far
+         * below 1 for |k0| < 2^20), and the columns' k0 shifted by its floor */
+        double scale[kSP(S)];
+        if constexpr (S > 0)
+        {
+            float mx[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) mx[s] = -3.0e38f;
+            for (int j = 0; j < ncols; ++j)
+            {
+                const float* c = cs + j * CW;
+#pragma unroll
+                for (int s = 0; s < S; ++s)
+                {
+                    const float rs = c[2 * (3 + 3 * s)], k2 = c[2 * (4 + 3 * s)], k0 = kf[j * S + s];
+#pragma unroll
+                    for (int i = 0; i < DFP; ++i)
+                    {
+                        const float u = __fsub_rn(r[i].hi, rs);
+                        mx[s] = fmaxf(mx[s], __fmaf_rn(k2, __fmul_rn(u, u), k0));
+                    }
+                }
+            }
+            int eref[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+            {
+                for (int o = 16; o > 0; o >>= 1) mx[s] = fmaxf(mx[s], __shfl_xor_sync(0xffffffffu, mx[s], o));
+                eref[s] = (int)floorf(fmaxf(mx[s], -1100.0f));
+                scale[s] = eref[s] > -1100 ? ldexp(1.0, eref[s]) : 0.0;
+            }
+            __syncwarp(); /* every lane is done with the previous group's constants */
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+                if (live && s < th.n_streams && th.stream_on[s])
+                    put<S>(cs + lane * CW, 5 + 3 * s, fmax(k0b[s] - (double)eref[s], -1.0e30));
+            __syncwarp();
+        }
+        df bg = D::mk(0.f, 0.f), st[kSP(S)];
 #pragma unroll
         for (int s = 0; s < S; ++s) st[s] = D::mk(0.f, 0.f);
         for (int j = 0; j < ncols; ++j)
@@ -158,13 +184,13 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                 const df rg = D::sqrt(D::add_same(D::mul(B2, D::sqr(t)), Db));
                 const df sum = D::add_same(rg, r0);
                 const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
-                bg = D::add_same(bg, D::mul(w[i], D::recip(den)));
+                bg = D::add_same(bg, D::div(w[i], den));
 #pragma unroll
                 for (int s = 0; s < S; ++s)
                 {
                     const df u = D::add(r[i], D::neg(get<S>(c, 3 + 3 * s)));
                     const df a = D::add(D::mul(get<S>(c, 4 + 3 * s), D::sqr(u)), get<S>(c, 5 + 3 * s));
-                    st[s] = D::add_same(st[s], D::mul(w[i], D::exp2(a, tab)));
+                    st[s] = D::add_same(st[s], D::mul_raw(w[i], D::exp2(a, tab)));
                 }
             }
         }
@@ -183,9 +209,10 @@ __global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (1 + S) * 32];
     __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * ColDF<S>::W];
-    __shared__ df tab[64];
+    __shared__ float kf[kBlock / 32][mwsep::kTileCols * kSP(S)];
+    __shared__ float2 tab[D::kExp2Table];
     mwsep::f64::load_theta(th, thetas + blockIdx.y);
-    if (threadIdx.x < 64) tab[threadIdx.x] = D::mk(c_exp2_tab[threadIdx.x].x, c_exp2_tab[threadIdx.x].y);
+    for (int j = threadIdx.x; j < D::kExp2Table; j += kBlock) tab[j] = c_exp2_tab[j];
     __syncthreads();
     double acc[1 + S];
 #pragma unroll
@@ -193,7 +220,7 @@ __global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area
     const int warp = threadIdx.x >> 5;
     const long long warps = (long long)gridDim.x * (kBlock / 32);
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
-        warp_tile_df<S>(A, th, wt, cs[warp], tab, acc);
+        warp_tile_df<S>(A, th, wt, cs[warp], kf[warp], tab, acc);
     /* block reduction into compensated pairs */
     mwsep::comp_sum cacc[1 + S];
 #pragma unroll
@@ -234,15 +261,15 @@ bool g_table_ready[64] = {};
 
 } // namespace
 
-/* Upload the 2^(j/64) table to this device (once per device). */
+/* Upload the 2^(j/1024) table to this device (once per device). */
 extern "C" int mwsep_df_prepare(int device)
 {
     if (device < 0 || device >= 64) return 1;
     if (g_table_ready[device]) return 0;
-    float2 t[64];
-    for (int j = 0; j < 64; ++j)
+    float2 t[D::kExp2Table];
+    for (int j = 0; j < D::kExp2Table; ++j)
     {
-        const mwsep::dfl::df v = mwsep::dfl::from_double(exp2((double)j / 64.0));
+        const mwsep::dfl::df v = mwsep::dfl::from_double(exp2((double)j / D::kExp2Table));
         t[j] = make_float2(v.hi, v.lo);
     }
     if (cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t)) != cudaSuccess) return 1;

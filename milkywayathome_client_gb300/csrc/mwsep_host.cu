@@ -361,6 +361,42 @@ long env_long(const char* name, long dflt)
  * SM x SMs); items (column x r-run) are sized so each thread gets ~48, which
  * keeps the static tail near 2%.  The engine uses the same items, in tiles of
  * tile_items.  MWSEP_TUNE_{KCHUNK,GRID_F32,GRID_F64} override the choice. */
+/* Warp-tile r-chunk for a wedge too small to fill the GPU: over chunks of
+ * 1..kc_max bins, the modelled time is the larger of the per-SM work and one
+ * warp's chain of tiles at the speed of a lone warp (an SM saturates at about
+ * half its warp slots).  Work is counted in lane groups (ceil of the chunk's
+ * points over the group size, ragged last chunk included) plus `prologue`
+ * groups per tile for the column constants. */
+int fill_kchunk(int max_r, int convolve, int group, long long tiles_per_chunk, int sms, long long slots,
+                double prologue, int kc_max)
+{
+    const double wsat = std::max(1.0, 0.5 * (double)slots / std::max(sms, 1));
+    int best = kc_max;
+    double best_cost = 1e300;
+    for (int kc = 1; kc <= kc_max; ++kc)
+    {
+        const int nk = (max_r + kc - 1) / kc;
+        double work = 0.0, gmax = 0.0;
+        for (int k = 0; k < nk; ++k)
+        {
+            const long long pts = (long long)std::min(kc, max_r - k * kc) * std::max(convolve, 1);
+            const double g = (double)((pts + group - 1) / group) + prologue;
+            work += g;
+            gmax = std::max(gmax, g);
+        }
+        const long long tiles = tiles_per_chunk * nk;
+        const double per_sm = work * (double)tiles_per_chunk / std::max(sms, 1);
+        const double chain = wsat * gmax * (double)((tiles + slots - 1) / slots);
+        const double cost = std::max(per_sm, chain);
+        if (cost <= best_cost)
+        {
+            best_cost = cost;
+            best = kc;
+        }
+    }
+    return best;
+}
+
 void default_tune(mwsep_ctx* c, Wedge& w)
 {
     const ProblemHost& p = w.prob;
@@ -408,6 +444,13 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             const int kmin = std::min(max_r, ((4 * group + p.convolve - 1) / p.convolve + ks - 1) / ks * ks);
             kc = std::max(kc, kmin);
             if (kc >= ks) kc = kc / ks * ks;
+            /* a small wedge whose tiles would leave warps idle: the chunk that
+             * minimises the modelled time instead (lane groups per tile, a
+             * per-tile prologue, and one warp's sequential chain) */
+            const long long slots = threads / 32;
+            if (tiles_per_chunk * ((max_r + kc - 1) / kc) < slots)
+                kc = fill_kchunk(max_r, p.convolve, group, tiles_per_chunk, c->sm_count, slots,
+                                 prec == MWSEP_PLAIN_DF ? 0.1 : 0.8, kc);
             t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", kc);
             long long g = (long long)c->sm_count * per_sm;
             g = env_long("MWSEP_TUNE_GRID_F32", g);

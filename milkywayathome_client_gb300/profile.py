@@ -22,7 +22,7 @@ from .separation import AstronomyParameters, Context, StarPoints
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--precision", choices=["plain", "mixed", "df"], default="mixed")
     ap.add_argument("--evals", type=int, default=2)
     ap.add_argument("--batch", type=int, default=1)
     ap.add_argument("--engine", action="store_true")
@@ -32,7 +32,7 @@ def main():
     N.lib(build_if_missing=True)
     m = syn.materialise(a.config, a.data_dir)
     f = m["files"][0]
-    prec = N.MWSEP_MIXED_F32 if a.precision == "mixed" else N.MWSEP_PLAIN_F64
+    prec = {"mixed": N.MWSEP_MIXED_F32, "plain": N.MWSEP_PLAIN_F64, "df": N.MWSEP_PLAIN_DF}[a.precision]
     import numpy as np
     thetas = m.get("thetas")
     if thetas is None or len(thetas) < a.batch:

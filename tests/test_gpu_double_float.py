@@ -84,3 +84,26 @@ def test_double_float_limits(gpu_ctx):
         with pytest.raises(mw.MwsepError) as e:
             ctx.evaluate_requests([(w, g["theta"])], mw.MWSEP_PLAIN_DF)
         assert e.value.status == N.MWSEP_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("mu,sigma", [(200.0, 1.0), (250.0, 0.5), (300.0, 1.0), (340.0, 0.5)])
+def test_double_float_far_stream(gpu_ctx, mu, sigma):
+    """A narrow stream moved far from the wedge: its terms sit hundreds of
+    binary orders below 1, outside FP32 range, and the per-group exponent
+    shift must bring each group's largest term back near 1.  Integrals are
+    compared with the native FP64 kernel while they stay in normal FP64
+    range."""
+    import milkywayathome_client_gb300 as mw
+    g = _setup(gpu_ctx, "three_streams")
+    theta = np.asarray(g["theta"], dtype=np.float64).copy()
+    theta[3] = mu      # stream 1: mu (degrees)
+    theta[7] = sigma   # stream 1: sigma
+    a = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_DF)
+    for x, y in zip(b.integrals, a.integrals):
+        if abs(y) > 1e-280:
+            assert _close_rel(x, y, REL), (x, y)
+        else:
+            assert abs(x) <= 1e-270, (x, y)
+    if not (math.isnan(a.likelihood) or math.isinf(a.likelihood)):
+        assert abs(a.likelihood - b.likelihood) <= ABS_LOGL, (a.likelihood, b.likelihood)
