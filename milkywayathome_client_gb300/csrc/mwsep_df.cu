@@ -170,6 +170,10 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                     put<S>(cs + lane * CW, 5 + 3 * s, fmax(k0b[s] - (double)eref[s], -1.0e30));
             __syncwarp();
         }
+        /* Per column: the background over the lane's points, then one
+         * stream at a time (a rolled loop: the unrolled body of every stream
+         * over every point overflows the instruction cache).  Each stream's
+         * eight terms are summed as a pair, then added to its lane sum. */
         df bg = D::mk(0.f, 0.f), st[kSP(S)];
 #pragma unroll
         for (int s = 0; s < S; ++s) st[s] = D::mk(0.f, 0.f);
@@ -185,13 +189,20 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                 const df sum = D::add_same(rg, r0);
                 const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
                 bg = D::add_same(bg, D::div(w[i], den));
+            }
+#pragma unroll 1
+            for (int s = 0; s < S; ++s)
+            {
+                const df nrs = D::neg(get<S>(c, 3 + 3 * s)), k2 = get<S>(c, 4 + 3 * s), k0 = get<S>(c, 5 + 3 * s);
+                df part = D::mk(0.f, 0.f);
 #pragma unroll
-                for (int s = 0; s < S; ++s)
+                for (int i = 0; i < DFP; ++i)
                 {
-                    const df u = D::add(r[i], D::neg(get<S>(c, 3 + 3 * s)));
-                    const df a = D::add(D::mul(get<S>(c, 4 + 3 * s), D::sqr(u)), get<S>(c, 5 + 3 * s));
-                    st[s] = D::add_same(st[s], D::mul_raw(w[i], D::exp2(a, tab)));
+                    const df u = D::add(r[i], nrs);
+                    const df a = D::add(D::mul(k2, D::sqr(u)), k0);
+                    part = D::add_same(part, D::mul_raw(w[i], D::exp2(a, tab)));
                 }
+                st[s] = D::add_same(st[s], part);
             }
         }
         acc[0] += ((double)bg.hi + (double)bg.lo) * idsv;
