@@ -181,28 +181,38 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
         {
             const float* c = cs + j * CW;
             const df B2 = get<S>(c, 0), nrb = D::neg(get<S>(c, 1)), Db = get<S>(c, 2);
+            D::lazy_sum pb;
 #pragma unroll
             for (int i = 0; i < DFP; ++i)
             {
-                const df t = D::add(r[i], nrb);
-                const df rg = D::sqrt(D::add_same(D::mul(B2, D::sqr(t)), Db));
-                const df sum = D::add_same(rg, r0);
+                const df t = D::add_fast(r[i], nrb);
+                const df rg = D::sqrt(D::add_fast(D::mul(B2, D::sqr(t)), Db));
+                const df sum = D::add_fast(rg, r0);
                 const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
-                bg = D::add_same(bg, D::div(w[i], den));
+                const df q = D::div(w[i], den);
+                if (i == 0)
+                    pb = D::lazy_start(q);
+                else
+                    D::lazy_add(pb, q);
             }
+            bg = D::add_fast(bg, D::lazy_end(pb));
 #pragma unroll 1
             for (int s = 0; s < S; ++s)
             {
                 const df nrs = D::neg(get<S>(c, 3 + 3 * s)), k2 = get<S>(c, 4 + 3 * s), k0 = get<S>(c, 5 + 3 * s);
-                df part = D::mk(0.f, 0.f);
+                D::lazy_sum ps;
 #pragma unroll
                 for (int i = 0; i < DFP; ++i)
                 {
-                    const df u = D::add(r[i], nrs);
-                    const df a = D::add(D::mul(k2, D::sqr(u)), k0);
-                    part = D::add_same(part, D::mul_raw(w[i], D::exp2(a, tab)));
+                    const df u = D::add_fast(r[i], nrs);
+                    const df a = D::add_fast(D::mul(k2, D::sqr(u)), k0);
+                    const df e = D::mul_raw(w[i], D::exp2(a, tab));
+                    if (i == 0)
+                        ps = D::lazy_start(e);
+                    else
+                        D::lazy_add(ps, e);
                 }
-                st[s] = D::add_same(st[s], part);
+                st[s] = D::add_fast(st[s], D::lazy_end(ps));
             }
         }
         acc[0] += ((double)bg.hi + (double)bg.lo) * idsv;
