@@ -177,8 +177,10 @@ enum
      * double-float arithmetic -- pairs of FP32 values, about 48 bits -- on
      * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Covers the
      * alpha = delta = 1 background without the aux profile and up to 4
-     * streams; any other problem is evaluated as MWSEP_PLAIN_F64.  Single-wedge evaluations and batches
-     * (mwsep_ctx_evaluate / _batch); the engine and the server take the
+     * streams; any other problem is evaluated as MWSEP_PLAIN_F64.  The
+     * log-likelihood is the plain form's.  Single-wedge evaluations and
+     * batches, engine requests (each wedge's requests as one batch) and the
+     * gradient/Hessian calls; the server and the engine autotuner take the
      * other two forms. */
     MWSEP_PLAIN_DF = 2
 };

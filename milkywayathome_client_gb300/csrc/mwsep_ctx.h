@@ -205,6 +205,8 @@ void default_tune(mwsep_ctx* c, Wedge& w);
 /* One evaluation (or a batch) of wedge 0 through the grid-stride kernels;
  * leaves the integrals in c->d_out after the area block. */
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out);
+/* The same for any resident wedge (wedge 0 is the one set_problem fills). */
+int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out);
 
 } // namespace mwsep
 

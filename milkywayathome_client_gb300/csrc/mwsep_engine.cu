@@ -403,6 +403,48 @@ int check_requests(mwsep_ctx* c, int n, const mwsep_request* reqs)
     return MWSEP_OK;
 }
 
+/* The double-float form: requests grouped by wedge, each group one batch
+ * through the single-wedge path (its warp-tile kernel takes a batch of
+ * parameter vectors as blockIdx.y); the timings are the groups' sums. */
+int evaluate_requests_df(mwsep_ctx* c, int n, const mwsep_request* reqs, mwsep_result* out)
+{
+    std::vector<char> done((size_t)n, 0);
+    std::vector<int> idx;
+    std::vector<double> th;
+    std::vector<mwsep_result> res;
+    double ms[5] = {};
+    int launches = 0;
+    for (int i = 0; i < n; ++i)
+    {
+        if (done[(size_t)i]) continue;
+        const int wid = reqs[i].wedge;
+        const int P = c->wedges[wid]->prob.n_theta;
+        idx.clear();
+        th.clear();
+        for (int j = i; j < n; ++j)
+            if (!done[(size_t)j] && reqs[j].wedge == wid)
+            {
+                done[(size_t)j] = 1;
+                idx.push_back(j);
+                th.insert(th.end(), reqs[j].theta, reqs[j].theta + P);
+            }
+        res.resize(idx.size());
+        for (size_t b = 0; b < idx.size(); b += 65535)
+        {
+            const int m = (int)std::min<size_t>(65535, idx.size() - b);
+            const double* tp = P > 0 ? th.data() + b * (size_t)P : reqs[i].theta;
+            const int rc = mwsep::evaluate_wedge(c, wid, m, tp, MWSEP_PLAIN_DF, res.data() + b);
+            if (rc) return rc;
+            for (int k = 0; k < 5; ++k) ms[k] += c->last_ms[k];
+            launches += c->last_launches;
+        }
+        for (size_t k = 0; k < idx.size(); ++k) out[idx[k]] = res[k];
+    }
+    for (int k = 0; k < 5; ++k) c->last_ms[k] = ms[k];
+    c->last_launches = launches;
+    return MWSEP_OK;
+}
+
 /* Estimated device bytes of a wedge before building it. */
 size_t wedge_bytes_estimate(const ASTRONOMY_PARAMETERS* ap, const STAR_POINTS* sp)
 {
@@ -482,11 +524,12 @@ extern "C" int mwsep_ctx_evaluate_requests(mwsep_ctx* c, int n, const mwsep_requ
                                            mwsep_result* out)
 {
     if (!c || !out) return mwsep_fail(MWSEP_ERR_ARG);
-    if (precision == MWSEP_PLAIN_DF) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
-    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
+        return mwsep_fail(MWSEP_ERR_ARG);
     int rc = check_requests(c, n, reqs);
     if (rc) return mwsep_fail(rc);
     CU(cudaSetDevice(c->device));
+    if (precision == MWSEP_PLAIN_DF) return evaluate_requests_df(c, n, reqs, out);
     rc = ensure_descriptors(c);
     if (rc) return rc;
     BatchShape shape;

@@ -771,10 +771,15 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
 
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out)
 {
+    return evaluate_wedge(c, 0, B, thetas, precision, out);
+}
+
+int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out)
+{
     mwsep::Range nvtx_range("mwsep.evaluate");
-    if (c->wedges.empty() || !c->wedges[0]->has_problem || !c->wedges[0]->has_stars)
+    if (wid < 0 || wid >= (int)c->wedges.size() || !c->wedges[wid]->has_problem || !c->wedges[wid]->has_stars)
         return mwsep_fail(MWSEP_ERR_STATE);
-    Wedge& w = *c->wedges[0];
+    Wedge& w = *c->wedges[wid];
     if (B < 1 || B > 65535 || !thetas || !out) return mwsep_fail(MWSEP_ERR_ARG);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
         return mwsep_fail(MWSEP_ERR_ARG);

@@ -60,8 +60,8 @@ int evaluate_points(mwsep_ctx* ctx, int wedge, int P, const std::vector<double>&
 int check_inputs(mwsep_ctx* ctx, int wedge, const double* theta, const double* step, int precision, int& P)
 {
     if (!ctx || !theta || !step) return MWSEP_ERR_ARG;
-    if (precision == MWSEP_PLAIN_DF) return MWSEP_ERR_UNSUPPORTED;
-    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return MWSEP_ERR_ARG;
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
+        return MWSEP_ERR_ARG;
     P = mwsep_ctx_wedge_theta_count(ctx, wedge);
     if (P < 1) return MWSEP_ERR_ARG;
     for (int i = 0; i < P; ++i)

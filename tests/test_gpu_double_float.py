@@ -80,10 +80,52 @@ def test_double_float_limits(gpu_ctx):
         assert a.integrals == b.integrals and a.likelihood == b.likelihood
     pf, sf, g = load_case("basic_1stream")
     with mw.Context(0) as ctx:
-        w = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
+        ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
         with pytest.raises(mw.MwsepError) as e:
-            ctx.evaluate_requests([(w, g["theta"])], mw.MWSEP_PLAIN_DF)
+            ctx.autotune(0, mw.MWSEP_PLAIN_DF)
         assert e.value.status == N.MWSEP_ERR_UNSUPPORTED
+
+
+def test_double_float_engine_requests():
+    """Engine requests in the double-float form over three wedges, in mixed
+    order: each result equals the single-wedge evaluation of its wedge bit
+    for bit, and stays within the plain form's tolerance of the reference."""
+    import milkywayathome_client_gb300 as mw
+    names = ["basic_1stream", "three_streams", "four_streams_c120"]
+    cases = [load_case(n) for n in names]
+    with mw.Context(0) as ctx:
+        ids = [ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf)) for pf, sf, _ in cases]
+        reqs = []
+        for k in range(3):
+            for wid, (_, _, g) in zip(ids, cases):
+                reqs.append((wid, np.asarray(g["theta"]) * (1 + 1e-3 * k)))
+        reqs = reqs[::-1]
+        res = ctx.evaluate_requests(reqs, mw.MWSEP_PLAIN_DF)
+    for (wid, th), r in zip(reqs, res):
+        pf, sf, g = cases[ids.index(wid)]
+        with mw.Context(0) as one:
+            one.set_problem(mw.AstronomyParameters.read(pf))
+            one.set_stars(mw.StarPoints.read(sf))
+            s = one.evaluate(th, mw.MWSEP_PLAIN_DF)
+        assert r.integrals == s.integrals and r.likelihood == s.likelihood
+        if np.array_equal(th, np.asarray(g["theta"])):
+            assert _close_rel(r.background_integral, g["background_integral"], REL)
+            assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
+
+
+def test_double_float_gradient_matches_plain(gpu_ctx):
+    """Central-difference gradient in the double-float form against the same
+    in native FP64: each evaluation agrees to ~1e-14, so the differences
+    agree to ~1e-14 / step."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case("three_streams")
+    with mw.Context(0) as ctx:
+        wid = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
+        step = np.full(len(g["theta"]), 1e-3)
+        f0a, ga = ctx.gradient(wid, g["theta"], step, mw.MWSEP_PLAIN_F64)
+        f0b, gb = ctx.gradient(wid, g["theta"], step, mw.MWSEP_PLAIN_DF)
+    assert abs(f0a - f0b) <= ABS_LOGL
+    np.testing.assert_allclose(gb, ga, rtol=0, atol=1e-12 / 1e-3)
 
 
 @pytest.mark.parametrize("mu,sigma", [(200.0, 1.0), (250.0, 0.5), (300.0, 1.0), (340.0, 0.5)])
