@@ -430,6 +430,10 @@ def population_batch(args):
         launches = ctx.last_launches()
         plain = ctx.evaluate_requests(reqs[:4], mw.MWSEP_PLAIN_F64)
         plain_ms = ctx.last_timings()["total_ms"]
+        # the plain form's accuracy in double-float: the whole population, one batch
+        ctx.evaluate_requests(reqs[:8], mw.MWSEP_PLAIN_DF)
+        dfres = ctx.evaluate_requests(reqs, mw.MWSEP_PLAIN_DF)
+        df_ms = ctx.last_timings()["total_ms"]
         # the errors() consumer: a finite-difference Hessian (2P^2+1 points) as engine batches
         step = mw.AstronomyParameters.read(f["params"]).step()
         P = len(step)
@@ -442,6 +446,9 @@ def population_batch(args):
             "launches_per_batch": launches, "graph": True,
             "plain_f64_evals_per_s": 4 / (plain_ms * 1e-3),
             "max_dlogL_mixed_vs_plain": max(abs(a.likelihood - b.likelihood) for a, b in zip(res[:4], plain)),
+            "double_float_evals_per_s": len(reqs) / (df_ms * 1e-3),
+            "max_dlogL_double_float_vs_plain": max(abs(a.likelihood - b.likelihood)
+                                                   for a, b in zip(dfres[:4], plain)),
             "hessian": {"parameters": P, "evaluations": 2 * P * P + 1, "seconds": hess_s,
                         "evals_per_s": (2 * P * P + 1) / hess_s, "precision": "mixed"}}
 

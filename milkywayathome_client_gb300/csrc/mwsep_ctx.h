@@ -134,6 +134,10 @@ struct Wedge
     bool has_stars = false;
     int n_stars = 0;
     DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_pts;
+    /* double-float star table, built on the first double-float likelihood
+     * of this catalogue */
+    DevBuf s_ptsdf;
+    bool has_star_df = false;
     mwsep_stars_dev stars_view{};
     HostPinned h_stars;
 

@@ -278,6 +278,137 @@ cudaError_t occupancy(int* b)
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_df_kernel<S>, kBlock, 0);
 }
 
+/* Per-star double-float table [C][N]: {r_hi, r_lo, qw_hi, qw_lo}. */
+__global__ void star_df_table_kernel(long long total, const double* __restrict__ r_point,
+                                     const double* __restrict__ qw, float4* __restrict__ out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x)
+    {
+        const df r = D::from_double(r_point[i]), q = D::from_double(qw[i]);
+        out[i] = make_float4(r.hi, r.lo, q.hi, q.lo);
+    }
+}
+
+/* calculate_likelihood for one star per thread (cpu/evaluation_optimized.c:
+ * 665-717) with the convolution in double-float: the star's completed-square
+ * constants in FP64 (as the integral's columns), each stream's exponent
+ * shifted by floor of its largest value over the star's points (the point
+ * nearest the stream's closest approach, found in FP32), the points' terms
+ * summed in runs of eight, and the mixture weights and log10 sums in FP64
+ * (likelihood_finish, shared with the FP64 kernel). */
+template <int S>
+__global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_dev St, const float4* __restrict__ pdf,
+                                                            const mwsep_theta_consts* __restrict__ thetas,
+                                                            const double* __restrict__ integrals,
+                                                            double2* __restrict__ partials, long long theta_stride)
+{
+    constexpr int SP = kSP(S);
+    __shared__ mwsep_theta_consts th;
+    __shared__ double red[2 * (3 + SP) * 32];
+    __shared__ float2 tab[D::kExp2Table];
+    mwsep::f64::load_theta(th, thetas + blockIdx.y);
+    for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x) tab[j] = c_exp2_tab[j];
+    __syncthreads();
+    const double* I = integrals + (size_t)blockIdx.y * (1 + th.n_streams);
+    mwsep::comp_sum acc[3 + SP];
+#pragma unroll
+    for (int k = 0; k < 3 + SP; ++k) acc[k].zero();
+    constexpr double kLog2e = 1.4426950408889634073599246810018921;
+    const int N = St.n_stars, C = St.convolve;
+    const df r0 = D::from_double(th.r0);
+    for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
+    {
+        const double* g = St.geom + 4 * (size_t)s0;
+        mwsep::f64::ColF64<SP> cc;
+        mwsep::f64::column_consts_f64<SP>(g[0], g[1], g[2], g[3], th, cc);
+        const df B2 = D::from_double(cc.B2), nrb = D::from_double(-cc.rb), Db = D::from_double(cc.Db);
+        df nrs[SP], k2[SP], k0[SP];
+        double scale[SP];
+        float rsf[SP], umin[SP];
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            rsf[s] = (float)cc.rs[s];
+            umin[s] = 3.0e38f;
+        }
+        if constexpr (S > 0)
+        {
+            for (int n = 0; n < C; ++n)
+            {
+                const float rh = pdf[(size_t)MWSEP_IDX((size_t)n * N + s0, (size_t)C * N, 8)].x;
+#pragma unroll
+                for (int s = 0; s < S; ++s) umin[s] = fminf(umin[s], fabsf(__fsub_rn(rh, rsf[s])));
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            const bool on = s < th.n_streams && th.stream_on[s];
+            const double k2b = on ? cc.k2[s] * kLog2e : 0.0, k0b = cc.k0[s] * kLog2e;
+            const double um = (double)umin[s];
+            const int eref = on ? (int)floor(fmax(k2b * um * um + k0b, -1100.0)) : -1100;
+            nrs[s] = D::from_double(-cc.rs[s]);
+            k2[s] = D::from_double(k2b);
+            k0[s] = D::from_double(on ? fmax(k0b - (double)eref, -1.0e30) : -1.0e30);
+            scale[s] = eref > -1100 ? ldexp(1.0, eref) : 0.0;
+        }
+        df bg = D::mk(0.f, 0.f), st[SP];
+#pragma unroll
+        for (int s = 0; s < S; ++s) st[s] = D::mk(0.f, 0.f);
+        for (int n0 = 0; n0 < C; n0 += 8)
+        {
+            D::lazy_sum pb = {0.f, 0.f}, ps[SP];
+#pragma unroll
+            for (int s = 0; s < S; ++s) ps[s] = {0.f, 0.f};
+            const int n1 = min(n0 + 8, C);
+#pragma unroll 1
+            for (int n = n0; n < n1; ++n)
+            {
+                const float4 v = pdf[(size_t)MWSEP_IDX((size_t)n * N + s0, (size_t)C * N, 8)];
+                const df r = D::mk(v.x, v.y), w = D::mk(v.z, v.w);
+                const df t = D::add_fast(r, nrb);
+                const df rg = D::sqrt(D::add_fast(D::mul(B2, D::sqr(t)), Db));
+                const df sum = D::add_fast(rg, r0);
+                D::lazy_add(pb, D::div(w, D::mul(rg, D::mul(sum, D::sqr(sum)))));
+#pragma unroll
+                for (int s = 0; s < S; ++s)
+                {
+                    const df u = D::add_fast(r, nrs[s]);
+                    const df a = D::add_fast(D::mul(k2[s], D::sqr(u)), k0[s]);
+                    D::lazy_add(ps[s], D::mul_raw(w, D::exp2(a, tab)));
+                }
+            }
+            bg = D::add_fast(bg, D::lazy_end(pb));
+#pragma unroll
+            for (int s = 0; s < S; ++s) st[s] = D::add_fast(st[s], D::lazy_end(ps[s]));
+        }
+        double stv[SP];
+        stv[0] = 0.0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) stv[s] = ((double)st[s].hi + (double)st[s].lo) * scale[s];
+        mwsep::f64::likelihood_finish<SP>(th, I, St.reff[s0], (double)bg.hi + (double)bg.lo, stv, acc);
+    }
+    mwsep::block_reduce<3 + SP>(acc, red);
+    if (threadIdx.x == 0)
+    {
+        double2* out = partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + th.n_streams);
+#pragma unroll
+        for (int k = 0; k < 3 + SP; ++k)
+            if (k < 3 + th.n_streams) out[k] = make_double2(acc[k].s, acc[k].c);
+    }
+}
+
+template <int S>
+int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_theta_consts* th,
+                      const mwsep_launch_shape* sh, const double* integrals, double2* partials, cudaStream_t st)
+{
+    const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
+    dim3 g(sh->grid, sh->n_theta);
+    likelihood_df_kernel<S><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
+    return (int)cudaGetLastError();
+}
+
 bool g_table_ready[64] = {};
 
 } // namespace
@@ -329,6 +460,34 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
     case 2: return launch<2>(area, th_dev, sh, partials, st);
     case 3: return launch<3>(area, th_dev, sh, partials, st);
     case 4: return launch<4>(area, th_dev, sh, partials, st);
+    default: return (int)cudaErrorInvalidValue; /* 5..8 streams run in native FP64 */
+    }
+}
+
+extern "C" int mwsep_launch_star_df_table(int n, int convolve, const double* r_point, const double* qw,
+                                         float4* out, void* stream)
+{
+    const long long total = (long long)n * convolve;
+    if (total <= 0) return 0;
+    long long grid = (total + 255) / 256;
+    if (grid > 152 * 16) grid = 152 * 16;
+    star_df_table_kernel<<<(int)grid, 256, 0, (cudaStream_t)stream>>>(total, r_point, qw, out);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mwsep_launch_likelihood_df(const mwsep_stars_dev* stars, const float4* star_df,
+                                          const mwsep_theta_consts* th_dev, const mwsep_launch_shape* sh,
+                                          const double* integrals, double2* partials, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (sh->block > 256) return (int)cudaErrorInvalidValue;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_likelihood<0>(stars, star_df, th_dev, sh, integrals, partials, st);
+    case 1: return launch_likelihood<1>(stars, star_df, th_dev, sh, integrals, partials, st);
+    case 2: return launch_likelihood<2>(stars, star_df, th_dev, sh, integrals, partials, st);
+    case 3: return launch_likelihood<3>(stars, star_df, th_dev, sh, integrals, partials, st);
+    case 4: return launch_likelihood<4>(stars, star_df, th_dev, sh, integrals, partials, st);
     default: return (int)cudaErrorInvalidValue; /* 5..8 streams run in native FP64 */
     }
 }

@@ -230,20 +230,33 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     }
 }
 
+template <int SMAX>
+__device__ __forceinline__ void likelihood_finish(const mwsep_theta_consts& th, const double* I, double rf,
+                                                  double bg, const double (&st)[SMAX], comp_sum (&acc)[3 + SMAX]);
+
 /* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717).
  * acc slots: [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
 template <int SMAX>
 __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
                                                 const double* I, int s0, comp_sum (&acc)[3 + SMAX])
 {
-    const int S = th.n_streams;
     const int N = St.n_stars;
     s0 = (int)MWSEP_IDX(s0, N, 7);
     const double* g = St.geom + 4 * (size_t)s0;
     double bg, st[SMAX];
     convolve_f64<SMAX>(St.r_point + s0, St.qw + s0, St.r_in_mag + s0, St.r_in_mag2 + s0, (size_t)N, St.convolve,
                        g[0], g[1], g[2], g[3], th, bg, st);
-    const double rf = St.reff[s0];
+    likelihood_finish<SMAX>(th, I, St.reff[s0], bg, st, acc);
+}
+
+/* The rest of calculate_likelihood for one star from its convolved bg and
+ * st[] before the reff_xr_rp3 factor rf (cpu/evaluation_optimized.c:679-716):
+ * the mixture weights, the -238 sentinel and the log10 sums. */
+template <int SMAX>
+__device__ __forceinline__ void likelihood_finish(const mwsep_theta_consts& th, const double* I, double rf,
+                                                  double bg, const double (&st)[SMAX], comp_sum (&acc)[3 + SMAX])
+{
+    const int S = th.n_streams;
     if (th.bg_mode != 2) bg *= rf;
 
     double bg_only = (bg / I[0]) * th.exp_bg_weight;

@@ -645,6 +645,7 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     v.r = w.s_r.as<double>();
     w.n_stars = n;
     w.has_stars = true;
+    w.has_star_df = false; /* rebuilt from these tables when first needed */
     for (int prec = 0; prec < 3; ++prec)
         w.tune[prec].lk_grid = occupancy_grid(c, w.tune[prec].lk_block, n);
     return MWSEP_OK;
@@ -762,8 +763,9 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
         for (DevBuf* b : bufs) b->release(t);
     }
     DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.d_nfac, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
-                      &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts};
+                      &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts, &w.s_ptsdf};
     for (DevBuf* b : bufs) b->release(t);
+    w.has_star_df = false;
     w.h_stars.release();
     w.bytes = 0;
     w.has_problem = w.has_stars = false;
@@ -809,6 +811,15 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     rc |= c->d_out.ensure(out_doubles * 8, tot);
     rc |= c->h_out.ensure(out_doubles * 8);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
+    if (precision == MWSEP_PLAIN_DF && !w.has_star_df)
+    {
+        const size_t before = tot;
+        if (w.s_ptsdf.ensure((size_t)w.n_stars * p.convolve * sizeof(float4), tot)) return mwsep_fail(MWSEP_ERR_NOMEM);
+        w.bytes += tot - before;
+        CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
+                                      w.s_ptsdf.as<float4>(), c->stream));
+        w.has_star_df = true;
+    }
 
     double* d_areas = c->d_out.as<double>();
     double* d_ints = d_areas + (size_t)B * A * ncomp;
@@ -867,7 +878,10 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     lk.block = t.lk_block;
     lk.grid = t.lk_grid;
     lk.area_index = 0;
-    if (precision != MWSEP_MIXED_F32) /* plain and double-float: the FP64 likelihood */
+    if (precision == MWSEP_PLAIN_DF)
+        CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
+                                      &lk, d_ints, c->d_lkpartials.as<double2>(), st));
+    else if (precision == MWSEP_PLAIN_F64)
         CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
     else

@@ -249,6 +249,14 @@ int mwsep_df_prepare(int device);
 int mwsep_integral_df_blocks_per_sm(int n_streams);
 int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                              const mwsep_launch_shape* sh, double2* partials, void* stream);
+/* Per-star double-float table [C][N] {r_hi, r_lo, qw_hi, qw_lo} from the
+ * FP64 tables, and the likelihood over it (same partial layout as the FP64
+ * likelihood; block <= 256, up to 4 streams). */
+int mwsep_launch_star_df_table(int n, int convolve, const double* r_point, const double* qw, float4* out,
+                               void* stream);
+int mwsep_launch_likelihood_df(const mwsep_stars_dev* stars, const float4* star_df,
+                               const mwsep_theta_consts* th_dev, const mwsep_launch_shape* sh,
+                               const double* integrals, double2* partials, void* stream);
 int mwsep_integral_f64_blocks_per_sm(int n_streams, int block);
 /* Reduce per-block compensated partials of every area into area integrals
  * and subtract the cut areas (cpu/evaluation_optimized.c:584-593):
