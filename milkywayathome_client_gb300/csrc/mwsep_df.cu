@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "milkyway_separation_gb300.h"
 #include "mwsep_checks.cuh"
 #include "mwsep_df.cuh"
 #include "mwsep_f64_point.cuh"
@@ -409,6 +410,31 @@ int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_
     return (int)cudaGetLastError();
 }
 
+/* Element-wise evaluation of the double-float primitives for the tests:
+ * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker); inputs are
+ * doubles split into pairs, results returned as hi + lo in FP64. */
+__global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, const double* __restrict__ y,
+                               double* __restrict__ out)
+{
+    __shared__ float2 tab[D::kExp2Table];
+    for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x) tab[j] = c_exp2_tab[j];
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const df a = D::from_double(x[i]), b = D::from_double(y[i]);
+        df r;
+        switch (op)
+        {
+        case 0: r = D::exp2(a, tab); break;
+        case 1: r = D::sqrt(a); break;
+        case 2: r = D::div(a, b); break;
+        case 3: r = D::mul(a, b); break;
+        default: r = D::add_fast(a, b); break;
+        }
+        out[i] = (double)r.hi + (double)r.lo;
+    }
+}
+
 bool g_table_ready[64] = {};
 
 } // namespace
@@ -462,6 +488,33 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
     case 4: return launch<4>(area, th_dev, sh, partials, st);
     default: return (int)cudaErrorInvalidValue; /* 5..8 streams run in native FP64 */
     }
+}
+
+/* Diagnostics entry (declared in the public header): host arrays in and
+ * out, synchronous, on the default stream of `device`. */
+extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, double* out)
+{
+    if (op < 0 || op > 4 || n < 0 || (n > 0 && (!x || !y || !out))) return MWSEP_ERR_ARG;
+    if (n == 0) return MWSEP_OK;
+    if (cudaSetDevice(device) != cudaSuccess || mwsep_df_prepare(device)) return MWSEP_ERR_CUDA;
+    const size_t bytes = (size_t)n * sizeof(double);
+    double* d = nullptr;
+    if (cudaMalloc(&d, 3 * bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return MWSEP_ERR_NOMEM;
+    }
+    cudaError_t e = cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, y, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+    {
+        const int grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+        df_eval_kernel<<<grid, 256>>>(op, n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? MWSEP_OK : MWSEP_ERR_CUDA;
 }
 
 extern "C" int mwsep_launch_star_df_table(int n, int convolve, const double* r_point, const double* qw,

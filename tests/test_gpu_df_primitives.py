@@ -1,0 +1,88 @@
+"""GPU: error bounds of the double-float primitives behind MWSEP_PLAIN_DF
+(exp2 by a 2^(j/1024) table and one FP32 correction, sqrt and the quotient
+by one Newton step from the SFU approximations, Dekker's add and the FMA
+product), against numpy's FP64 results for the same split inputs.  Measured
+maxima on GB300: exp2 1.9e-14, sqrt 1.5e-14, quotient 2.4e-14, product
+1.2e-14, sum 8e-15 of |x| + |y|; the bounds below are 2^-45 (2.8e-14) and
+2^-46 (1.4e-14)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EXP2, SQRT, DIV, MUL, ADD = range(5)
+
+
+def _split(x):
+    """The pair a double becomes on the device, as its exact double value."""
+    hi = np.asarray(x, dtype=np.float64).astype(np.float32)
+    lo = (np.asarray(x, dtype=np.float64) - hi.astype(np.float64)).astype(np.float32)
+    return hi.astype(np.float64) + lo.astype(np.float64)
+
+
+def _eval(op, x, y=None):
+    from milkywayathome_client_gb300 import native as N
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
+    out = np.zeros_like(x)
+    P = C.POINTER(C.c_double)
+    rc = N.lib().mwsep_df_eval(0, op, x.size, x.ctypes.data_as(P), y.ctypes.data_as(P), out.ctypes.data_as(P))
+    assert rc == 0, rc
+    return out
+
+
+@pytest.fixture(scope="module")
+def rng(built_library):
+    return np.random.default_rng(20261203)
+
+
+def test_exp2(rng):
+    x = np.concatenate([rng.uniform(-100.0, 2.0, 200000), rng.uniform(-1e-3, 1e-3, 20000),
+                        np.arange(-100, 3, dtype=np.float64),
+                        np.arange(-2048, 2049) / 1024.0,                    # table knots
+                        (np.arange(-2048, 2048) + 0.5) / 1024.0])           # rounding ties
+    got = _eval(EXP2, x)
+    want = np.exp2(_split(x))
+    rel = np.abs(got - want) / want
+    assert rel.max() <= 2.0 ** -45, rel.max()
+    # the bottom of FP32 range: the low part turns subnormal, a few bits go
+    deep = rng.uniform(-126.0, -100.0, 20000)
+    rel = np.abs(_eval(EXP2, deep) - np.exp2(_split(deep))) / np.exp2(_split(deep))
+    assert rel.max() <= 2.0 ** -20, rel.max()
+    # below range: exactly 0; NaN propagates
+    below = np.array([-126.5, -127.0, -150.0, -1e6, -1e30, -np.inf])
+    assert np.all(_eval(EXP2, below) == 0.0)
+    assert np.isnan(_eval(EXP2, np.array([np.nan]))).all()
+
+
+def test_sqrt(rng):
+    x = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), 200000))
+    got = _eval(SQRT, x)
+    want = np.sqrt(_split(x))
+    err = (np.abs(got - want) / want).max()
+    assert err <= 2.0 ** -45, err
+
+
+def test_quotient(rng):
+    x = np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 200000))
+    y = np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 200000))
+    got = _eval(DIV, x, y)
+    want = _split(x) / _split(y)
+    err = (np.abs(got - want) / want).max()
+    assert err <= 2.0 ** -45, err
+    assert np.all(_eval(DIV, np.zeros(4), np.array([1.0, 2.0, 1e-9, 1e9])) == 0.0)
+
+
+def test_product_and_sum(rng):
+    x = rng.uniform(-100.0, 100.0, 200000)
+    y = rng.uniform(-100.0, 100.0, 200000)
+    xs, ys = _split(x), _split(y)
+    got = _eval(MUL, x, y)
+    err = (np.abs(got - xs * ys) / np.abs(xs * ys)).max()
+    assert err <= 2.0 ** -46, err
+    # Dekker's add: 2^-48-ish of |x| + |y| (not of the sum, under cancellation)
+    got = _eval(ADD, x, y)
+    err = np.abs(got - (xs + ys)) / (np.abs(xs) + np.abs(ys))
+    assert err.max() <= 2.0 ** -46, err.max()
