@@ -22,8 +22,9 @@
  * Per lane the group sums are double-float; per group they go to FP64
  * (times ids), across blocks the usual compensated FP64 reduction.
  *
- * Background forms: alpha = delta = 1 without the aux profile, up to 4
- * streams; the host runs any other problem through the native FP64 kernel.
+ * Background forms: alpha = delta = 1, with or without the aux profile
+ * (whose column-independent share aux_area_kernel adds), up to 4 streams;
+ * the host runs any other problem through the native FP64 kernel.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -384,11 +385,23 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
 #pragma unroll
             for (int s = 0; s < S; ++s) st[s] = D::add_fast(st[s], D::lazy_end(ps[s]));
         }
+        /* the aux profile, point by point in FP64 as the reference adds it */
+        double bgd = (double)bg.hi + (double)bg.lo;
+        if (th.aux && th.bg_mode == 0)
+        {
+            double v = 0.0;
+            for (int n = 0; n < C; ++n)
+            {
+                const size_t o = (size_t)MWSEP_IDX((size_t)n * N + s0, (size_t)C * N, 8);
+                v += St.qw[o] * (th.bg_a * St.r_in_mag2[o] + th.bg_b * St.r_in_mag[o] + th.bg_c);
+            }
+            bgd += v;
+        }
         double stv[SP];
         stv[0] = 0.0;
 #pragma unroll
         for (int s = 0; s < S; ++s) stv[s] = ((double)st[s].hi + (double)st[s].lo) * scale[s];
-        mwsep::f64::likelihood_finish<SP>(th, I, St.reff[s0], (double)bg.hi + (double)bg.lo, stv, acc);
+        mwsep::f64::likelihood_finish<SP>(th, I, St.reff[s0], bgd, stv, acc);
     }
     mwsep::block_reduce<3 + SP>(acc, red);
     if (threadIdx.x == 0)
@@ -408,6 +421,47 @@ int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_
     dim3 g(sh->grid, sh->n_theta);
     likelihood_df_kernel<S><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
     return (int)cudaGetLastError();
+}
+
+/* The aux profile's share of an area integral (form-1 problems: alpha =
+ * delta = 1 plus qw (a g^2 + b g + c), cpu/evaluation_optimized.c:234-239).
+ * That term does not depend on the column, so summed over the area's cells
+ * as :498-520 does (times reff, times V = irv_k ids_j) it is
+ *   mu_steps * sum_j ids_j * sum_k irv_k reff_k sum_n qw_kn (a g2_kn + b g_kn + c),
+ * O(R C) work in FP64, added (TwoSum) to block 0's background partial of
+ * the area after the double-float kernel has written it.  One block per
+ * theta; thetas without the aux profile are left alone. */
+__global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts* __restrict__ thetas,
+                                double2* __restrict__ partials, long long theta_stride)
+{
+    __shared__ double red[2 * 2 * 32];
+    const mwsep_theta_consts* th = thetas + blockIdx.y;
+    if (!th->aux || th->bg_mode != 0) return; /* uniform per block */
+    const double a = th->bg_a, b = th->bg_b, c = th->bg_c;
+    mwsep::comp_sum acc[2];
+    acc[0].zero();
+    acc[1].zero();
+    const int C = A.convolve;
+    for (int k = threadIdx.x; k < A.r_steps; k += blockDim.x)
+    {
+        const size_t row = (size_t)k * C;
+        double v = 0.0;
+        for (int n = 0; n < C; ++n)
+            v += A.qw[row + n] * (a * A.r_in_mag2[row + n] + b * A.r_in_mag[row + n] + c);
+        acc[0].add(v * A.reff[k] * A.irv[k]);
+    }
+    for (int j = threadIdx.x; j < A.nu_steps; j += blockDim.x) acc[1].add(A.ids[j]);
+    mwsep::block_reduce<2>(acc, red);
+    if (threadIdx.x == 0)
+    {
+        const double v = (acc[0].s + acc[0].c) * (acc[1].s + acc[1].c) * (double)A.mu_steps;
+        double2* p = partials + (size_t)blockIdx.y * theta_stride;
+        const double s = p->x + v;
+        const double bb = s - p->x;
+        const double e = (p->x - (s - bb)) + (v - bb);
+        p->x = s;
+        p->y += e;
+    }
 }
 
 /* Element-wise evaluation of the double-float primitives for the tests:
@@ -515,6 +569,16 @@ extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const d
     if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
     cudaFree(d);
     return e == cudaSuccess ? MWSEP_OK : MWSEP_ERR_CUDA;
+}
+
+extern "C" int mwsep_launch_aux_area_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                        const mwsep_launch_shape* sh, double2* partials, void* stream)
+{
+    const long long ncomp = 1 + sh->n_streams;
+    const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
+    double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
+    aux_area_kernel<<<dim3(1, sh->n_theta), 256, 0, (cudaStream_t)stream>>>(*area, th_dev, base, theta_stride);
+    return (int)cudaGetLastError();
 }
 
 extern "C" int mwsep_launch_star_df_table(int n, int convolve, const double* r_point, const double* qw,

@@ -794,11 +794,17 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     if (c->h_theta.ensure(th_bytes)) return mwsep_fail(MWSEP_ERR_NOMEM);
     mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
     for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
-    /* the double-float integral covers the alpha = delta = 1, no-aux
-     * background with up to 4 streams; anything else runs in native FP64 */
+    /* the double-float integral covers the alpha = delta = 1 background,
+     * with or without the aux profile, and up to 4 streams; anything else
+     * runs in native FP64 */
+    bool df_aux = false;
     if (precision == MWSEP_PLAIN_DF)
         for (int i = 0; i < B; ++i)
-            if (mwsep_bg_form(&hth[i]) != 0 || S > 4) precision = MWSEP_PLAIN_F64;
+        {
+            const int form = mwsep_bg_form(&hth[i]);
+            if (form > 1 || S > 4) precision = MWSEP_PLAIN_F64;
+            df_aux = df_aux || form == 1;
+        }
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
     const Tune& t = w.tune[precision];
     const size_t part_bytes = sizeof(double2) * (size_t)B * A * t.grid * ncomp;
@@ -857,6 +863,12 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
             CK(mwsep_launch_integral_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
                                         c->d_partials.as<double2>(), st));
             ++launches;
+            if (df_aux)
+            {
+                CK(mwsep_launch_aux_area_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                            c->d_partials.as<double2>(), st));
+                ++launches;
+            }
         }
         else
         {

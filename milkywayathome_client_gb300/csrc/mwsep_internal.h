@@ -249,6 +249,11 @@ int mwsep_df_prepare(int device);
 int mwsep_integral_df_blocks_per_sm(int n_streams);
 int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                              const mwsep_launch_shape* sh, double2* partials, void* stream);
+/* Adds the aux profile's column-independent share of an area integral to
+ * the double-float partials of the thetas that have it (after
+ * mwsep_launch_integral_df for that area, same shape). */
+int mwsep_launch_aux_area_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                             const mwsep_launch_shape* sh, double2* partials, void* stream);
 /* Per-star double-float table [C][N] {r_hi, r_lo, qw_hi, qw_lo} from the
  * FP64 tables, and the likelihood over it (same partial layout as the FP64
  * likelihood; block <= 256, up to 4 streams). */

@@ -1,8 +1,9 @@
 """GPU: the double-float form (MWSEP_PLAIN_DF) against the reference's own
 outputs at the plain form's tolerances (1e-12 relative on every integral,
-1e-12 absolute on the log-likelihood), against the native FP64 kernel at
-full size, batch == single, and its limits (other background forms and more
-than 4 streams run in native FP64; the engine refuses it)."""
+1e-12 absolute on the log-likelihood) -- every golden case, the aux profile
+included -- against the native FP64 kernel at full size, batch == single,
+engine requests and gradients, and its limits (general alpha/delta, q = 0
+and more than 4 streams run in native FP64; the autotuner refuses it)."""
 import math
 
 import numpy as np
@@ -73,7 +74,7 @@ def test_double_float_matches_native_fp64_at_full_size(gpu_ctx):
 def test_double_float_limits(gpu_ctx):
     import milkywayathome_client_gb300 as mw
     from milkywayathome_client_gb300 import native as N
-    for name in ("aux_profile", "six_streams"):  # run in native FP64: identical bits
+    for name in ("general_alpha_delta", "six_streams"):  # run in native FP64: identical bits
         g = _setup(gpu_ctx, name)
         a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
         b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
