@@ -819,8 +819,9 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
     if (precision == MWSEP_PLAIN_DF && !w.has_star_df)
     {
-        const size_t before = tot;
-        if (w.s_ptsdf.ensure((size_t)w.n_stars * p.convolve * sizeof(float4), tot)) return mwsep_fail(MWSEP_ERR_NOMEM);
+        const size_t before = tot, need = (size_t)w.n_stars * p.convolve * sizeof(float4);
+        if (c->hbm_budget && tot + need > c->hbm_budget) return mwsep_fail(MWSEP_ERR_BUDGET);
+        if (w.s_ptsdf.ensure(need, tot)) return mwsep_fail(MWSEP_ERR_NOMEM);
         w.bytes += tot - before;
         CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
                                       w.s_ptsdf.as<float4>(), c->stream));

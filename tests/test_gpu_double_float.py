@@ -150,3 +150,30 @@ def test_double_float_far_stream(gpu_ctx, mu, sigma):
             assert abs(x) <= 1e-270, (x, y)
     if not (math.isnan(a.likelihood) or math.isinf(a.likelihood)):
         assert abs(a.likelihood - b.likelihood) <= ABS_LOGL, (a.likelihood, b.likelihood)
+
+
+def test_double_float_star_table_respects_hbm_budget():
+    """The per-star pair table is built on the first double-float
+    evaluation; a context whose device-memory budget cannot hold it reports
+    MWSEP_ERR_BUDGET, keeps working in the other forms, and builds it once
+    the budget allows."""
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    pf, sf, g = load_case("three_streams")
+    sp = mw.StarPoints.read(sf)
+    with mw.Context(0) as ctx:
+        ctx.set_problem(mw.AstronomyParameters.read(pf))
+        ctx.set_stars(sp)
+        ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+        ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32)
+        ctx.set_hbm_budget(ctx.device_bytes() + 1024)
+        with pytest.raises(mw.MwsepError) as e:
+            ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+        assert e.value.status == N.MWSEP_ERR_BUDGET
+        r = ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+        assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
+        before = ctx.device_bytes()
+        ctx.set_hbm_budget(0)
+        r = ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+        assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
+        assert ctx.device_bytes() - before >= 16 * sp.to_array().shape[0] * 20  # convolve 20
