@@ -12,7 +12,8 @@
  * FP64 kernel) and the stream exponent is in base 2.  FP32 has an exponent
  * range of 2^+-126, so before each lane group the warp finds, in FP32, the
  * largest stream exponent over the group's points and the tile's columns
- * (a cheap pass: 4 operations per point, column and stream), and each column
+ * (a cheap pass: per column and stream the point nearest the stream's
+ * closest approach, 2 operations per point), and each column
  * writes its k0 shifted by floor of that maximum, formed in FP64.  The
  * group's largest term is then about 1 and its sums are scaled back in FP64,
  * so integrals far below FP32 range keep their FP64 magnitude; terms more
@@ -148,13 +149,12 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
 #pragma unroll
                 for (int s = 0; s < S; ++s)
                 {
+                    /* k2 <= 0: the largest exponent is at the point nearest rs */
                     const float rs = c[2 * (3 + 3 * s)], k2 = c[2 * (4 + 3 * s)], k0 = kf[j * S + s];
+                    float um = fabsf(__fsub_rn(r[0].hi, rs));
 #pragma unroll
-                    for (int i = 0; i < DFP; ++i)
-                    {
-                        const float u = __fsub_rn(r[i].hi, rs);
-                        mx[s] = fmaxf(mx[s], __fmaf_rn(k2, __fmul_rn(u, u), k0));
-                    }
+                    for (int i = 1; i < DFP; ++i) um = fminf(um, fabsf(__fsub_rn(r[i].hi, rs)));
+                    mx[s] = fmaxf(mx[s], __fmaf_rn(k2, __fmul_rn(um, um), k0));
                 }
             }
             int eref[S];
@@ -187,8 +187,7 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
 #pragma unroll
             for (int i = 0; i < DFP; ++i)
             {
-                const df t = D::add_fast(r[i], nrb);
-                const df rg = D::sqrt(D::add_fast(D::mul(B2, D::sqr(t)), Db));
+                const df rg = D::sqrt(D::sq_scale_add(B2, D::add_fast(r[i], nrb), Db));
                 const df sum = D::add_fast(rg, r0);
                 const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
                 const df q = D::div(w[i], den);
@@ -206,8 +205,7 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
 #pragma unroll
                 for (int i = 0; i < DFP; ++i)
                 {
-                    const df u = D::add_fast(r[i], nrs);
-                    const df a = D::add_fast(D::mul(k2, D::sqr(u)), k0);
+                    const df a = D::sq_scale_add(k2, D::add_fast(r[i], nrs), k0);
                     const df e = D::mul_raw(w[i], D::exp2(a, tab));
                     if (i == 0)
                         ps = D::lazy_start(e);
@@ -369,15 +367,13 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
             {
                 const float4 v = pdf[(size_t)MWSEP_IDX((size_t)n * N + s0, (size_t)C * N, 8)];
                 const df r = D::mk(v.x, v.y), w = D::mk(v.z, v.w);
-                const df t = D::add_fast(r, nrb);
-                const df rg = D::sqrt(D::add_fast(D::mul(B2, D::sqr(t)), Db));
+                const df rg = D::sqrt(D::sq_scale_add(B2, D::add_fast(r, nrb), Db));
                 const df sum = D::add_fast(rg, r0);
                 D::lazy_add(pb, D::div(w, D::mul(rg, D::mul(sum, D::sqr(sum)))));
 #pragma unroll
                 for (int s = 0; s < S; ++s)
                 {
-                    const df u = D::add_fast(r, nrs[s]);
-                    const df a = D::add_fast(D::mul(k2[s], D::sqr(u)), k0[s]);
+                    const df a = D::sq_scale_add(k2[s], D::add_fast(r, nrs[s]), k0[s]);
                     D::lazy_add(ps[s], D::mul_raw(w, D::exp2(a, tab)));
                 }
             }
@@ -465,10 +461,10 @@ __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts
 }
 
 /* Element-wise evaluation of the double-float primitives for the tests:
- * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker); inputs are
- * doubles split into pairs, results returned as hi + lo in FP64. */
+ * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker), 5 x y^2 + z;
+ * inputs are doubles split into pairs, results returned as hi + lo in FP64. */
 __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, const double* __restrict__ y,
-                               double* __restrict__ out)
+                               const double* __restrict__ z, double* __restrict__ out)
 {
     __shared__ float2 tab[D::kExp2Table];
     for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x) tab[j] = c_exp2_tab[j];
@@ -483,7 +479,8 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
         case 1: r = D::sqrt(a); break;
         case 2: r = D::div(a, b); break;
         case 3: r = D::mul(a, b); break;
-        default: r = D::add_fast(a, b); break;
+        case 4: r = D::add_fast(a, b); break;
+        default: r = D::sq_scale_add(a, b, D::from_double(z[i])); break;
         }
         out[i] = (double)r.hi + (double)r.lo;
     }
@@ -546,27 +543,29 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
 
 /* Diagnostics entry (declared in the public header): host arrays in and
  * out, synchronous, on the default stream of `device`. */
-extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, double* out)
+extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z,
+                             double* out)
 {
-    if (op < 0 || op > 4 || n < 0 || (n > 0 && (!x || !y || !out))) return MWSEP_ERR_ARG;
+    if (op < 0 || op > 5 || n < 0 || (n > 0 && (!x || !y || !z || !out))) return MWSEP_ERR_ARG;
     if (n == 0) return MWSEP_OK;
     if (cudaSetDevice(device) != cudaSuccess || mwsep_df_prepare(device)) return MWSEP_ERR_CUDA;
     const size_t bytes = (size_t)n * sizeof(double);
     double* d = nullptr;
-    if (cudaMalloc(&d, 3 * bytes) != cudaSuccess)
+    if (cudaMalloc(&d, 4 * bytes) != cudaSuccess)
     {
         cudaGetLastError();
         return MWSEP_ERR_NOMEM;
     }
     cudaError_t e = cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d + n, y, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + 2 * (size_t)n, z, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
     {
         const int grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
-        df_eval_kernel<<<grid, 256>>>(op, n, d, d + n, d + 2 * (size_t)n);
+        df_eval_kernel<<<grid, 256>>>(op, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
     cudaFree(d);
     return e == cudaSuccess ? MWSEP_OK : MWSEP_ERR_CUDA;
 }

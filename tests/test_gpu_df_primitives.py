@@ -4,7 +4,8 @@ by one Newton step from the SFU approximations, Dekker's add and the FMA
 product), against numpy's FP64 results for the same split inputs.  Measured
 maxima on GB300: exp2 1.9e-14, sqrt 1.5e-14, quotient 2.4e-14, product
 1.2e-14, sum 8e-15 of |x| + |y|; the bounds below are 2^-45 (2.8e-14) and
-2^-46 (1.4e-14)."""
+2^-46 (1.4e-14).  The reference values ks*us*us are FP64 products: their own
+rounding (~2^-52) is far below the bounds."""
 import ctypes as C
 
 import numpy as np
@@ -12,7 +13,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-EXP2, SQRT, DIV, MUL, ADD = range(5)
+EXP2, SQRT, DIV, MUL, ADD, SQ_SCALE_ADD = range(6)
 
 
 def _split(x):
@@ -22,13 +23,15 @@ def _split(x):
     return hi.astype(np.float64) + lo.astype(np.float64)
 
 
-def _eval(op, x, y=None):
+def _eval(op, x, y=None, z=None):
     from milkywayathome_client_gb300 import native as N
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
+    z = np.ascontiguousarray(np.zeros_like(x) if z is None else z, dtype=np.float64)
     out = np.zeros_like(x)
     P = C.POINTER(C.c_double)
-    rc = N.lib().mwsep_df_eval(0, op, x.size, x.ctypes.data_as(P), y.ctypes.data_as(P), out.ctypes.data_as(P))
+    rc = N.lib().mwsep_df_eval(0, op, x.size, x.ctypes.data_as(P), y.ctypes.data_as(P), z.ctypes.data_as(P),
+                               out.ctypes.data_as(P))
     assert rc == 0, rc
     return out
 
@@ -86,3 +89,18 @@ def test_product_and_sum(rng):
     got = _eval(ADD, x, y)
     err = np.abs(got - (xs + ys)) / (np.abs(xs) + np.abs(ys))
     assert err.max() <= 2.0 ** -46, err.max()
+
+
+def test_sq_scale_add(rng):
+    """k u^2 + c, the exponent and halo quadratic: about five roundings of
+    2^-47 of |k u^2| + |c| (measured 3.3e-14), also where the two cancel
+    (c ~ -k u^2)."""
+    k = -np.exp(rng.uniform(np.log(1e-3), np.log(10.0), 200000))
+    u = rng.uniform(-30.0, 30.0, 200000)
+    ks, us = _split(k), _split(u)
+    ku2 = ks * us * us
+    c = np.where(rng.random(200000) < 0.5, rng.uniform(-50.0, 0.0, 200000), -ku2 * rng.uniform(0.9, 1.1, 200000))
+    got = _eval(SQ_SCALE_ADD, k, u, c)
+    want = ku2 + _split(c)
+    err = (np.abs(got - want) / (np.abs(ku2) + np.abs(_split(c)))).max()
+    assert err <= 2.0 ** -44, err

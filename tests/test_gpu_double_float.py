@@ -166,14 +166,14 @@ def test_double_float_star_table_respects_hbm_budget():
         ctx.set_stars(sp)
         ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
         ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32)
-        ctx.set_hbm_budget(ctx.device_bytes() + 1024)
+        ctx.set_hbm_budget(ctx.device_bytes + 1024)
         with pytest.raises(mw.MwsepError) as e:
             ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
         assert e.value.status == N.MWSEP_ERR_BUDGET
         r = ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
         assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
-        before = ctx.device_bytes()
+        before = ctx.device_bytes
         ctx.set_hbm_budget(0)
         r = ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
         assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
-        assert ctx.device_bytes() - before >= 16 * sp.to_array().shape[0] * 20  # convolve 20
+        assert ctx.device_bytes - before >= 16 * sp.to_array().shape[0] * 20  # convolve 20
