@@ -179,8 +179,8 @@ enum
      * alpha = delta = 1 background, with or without the aux profile, and up
      * to 4 streams; any other problem is evaluated as MWSEP_PLAIN_F64.
      * Single-wedge evaluations and
-     * batches, engine requests (each wedge's requests as one batch) and the
-     * gradient/Hessian calls; the server and the engine autotuner take the
+     * batches, engine requests (each wedge's requests as one batch), the
+     * server and the gradient/Hessian calls; the engine autotuner takes the
      * other two forms. */
     MWSEP_PLAIN_DF = 2
 };

@@ -202,8 +202,8 @@ extern "C" int mwsep_server_submit(mwsep_server* s, int wedge, const double* the
                                    unsigned long long* id)
 {
     if (!s || !theta || !id) return mwsep_fail(MWSEP_ERR_ARG);
-    if (precision == MWSEP_PLAIN_DF) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
-    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
+        return mwsep_fail(MWSEP_ERR_ARG);
     const int n = mwsep_ctx_wedge_theta_count(s->parent, wedge);
     if (n < 0) return mwsep_fail(MWSEP_ERR_ARG);
     Request* r = new (std::nothrow) Request();

@@ -66,6 +66,24 @@ def test_served_results_equal_alone(served):
     assert 0 < st["p50_latency_s"] <= st["p99_latency_s"] <= st["max_latency_s"]
 
 
+def test_served_double_float_equal_alone(served):
+    """The double-float form through the server: requests of all three
+    forms interleaved, each batch one form, results bit-identical to the
+    request evaluated alone."""
+    import milkywayathome_client_gb300 as mw
+    ctx, wedges = served
+    rng = np.random.default_rng(29)
+    work = [(w, t, int(rng.integers(3))) for w, t, _ in _workload(wedges, 24, 29)]
+    assert any(p == mw.MWSEP_PLAIN_DF for _, _, p in work)
+    alone = [ctx.evaluate_requests([(w, t)], p)[0] for w, t, p in work]
+    with mw.Server(ctx, lanes=2, max_batch=8) as srv:
+        ids = [srv.submit(w, t, p) for w, t, p in work]
+        got = [srv.wait(i, timeout=300) for i in ids]
+    for a, b in zip(alone, got):
+        assert a.integrals == b.integrals
+        assert a.likelihood == b.likelihood or (a.likelihood != a.likelihood and b.likelihood != b.likelihood)
+
+
 def test_cancel_and_timeout(served):
     import milkywayathome_client_gb300 as mw
     from milkywayathome_client_gb300 import native as N
