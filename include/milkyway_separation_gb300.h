@@ -199,9 +199,11 @@ const char* mwsep_version(void);
 int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, unsigned long long* first);
 /* The double-float primitives of MWSEP_PLAIN_DF evaluated element-wise on
  * `device`, for testing their error bounds: op 0 2^x, 1 sqrt(x), 2 x / y,
- * 3 x * y, 4 x + y, 5 x y^2 + z.  Inputs are doubles (split into FP32 pairs
- * on the device), outputs the pairs' values as doubles; host arrays of n
- * elements (y and z unused by the ops that do not take them), synchronous. */
+ * 3 x * y, 4 x + y, 5 x y^2 + z; ops 10-15 the same through the packed
+ * versions the integral kernel uses (elements taken two at a time).  Inputs
+ * are doubles (split into FP32 pairs on the device), outputs the pairs'
+ * values as doubles; host arrays of n elements (y and z unused by the ops
+ * that do not take them), synchronous. */
 int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z, double* out);
 
 /* ------------------------------------------------------------------ */

@@ -48,6 +48,8 @@ namespace D = mwsep::dfl;
 
 constexpr int kBlock = 256;
 constexpr int DFP = MWSEP_DF_TILE_P; /* points per lane per group */
+constexpr int NPR = DFP / 2;           /* ... as pairs of points */
+static_assert(DFP % 2 == 0, "points are taken in pairs");
 
 /* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0 - eref. */
 template <int S>
@@ -79,7 +81,8 @@ __device__ __forceinline__ df get(const float* src, int i)
 template <int S>
 __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwsep_theta_consts& th, long long wt,
                                              float* __restrict__ cs, float* __restrict__ kf,
-                                             const float2* __restrict__ tab, double (&acc)[1 + S])
+                                             const float* __restrict__ thi, const float* __restrict__ tlo,
+                                             double (&acc)[1 + S])
 {
     constexpr int CW = ColDF<S>::W;
     const int lane = threadIdx.x & 31;
@@ -117,7 +120,7 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     }
     __syncwarp();
 
-    const df r0 = D::from_double(th.r0);
+    const D::df2 r0 = D::dup(D::from_double(th.r0));
     const int C = A.convolve;
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
@@ -125,15 +128,19 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     for (int g0 = 0; g0 < nf; g0 += 32 * DFP)
     {
-        df r[DFP], w[DFP];
+        /* the lane's points as pairs of points: pair q holds points 2q and
+         * 2q + 1 in the two halves of each register pair */
+        D::df2 r[NPR], w[NPR];
 #pragma unroll
-        for (int i = 0; i < DFP; ++i)
+        for (int q = 0; q < NPR; ++q)
         {
-            const int f = g0 + 32 * i + lane;
+            const int fa = g0 + 32 * (2 * q) + lane, fb = fa + 32;
             /* past the tile's end: a copy of its first point with zero weight */
-            const float4 v = A.ptsdf[MWSEP_IDX((size_t)k0 * C + (f < nf ? f : 0), (size_t)A.r_steps * C, 2)];
-            r[i] = D::mk(v.x, v.y);
-            w[i] = (f < nf) ? D::mk(v.z, v.w) : D::mk(0.f, 0.f);
+            const float4 va = A.ptsdf[MWSEP_IDX((size_t)k0 * C + (fa < nf ? fa : 0), (size_t)A.r_steps * C, 2)];
+            const float4 vb = A.ptsdf[MWSEP_IDX((size_t)k0 * C + (fb < nf ? fb : 0), (size_t)A.r_steps * C, 2)];
+            r[q] = D::mk2(make_float2(va.x, vb.x), make_float2(va.y, vb.y));
+            w[q] = D::mk2(make_float2(fa < nf ? va.z : 0.f, fb < nf ? vb.z : 0.f),
+                          make_float2(fa < nf ? va.w : 0.f, fb < nf ? vb.w : 0.f));
         }
         /* the group's largest stream exponent (FP32 estimate, error far
          * below 1 for |k0| < 2^20), and the columns' k0 shifted by its floor */
@@ -151,9 +158,10 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                 {
                     /* k2 <= 0: the largest exponent is at the point nearest rs */
                     const float rs = c[2 * (3 + 3 * s)], k2 = c[2 * (4 + 3 * s)], k0 = kf[j * S + s];
-                    float um = fabsf(__fsub_rn(r[0].hi, rs));
+                    float um = 3.0e38f;
 #pragma unroll
-                    for (int i = 1; i < DFP; ++i) um = fminf(um, fabsf(__fsub_rn(r[i].hi, rs)));
+                    for (int q = 0; q < NPR; ++q)
+                        um = fminf(um, fminf(fabsf(__fsub_rn(r[q].hi.x, rs)), fabsf(__fsub_rn(r[q].hi.y, rs))));
                     mx[s] = fmaxf(mx[s], __fmaf_rn(k2, __fmul_rn(um, um), k0));
                 }
             }
@@ -175,49 +183,53 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
         /* Per column: the background over the lane's points, then one
          * stream at a time (a rolled loop: the unrolled body of every stream
          * over every point overflows the instruction cache).  Each stream's
-         * eight terms are summed as a pair, then added to its lane sum. */
-        df bg = D::mk(0.f, 0.f), st[kSP(S)];
+         * terms are summed as a run (two halves of four), then added to its
+         * lane sums (two halves, joined in FP64 at the end of the group). */
+        D::df2 bg = D::mk2(D::pd(0.f), D::pd(0.f)), st[kSP(S)];
 #pragma unroll
-        for (int s = 0; s < S; ++s) st[s] = D::mk(0.f, 0.f);
+        for (int s = 0; s < S; ++s) st[s] = D::mk2(D::pd(0.f), D::pd(0.f));
         for (int j = 0; j < ncols; ++j)
         {
             const float* c = cs + j * CW;
-            const df B2 = get<S>(c, 0), nrb = D::neg(get<S>(c, 1)), Db = get<S>(c, 2);
-            D::lazy_sum pb;
+            const D::df2 B2 = D::dup(get<S>(c, 0)), nrb = D::dup(D::neg(get<S>(c, 1))), Db = D::dup(get<S>(c, 2));
+            D::lazy_sum2 pb;
 #pragma unroll
-            for (int i = 0; i < DFP; ++i)
+            for (int q = 0; q < NPR; ++q)
             {
-                const df rg = D::sqrt(D::sq_scale_add(B2, D::add_fast(r[i], nrb), Db));
-                const df sum = D::add_fast(rg, r0);
-                const df den = D::mul(rg, D::mul(sum, D::sqr(sum)));
-                const df q = D::div(w[i], den);
-                if (i == 0)
-                    pb = D::lazy_start(q);
+                const D::df2 rg = D::sqrt2(D::sq_scale_add2(B2, D::add_fast2(r[q], nrb), Db));
+                const D::df2 sum = D::add_fast2(rg, r0);
+                const D::df2 den = D::mul2(rg, D::mul2(sum, D::sqr2(sum)));
+                const D::df2 v = D::div2(w[q], den);
+                if (q == 0)
+                    pb = D::lazy_start2(v);
                 else
-                    D::lazy_add(pb, q);
+                    D::lazy_add2(pb, v);
             }
-            bg = D::add_fast(bg, D::lazy_end(pb));
+            bg = D::add_fast2(bg, D::lazy_end2(pb));
 #pragma unroll 1
             for (int s = 0; s < S; ++s)
             {
-                const df nrs = D::neg(get<S>(c, 3 + 3 * s)), k2 = get<S>(c, 4 + 3 * s), k0 = get<S>(c, 5 + 3 * s);
-                D::lazy_sum ps;
+                const D::df2 nrs = D::dup(D::neg(get<S>(c, 3 + 3 * s))), k2 = D::dup(get<S>(c, 4 + 3 * s)),
+                             k0 = D::dup(get<S>(c, 5 + 3 * s));
+                D::lazy_sum2 ps;
 #pragma unroll
-                for (int i = 0; i < DFP; ++i)
+                for (int q = 0; q < NPR; ++q)
                 {
-                    const df a = D::sq_scale_add(k2, D::add_fast(r[i], nrs), k0);
-                    const df e = D::mul_raw(w[i], D::exp2(a, tab));
-                    if (i == 0)
-                        ps = D::lazy_start(e);
+                    const D::df2 a = D::sq_scale_add2(k2, D::add_fast2(r[q], nrs), k0);
+                    const D::df2 e = D::mul_raw2(w[q], D::exp2_2(a, thi, tlo));
+                    if (q == 0)
+                        ps = D::lazy_start2(e);
                     else
-                        D::lazy_add(ps, e);
+                        D::lazy_add2(ps, e);
                 }
-                st[s] = D::add_fast(st[s], D::lazy_end(ps));
+                st[s] = D::add_fast2(st[s], D::lazy_end2(ps));
             }
         }
-        acc[0] += ((double)bg.hi + (double)bg.lo) * idsv;
+        acc[0] += (((double)bg.hi.x + (double)bg.lo.x) + ((double)bg.hi.y + (double)bg.lo.y)) * idsv;
 #pragma unroll
-        for (int s = 0; s < S; ++s) acc[1 + s] += ((double)st[s].hi + (double)st[s].lo) * scale[s] * idsv;
+        for (int s = 0; s < S; ++s)
+            acc[1 + s] += (((double)st[s].hi.x + (double)st[s].lo.x) + ((double)st[s].hi.y + (double)st[s].lo.y)) *
+                          scale[s] * idsv;
     }
     __syncwarp();
 }
@@ -231,9 +243,13 @@ __global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area
     __shared__ double red[2 * (1 + S) * 32];
     __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * ColDF<S>::W];
     __shared__ float kf[kBlock / 32][mwsep::kTileCols * kSP(S)];
-    __shared__ float2 tab[D::kExp2Table];
+    __shared__ float thi[D::kExp2Table], tlo[D::kExp2Table];
     mwsep::f64::load_theta(th, thetas + blockIdx.y);
-    for (int j = threadIdx.x; j < D::kExp2Table; j += kBlock) tab[j] = c_exp2_tab[j];
+    for (int j = threadIdx.x; j < D::kExp2Table; j += kBlock)
+    {
+        thi[j] = c_exp2_tab[j].x;
+        tlo[j] = c_exp2_tab[j].y;
+    }
     __syncthreads();
     double acc[1 + S];
 #pragma unroll
@@ -241,7 +257,7 @@ __global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area
     const int warp = threadIdx.x >> 5;
     const long long warps = (long long)gridDim.x * (kBlock / 32);
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
-        warp_tile_df<S>(A, th, wt, cs[warp], kf[warp], tab, acc);
+        warp_tile_df<S>(A, th, wt, cs[warp], kf[warp], thi, tlo, acc);
     /* block reduction into compensated pairs */
     mwsep::comp_sum cacc[1 + S];
 #pragma unroll
@@ -462,13 +478,47 @@ __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts
 
 /* Element-wise evaluation of the double-float primitives for the tests:
  * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker), 5 x y^2 + z;
+ * ops 10-15 the same through the packed (two values at once) versions;
  * inputs are doubles split into pairs, results returned as hi + lo in FP64. */
 __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, const double* __restrict__ y,
                                const double* __restrict__ z, double* __restrict__ out)
 {
     __shared__ float2 tab[D::kExp2Table];
-    for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x) tab[j] = c_exp2_tab[j];
+    __shared__ float thi[D::kExp2Table], tlo[D::kExp2Table];
+    for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x)
+    {
+        tab[j] = c_exp2_tab[j];
+        thi[j] = c_exp2_tab[j].x;
+        tlo[j] = c_exp2_tab[j].y;
+    }
     __syncthreads();
+    if (op >= 10)
+    {
+        /* element pairs (2i, 2i + 1); an odd last element is paired with itself */
+        const int np = (n + 1) / 2;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+        {
+            const int ia = 2 * i, ib = (2 * i + 1 < n) ? 2 * i + 1 : 2 * i;
+            auto pair = [&](const double* v) {
+                const df a = D::from_double(v[ia]), b = D::from_double(v[ib]);
+                return D::mk2(make_float2(a.hi, b.hi), make_float2(a.lo, b.lo));
+            };
+            const D::df2 a = pair(x), b = pair(y), c = pair(z);
+            D::df2 r;
+            switch (op)
+            {
+            case 10: r = D::exp2_2(a, thi, tlo); break;
+            case 11: r = D::sqrt2(a); break;
+            case 12: r = D::div2(a, b); break;
+            case 13: r = D::mul2(a, b); break;
+            case 14: r = D::add_fast2(a, b); break;
+            default: r = D::sq_scale_add2(a, b, c); break;
+            }
+            out[ia] = (double)r.hi.x + (double)r.lo.x;
+            out[ib] = (double)r.hi.y + (double)r.lo.y;
+        }
+        return;
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const df a = D::from_double(x[i]), b = D::from_double(y[i]);
@@ -546,7 +596,8 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
 extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z,
                              double* out)
 {
-    if (op < 0 || op > 5 || n < 0 || (n > 0 && (!x || !y || !z || !out))) return MWSEP_ERR_ARG;
+    if (op < 0 || (op > 5 && op < 10) || op > 15 || n < 0 || (n > 0 && (!x || !y || !z || !out)))
+        return MWSEP_ERR_ARG;
     if (n == 0) return MWSEP_OK;
     if (cudaSetDevice(device) != cudaSuccess || mwsep_df_prepare(device)) return MWSEP_ERR_CUDA;
     const size_t bytes = (size_t)n * sizeof(double);
