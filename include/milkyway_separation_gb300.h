@@ -299,6 +299,12 @@ double mwsep_evaluate(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_S
  * log-likelihood. */
 double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
 
+/* Same contract in the double-float form (MWSEP_PLAIN_DF): the plain form's
+ * bounds (1e-12 relative on the integrals, 1e-12 absolute on the
+ * log-likelihood) at about 16x its speed; problems outside that form's
+ * coverage are evaluated as mwsep_evaluate does. */
+double mwsep_evaluate_df(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
+
 /* ------------------------------------------------------------------ */
 /* Context API: resident wedges and catalogues, batches                 */
 /* ------------------------------------------------------------------ */
@@ -444,7 +450,7 @@ int mwsep_server_destroy(mwsep_server* s);
 int mwsep_ctx_transfer_bytes(const mwsep_ctx* ctx, size_t* h2d, size_t* d2h);
 
 /* Bytes copied host->device and device->host by the most recent
- * mwsep_evaluate / mwsep_evaluate_mixed call on this process. */
+ * mwsep_evaluate / _mixed / _df call on this process. */
 int mwsep_evalfunc_transfer_bytes(size_t* h2d, size_t* d2h);
 
 /* ------------------------------------------------------------------ */

@@ -10,8 +10,9 @@
  * and the reference's result lines on stderr.  Without BOINC or popt: flags
  * are parsed by hand.
  *
- *   mwsep_client -a astronomy_parameters.txt -p stars.txt [--mixed] [-k N] theta...
+ *   mwsep_client -a astronomy_parameters.txt -p stars.txt [--mixed | --df] [-k N] theta...
  *     --mixed   compensated-FP32 evaluator (default: plain FP64)
+ *     --df      double-float evaluator (the plain form's bounds on the FP32 pipes)
  *     -k N      evaluate N times (timing; prints seconds per evaluation)
  */
 #include <stdio.h>
@@ -59,11 +60,12 @@ int main(int argc, char** argv)
         else if (!strcmp(argv[i], "-p") && i + 1 < argc) sfile = argv[++i];
         else if (!strcmp(argv[i], "-k") && i + 1 < argc) repeats = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--mixed")) mixed = 1;
+        else if (!strcmp(argv[i], "--df")) mixed = 2;
         else params[n++] = strtod(argv[i], NULL);
     }
     if (!pfile || !sfile)
     {
-        fprintf(stderr, "usage: %s -a params -p stars [--mixed] [-k N] theta...\n", argv[0]);
+        fprintf(stderr, "usage: %s -a params -p stars [--mixed | --df] [-k N] theta...\n", argv[0]);
         return 2;
     }
     memset(&ap, 0, sizeof(ap));
@@ -94,7 +96,7 @@ int main(int argc, char** argv)
     }
     mwsep_set_astronomy_parameters(&ap, params);
 
-    evaluate = mixed ? mwsep_evaluate_mixed : mwsep_evaluate;
+    evaluate = mixed == 1 ? mwsep_evaluate_mixed : mixed == 2 ? mwsep_evaluate_df : mwsep_evaluate;
     if (repeats < 1)
         repeats = 1;
     t0 = now_s();
@@ -114,7 +116,7 @@ int main(int argc, char** argv)
     fprintf(stderr, " </stream_integrals>\n");
     fprintf(stderr, "<search_likelihood> %0.20f </search_likelihood>\n", likelihood);
     fprintf(stderr, "<search_application> %s %s </search_application>\n", mwsep_version(),
-            mixed ? "mixed" : "double");
+            mixed == 1 ? "mixed" : mixed == 2 ? "double-float" : "double");
     if (repeats > 1)
         fprintf(stderr, "<seconds_per_evaluation> %.6f </seconds_per_evaluation>\n", (t1 - t0) / repeats);
 

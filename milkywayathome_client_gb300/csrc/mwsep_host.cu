@@ -1210,3 +1210,9 @@ extern "C" double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS*
 {
     return evalfunc_impl(parameters, ap, es, sp, MWSEP_MIXED_F32);
 }
+
+extern "C" double mwsep_evaluate_df(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                                    STAR_POINTS* sp)
+{
+    return evalfunc_impl(parameters, ap, es, sp, MWSEP_PLAIN_DF);
+}

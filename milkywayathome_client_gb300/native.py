@@ -198,6 +198,8 @@ _SIGS = {
                                     _P(STAR_POINTS)]),
     "mwsep_evaluate_mixed": (C.c_double, [_P(C.c_double), _P(ASTRONOMY_PARAMETERS),
                                           _P(EVALUATION_STATE), _P(STAR_POINTS)]),
+    "mwsep_evaluate_df": (C.c_double, [_P(C.c_double), _P(ASTRONOMY_PARAMETERS),
+                                       _P(EVALUATION_STATE), _P(STAR_POINTS)]),
     "mwsep_ctx_create": (C.c_int, [C.c_int, _P(C.c_void_p)]),
     "mwsep_ctx_destroy": (C.c_int, [C.c_void_p]),
     "mwsep_ctx_set_problem": (C.c_int, [C.c_void_p, _P(ASTRONOMY_PARAMETERS)]),

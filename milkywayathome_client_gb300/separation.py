@@ -282,6 +282,12 @@ def evaluate_mixed(theta, ap: AstronomyParameters, es: EvaluationState, sp: Star
     return _evalfunc(N.lib().mwsep_evaluate_mixed, theta, ap, es, sp)
 
 
+def evaluate_df(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> float:
+    """Double-float GPU evaluation (the plain form's bounds) with the same
+    contract as evaluate."""
+    return _evalfunc(N.lib().mwsep_evaluate_df, theta, ap, es, sp)
+
+
 @dataclass
 class Result:
     likelihood: float

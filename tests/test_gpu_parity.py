@@ -97,6 +97,14 @@ def test_evalfunc_dropin(built_library, name):
     np.testing.assert_array_equal(ap.search_parameters(), np.asarray(g["theta"]))
     vm = mw.evaluate_mixed(g["theta"], ap, es, sp)
     assert abs((vm - 3.0) - g["likelihood"]) <= ABS_LOGL_F32
+    # the double-float EvalFunc: the plain form's bounds, the same state filled
+    es2 = mw.EvaluationState(ap, sp)
+    vd = mw.evaluate_df(g["theta"], ap, es2, sp)
+    assert _close_abs(vd - 3.0, g["likelihood"], ABS_LOGL_F64)
+    assert _close_rel(es2.background_integral, g["background_integral"], REL_INT_F64)
+    for x, y in zip(es2.stream_integrals, g["stream_integrals"]):
+        assert _close_rel(x, y, REL_INT_F64)
+    assert _close_rel(es2.prob_sum, g["prob_sum"], 1e-12)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -134,15 +142,16 @@ def test_against_live_oracle(gpu_ctx, oracle_built, name):
         assert _close_abs(x, y, 1e-12)
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_c_client_matches_reference(built_library, mixed):
+@pytest.mark.parametrize("flag", [None, "--mixed", "--df"])
+def test_c_client_matches_reference(built_library, flag):
     """The C command-line client (worker() on the C ABI) prints the
     reference's result lines with the reference's numbers."""
     import re
     import subprocess
     from milkywayathome_client_gb300 import build
     pf, sf, g = load_case("cut_area")
-    cmd = [build.CLIENT_PATH, "-a", pf, "-p", sf] + (["--mixed"] if mixed else []) + \
+    mixed = flag == "--mixed"
+    cmd = [build.CLIENT_PATH, "-a", pf, "-p", sf] + ([flag] if flag else []) + \
         [repr(float(x)) for x in g["theta"]]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
