@@ -331,6 +331,13 @@ def run_gb300_arm(args, ws, rank, local):
     e2e_step = allreduce_max(ws, sum(e2e_t)) / args.e2e_steps
     e2e_value = ws / e2e_step
     e2e_logl = v - 3.0
+    # the double-float form through its EvalFunc entry (mwsep_evaluate_df)
+    es_df = mw.EvaluationState(ap, sp)
+    mw.evaluate_df(theta, ap, es_df, sp)
+    t0 = time.perf_counter()
+    mw.evaluate_df(theta, ap, es_df, sp)
+    double_float["e2e"] = {"value": ws / allreduce_max(ws, time.perf_counter() - t0), "unit": "evals/s",
+                           "api": "mwsep_evaluate_df (EvalFunc, host structs)"}
 
     # roofline of the dominant kernel (the compensated integral, packed warp
     # tiles).  Per convolution point it issues 10.5 + 4S FP32 lane-ops
