@@ -176,8 +176,9 @@ enum
     /* The plain form's accuracy (1e-12 relative on the integrals) computed in
      * double-float arithmetic -- pairs of FP32 values, about 48 bits -- on
      * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Covers the
-     * alpha = delta = 1 background, with or without the aux profile, and up
-     * to 4 streams; any other problem is evaluated as MWSEP_PLAIN_F64.
+     * alpha = delta = 1 background, with or without the aux profile (its
+     * likelihood in double-float up to 4 streams, in FP64 beyond); general
+     * alpha/delta and q = 0 are evaluated as MWSEP_PLAIN_F64.
      * Single-wedge evaluations and
      * batches, engine requests (each wedge's requests as one batch), the
      * server and the gradient/Hessian calls; the engine autotuner takes the

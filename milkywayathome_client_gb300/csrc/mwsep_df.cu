@@ -24,8 +24,9 @@
  * (times ids), across blocks the usual compensated FP64 reduction.
  *
  * Background forms: alpha = delta = 1, with or without the aux profile
- * (whose column-independent share aux_area_kernel adds), up to 4 streams;
- * the host runs any other problem through the native FP64 kernel.
+ * (whose column-independent share aux_area_kernel adds), up to 8 streams
+ * (the likelihood kernel below up to 4; the host runs the FP64 likelihood
+ * beyond); the host runs any other form through the native FP64 kernels.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -46,7 +47,14 @@ namespace {
 using mwsep::dfl::df;
 namespace D = mwsep::dfl;
 
-constexpr int kBlock = 256;
+/* Integral blocks: 8 warps up to 4 streams, 4 warps for 5-8 streams (the
+ * columns' constants then take twice the shared memory per warp). */
+template <int S>
+struct DfShape
+{
+    static constexpr int block = S > 4 ? 128 : 256;
+    static constexpr int min_blocks = S > 4 ? 4 : 2;
+};
 constexpr int DFP = MWSEP_DF_TILE_P; /* points per lane per group */
 constexpr int NPR = DFP / 2;           /* ... as pairs of points */
 static_assert(DFP % 2 == 0, "points are taken in pairs");
@@ -235,12 +243,13 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
 }
 
 template <int S>
-__global__ void __launch_bounds__(kBlock, 2) integral_df_kernel(const mwsep_area_dev A,
+__global__ void __launch_bounds__(DfShape<S>::block, DfShape<S>::min_blocks) integral_df_kernel(const mwsep_area_dev A,
                                                                 const mwsep_theta_consts* __restrict__ thetas,
                                                                 double2* __restrict__ partials, long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (1 + S) * 32];
+    constexpr int kBlock = DfShape<S>::block;
     __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * ColDF<S>::W];
     __shared__ float kf[kBlock / 32][mwsep::kTileCols * kSP(S)];
     __shared__ float thi[D::kExp2Table], tlo[D::kExp2Table];
@@ -284,14 +293,14 @@ int launch(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_la
     const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
     double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
-    integral_df_kernel<S><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride);
+    integral_df_kernel<S><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
     return (int)cudaGetLastError();
 }
 
 template <int S>
 cudaError_t occupancy(int* b)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_df_kernel<S>, kBlock, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_df_kernel<S>, DfShape<S>::block, 0);
 }
 
 /* Per-star double-float table [C][N]: {r_hi, r_lo, qw_hi, qw_lo}. */
@@ -566,7 +575,11 @@ extern "C" int mwsep_integral_df_blocks_per_sm(int n_streams)
     case 1: e = occupancy<1>(&b); break;
     case 2: e = occupancy<2>(&b); break;
     case 3: e = occupancy<3>(&b); break;
-    default: e = occupancy<4>(&b); break; /* 5..8 streams run in native FP64 */
+    case 4: e = occupancy<4>(&b); break;
+    case 5: e = occupancy<5>(&b); break;
+    case 6: e = occupancy<6>(&b); break;
+    case 7: e = occupancy<7>(&b); break;
+    default: e = occupancy<8>(&b); break;
     }
     if (e != cudaSuccess)
     {
@@ -587,7 +600,11 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
     case 2: return launch<2>(area, th_dev, sh, partials, st);
     case 3: return launch<3>(area, th_dev, sh, partials, st);
     case 4: return launch<4>(area, th_dev, sh, partials, st);
-    default: return (int)cudaErrorInvalidValue; /* 5..8 streams run in native FP64 */
+    case 5: return launch<5>(area, th_dev, sh, partials, st);
+    case 6: return launch<6>(area, th_dev, sh, partials, st);
+    case 7: return launch<7>(area, th_dev, sh, partials, st);
+    case 8: return launch<8>(area, th_dev, sh, partials, st);
+    default: return (int)cudaErrorInvalidValue;
     }
 }
 

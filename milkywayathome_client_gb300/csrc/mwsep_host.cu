@@ -410,7 +410,7 @@ void default_tune(mwsep_ctx* c, Wedge& w)
     for (int prec = 0; prec < 3; ++prec)
     {
         Tune& t = w.tune[prec];
-        t.block = 256;
+        t.block = (prec == MWSEP_PLAIN_DF && p.n_streams > 4) ? 128 : 256; /* the DF kernel's own blocks */
         t.warp_items = (prec == MWSEP_PLAIN_DF ||
                         (prec == MWSEP_MIXED_F32 && env_long("MWSEP_F32_WARP_TILES", 1) != 0)) ? 1 : 0;
         const int per_sm = prec == MWSEP_PLAIN_F64   ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
@@ -795,16 +795,18 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
     for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
     /* the double-float integral covers the alpha = delta = 1 background,
-     * with or without the aux profile, and up to 4 streams; anything else
+     * with or without the aux profile (any stream count), its likelihood up
+     * to 4 streams (the FP64 likelihood beyond); any other background form
      * runs in native FP64 */
     bool df_aux = false;
     if (precision == MWSEP_PLAIN_DF)
         for (int i = 0; i < B; ++i)
         {
             const int form = mwsep_bg_form(&hth[i]);
-            if (form > 1 || S > 4) precision = MWSEP_PLAIN_F64;
+            if (form > 1) precision = MWSEP_PLAIN_F64;
             df_aux = df_aux || form == 1;
         }
+    const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4;
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
     const Tune& t = w.tune[precision];
     const size_t part_bytes = sizeof(double2) * (size_t)B * A * t.grid * ncomp;
@@ -817,7 +819,7 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     rc |= c->d_out.ensure(out_doubles * 8, tot);
     rc |= c->h_out.ensure(out_doubles * 8);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
-    if (precision == MWSEP_PLAIN_DF && !w.has_star_df)
+    if (df_likelihood && !w.has_star_df)
     {
         const size_t before = tot, need = (size_t)w.n_stars * p.convolve * sizeof(float4);
         if (c->hbm_budget && tot + need > c->hbm_budget) return mwsep_fail(MWSEP_ERR_BUDGET);
@@ -891,10 +893,10 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     lk.block = t.lk_block;
     lk.grid = t.lk_grid;
     lk.area_index = 0;
-    if (precision == MWSEP_PLAIN_DF)
+    if (df_likelihood)
         CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
                                       &lk, d_ints, c->d_lkpartials.as<double2>(), st));
-    else if (precision == MWSEP_PLAIN_F64)
+    else if (precision != MWSEP_MIXED_F32)
         CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
     else

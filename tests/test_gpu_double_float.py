@@ -74,11 +74,25 @@ def test_double_float_matches_native_fp64_at_full_size(gpu_ctx):
 def test_double_float_limits(gpu_ctx):
     import milkywayathome_client_gb300 as mw
     from milkywayathome_client_gb300 import native as N
-    for name in ("general_alpha_delta", "six_streams"):  # run in native FP64: identical bits
-        g = _setup(gpu_ctx, name)
-        a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
-        b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
-        assert a.integrals == b.integrals and a.likelihood == b.likelihood
+    # general alpha/delta and q = 0 run in native FP64: identical bits
+    g = _setup(gpu_ctx, "general_alpha_delta")
+    a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+    assert a.integrals == b.integrals and a.likelihood == b.likelihood
+    g = _setup(gpu_ctx, "three_streams")
+    theta = list(g["theta"])
+    theta[0] = 0.0  # q
+    a = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_DF)
+    assert a.background_integral == b.background_integral
+    # more than 4 streams: the double-float integral with the FP64 likelihood
+    g = _setup(gpu_ctx, "six_streams")
+    a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
+    assert a.integrals != b.integrals
+    for x, y in zip(b.integrals, a.integrals):
+        assert _close_rel(x, y, REL), (x, y)
+    assert abs(a.likelihood - b.likelihood) <= ABS_LOGL
     pf, sf, g = load_case("basic_1stream")
     with mw.Context(0) as ctx:
         ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
