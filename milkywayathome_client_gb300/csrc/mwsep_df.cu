@@ -38,9 +38,6 @@
 #include "mwsep_internal.h"
 #include "mwsep_reduce.cuh"
 
-#ifndef MWSEP_DF_TILE_P
-#define MWSEP_DF_TILE_P 8
-#endif
 
 namespace {
 
@@ -55,9 +52,7 @@ struct DfShape
     static constexpr int block = S > 4 ? 128 : 256;
     static constexpr int min_blocks = S > 4 ? 4 : 2;
 };
-constexpr int DFP = MWSEP_DF_TILE_P; /* points per lane per group */
-constexpr int NPR = DFP / 2;           /* ... as pairs of points */
-static_assert(DFP % 2 == 0, "points are taken in pairs");
+static_assert(MWSEP_DF_TILE_P % 2 == 0, "points are taken in pairs");
 
 /* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0 - eref. */
 template <int S>
@@ -93,6 +88,8 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                                              double (&acc)[1 + S])
 {
     constexpr int CW = ColDF<S>::W;
+    constexpr int DFP = mwsep_df_tile_p(S); /* points per lane per group */
+    constexpr int NPR = DFP / 2;            /* ... as pairs of points */
     const int lane = threadIdx.x & 31;
     const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
     const long long rest = wt / nmb;

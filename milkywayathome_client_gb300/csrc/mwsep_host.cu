@@ -429,7 +429,7 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             nk = std::max<long long>(1, std::min<long long>(nk, max_r));
             int kc = (int)((max_r + nk - 1) / nk);
             const int group = prec == MWSEP_PLAIN_DF
-                                  ? 32 * MWSEP_DF_TILE_P
+                                  ? 32 * mwsep_df_tile_p(p.n_streams)
                                   : 32 * (p.n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
             int ks = group;
             for (int a = group, b = std::max(p.convolve, 1); b;)

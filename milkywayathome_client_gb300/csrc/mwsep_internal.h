@@ -245,8 +245,13 @@ int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_con
 int mwsep_integral_f32_blocks_per_sm(int n_streams, int warp_items);
 /* double-float integral (mwsep_df.cu) */
 #ifndef MWSEP_DF_TILE_P
-#define MWSEP_DF_TILE_P 8
+/* points per lane, even; 8 / 12 / 16: 171.5 / 172.3 / 171.2 ms on the
+ * full-size wedge, 6.55 / 6.26 / 6.72 ms on the 400 x 160 x 140 one */
+#define MWSEP_DF_TILE_P 12
 #endif
+/* ... up to 4 streams; the 5-8 stream instances (4-warp blocks, 128
+ * registers) take 8, which they hold without spilling */
+MWSEP_HD constexpr int mwsep_df_tile_p(int n_streams) { return n_streams > 4 ? 8 : MWSEP_DF_TILE_P; }
 int mwsep_df_prepare(int device);
 int mwsep_integral_df_blocks_per_sm(int n_streams);
 int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
