@@ -31,6 +31,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "milkyway_separation_gb300.h"
 #include "mwsep_checks.cuh"
 #include "mwsep_df.cuh"
@@ -542,23 +545,31 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
     }
 }
 
-bool g_table_ready[64] = {};
+std::atomic<bool> g_table_ready[64];
+std::mutex g_table_mu;
 
 } // namespace
 
-/* Upload the 2^(j/1024) table to this device (once per device). */
+/* Upload the 2^(j/1024) table to `device` (once per device; contexts on
+ * other threads may ask at the same time). */
 extern "C" int mwsep_df_prepare(int device)
 {
     if (device < 0 || device >= 64) return 1;
-    if (g_table_ready[device]) return 0;
+    if (g_table_ready[device].load(std::memory_order_acquire)) return 0;
+    std::lock_guard<std::mutex> lock(g_table_mu);
+    if (g_table_ready[device].load(std::memory_order_relaxed)) return 0;
     float2 t[D::kExp2Table];
     for (int j = 0; j < D::kExp2Table; ++j)
     {
         const mwsep::dfl::df v = mwsep::dfl::from_double(exp2((double)j / D::kExp2Table));
         t[j] = make_float2(v.hi, v.lo);
     }
-    if (cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t)) != cudaSuccess) return 1;
-    g_table_ready[device] = true;
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) return 1;
+    const cudaError_t e = cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t));
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return 1;
+    g_table_ready[device].store(true, std::memory_order_release);
     return 0;
 }
 

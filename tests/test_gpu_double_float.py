@@ -2,9 +2,11 @@
 outputs at the plain form's tolerances (1e-12 relative on every integral,
 1e-12 absolute on the log-likelihood) -- every golden case, the aux profile
 included -- against the native FP64 kernel at full size, batch == single,
-engine requests and gradients, and its limits (general alpha/delta, q = 0
-and more than 4 streams run in native FP64; the autotuner refuses it)."""
+engine requests and gradients, first use from several threads, the device
+memory budget, and its limits (general alpha/delta and q = 0 run in native
+FP64, beyond 4 streams the likelihood does; the autotuner refuses it)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -191,3 +193,37 @@ def test_double_float_star_table_respects_hbm_budget():
         r = ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
         assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
         assert ctx.device_bytes - before >= 16 * sp.to_array().shape[0] * 20  # convolve 20
+
+
+def test_double_float_first_use_from_threads():
+    """Four contexts on four threads making their first double-float
+    evaluation at once (a fresh process, so the exp2 table is not yet on
+    the device): every result equals a single-threaded evaluation."""
+    import subprocess
+    import sys
+    import textwrap
+    pf, sf, g = load_case("three_streams")
+    code = textwrap.dedent(f"""
+        import threading, sys
+        sys.path.insert(0, {repr(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))})
+        import milkywayathome_client_gb300 as mw
+        ap, sp = mw.AstronomyParameters.read({pf!r}), mw.StarPoints.read({sf!r})
+        theta = {list(g["theta"])!r}
+        ctxs = [mw.Context(0) for _ in range(4)]
+        for c in ctxs:
+            c.set_problem(ap); c.set_stars(sp)
+        out = [None] * 4
+        go = threading.Barrier(4)
+        def run(i):
+            go.wait()
+            out[i] = ctxs[i].evaluate(theta, mw.MWSEP_PLAIN_DF)
+        ths = [threading.Thread(target=run, args=(i,)) for i in range(4)]
+        for t in ths: t.start()
+        for t in ths: t.join()
+        ref = ctxs[0].evaluate(theta, mw.MWSEP_PLAIN_DF)
+        assert all(o.integrals == ref.integrals and o.likelihood == ref.likelihood for o in out)
+        print("ok", ref.likelihood)
+    """)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.startswith("ok")
