@@ -176,9 +176,9 @@ enum
     /* The plain form's accuracy (1e-12 relative on the integrals) computed in
      * double-float arithmetic -- pairs of FP32 values, about 48 bits -- on
      * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Covers the
-     * alpha = delta = 1 background, with or without the aux profile (its
-     * likelihood in double-float up to 4 streams, in FP64 beyond); general
-     * alpha/delta and q = 0 are evaluated as MWSEP_PLAIN_F64.
+     * alpha = delta = 1 background with or without the aux profile and
+     * general alpha/delta (its likelihood in double-float up to 4 streams,
+     * in FP64 beyond); q = 0 is evaluated as MWSEP_PLAIN_F64.
      * Single-wedge evaluations and
      * batches, engine requests (each wedge's requests as one batch), the
      * server and the gradient/Hessian calls; the engine autotuner takes the
@@ -200,7 +200,7 @@ const char* mwsep_version(void);
 int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, unsigned long long* first);
 /* The double-float primitives of MWSEP_PLAIN_DF evaluated element-wise on
  * `device`, for testing their error bounds: op 0 2^x, 1 sqrt(x), 2 x / y,
- * 3 x * y, 4 x + y, 5 x y^2 + z; ops 10-15 the same through the packed
+ * 3 x * y, 4 x + y, 5 x y^2 + z, 6 log2(x); ops 10-16 the same through the packed
  * versions the integral kernel uses (elements taken two at a time).  Inputs
  * are doubles (split into FP32 pairs on the device), outputs the pairs'
  * values as doubles; host arrays of n elements (y and z unused by the ops

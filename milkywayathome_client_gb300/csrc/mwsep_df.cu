@@ -52,9 +52,17 @@ namespace D = mwsep::dfl;
 template <int S>
 struct DfShape
 {
-    static constexpr int block = S > 4 ? 128 : 256;
-    static constexpr int min_blocks = S > 4 ? 4 : 2;
+    static constexpr int block = S >= 4 ? 128 : 256;
+    static constexpr int min_blocks = S >= 4 ? 4 : 2;
 };
+/* Background forms of the double-float kernels: alpha = delta = 1 (the aux
+ * profile's share added separately) or general alpha/delta; each launch
+ * skips the thetas of the other form. */
+constexpr int kFormHern = 0, kFormGeneral = 2;
+__device__ __forceinline__ bool df_form_is(const mwsep_theta_consts& th, int form)
+{
+    return (mwsep_bg_form(&th) == 2) == (form == kFormGeneral);
+}
 static_assert(MWSEP_DF_TILE_P % 2 == 0, "points are taken in pairs");
 
 /* Column constants, as pairs: B2, rb, Db, then per stream rs, k2, k0 - eref. */
@@ -67,6 +75,8 @@ __host__ __device__ constexpr int kSP(int S) { return S > 0 ? S : 1; }
 
 /* 2^(j/1024) as pairs (host-built). */
 __constant__ float2 c_exp2_tab[D::kExp2Table];
+/* {log2 c, 1/c} as pairs for c = 1 + j/256 (host-built). */
+__constant__ float4 c_log2_tab[D::kLog2Table];
 
 template <int S>
 __device__ __forceinline__ void put(float* dst, int i, double v)
@@ -84,11 +94,11 @@ __device__ __forceinline__ df get(const float* src, int i)
 }
 
 /* One warp tile of the double-float integral (all 32 lanes). */
-template <int S>
+template <int S, int FORM>
 __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwsep_theta_consts& th, long long wt,
                                              float* __restrict__ cs, float* __restrict__ kf,
                                              const float* __restrict__ thi, const float* __restrict__ tlo,
-                                             double (&acc)[1 + S])
+                                             const float4* __restrict__ ltab, double (&acc)[1 + S])
 {
     constexpr int CW = ColDF<S>::W;
     constexpr int DFP = mwsep_df_tile_p(S); /* points per lane per group */
@@ -129,6 +139,7 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     __syncwarp();
 
     const D::df2 r0 = D::dup(D::from_double(th.r0));
+    const D::df2 al = D::dup(D::from_double(th.alpha)), ad3 = D::dup(D::from_double(th.alpha_delta3));
     const int C = A.convolve;
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
@@ -206,8 +217,14 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
             {
                 const D::df2 rg = D::sqrt2(D::sq_scale_add2(B2, D::add_fast2(r[q], nrb), Db));
                 const D::df2 sum = D::add_fast2(rg, r0);
-                const D::df2 den = D::mul2(rg, D::mul2(sum, D::sqr2(sum)));
-                const D::df2 v = D::div2(w[q], den);
+                D::df2 v;
+                if constexpr (FORM == kFormHern)
+                    v = D::div2(w[q], D::mul2(rg, D::mul2(sum, D::sqr2(sum))));
+                else /* w / (rg^alpha (rg + r0)^(3 - alpha + delta)) = w 2^-(alpha log2 rg + ad3 log2(rg + r0)) */
+                {
+                    const D::df2 E = D::add_fast2(D::mul2(al, D::log2_2(rg, ltab)), D::mul2(ad3, D::log2_2(sum, ltab)));
+                    v = D::mul_raw2(w[q], D::exp2_2(D::mk2(D::pneg(E.hi), D::pneg(E.lo)), thi, tlo));
+                }
                 if (q == 0)
                     pb = D::lazy_start2(v);
                 else
@@ -242,32 +259,39 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     __syncwarp();
 }
 
-template <int S>
+template <int S, int FORM>
 __global__ void __launch_bounds__(DfShape<S>::block, DfShape<S>::min_blocks) integral_df_kernel(const mwsep_area_dev A,
                                                                 const mwsep_theta_consts* __restrict__ thetas,
                                                                 double2* __restrict__ partials, long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (1 + S) * 32];
     constexpr int kBlock = DfShape<S>::block;
     __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * ColDF<S>::W];
+    static_assert(sizeof(cs) >= 2 * (1 + S) * 32 * sizeof(double), "the block reduction reuses cs");
     __shared__ float kf[kBlock / 32][mwsep::kTileCols * kSP(S)];
     __shared__ float thi[D::kExp2Table], tlo[D::kExp2Table];
+    __shared__ float4 ltab[FORM == kFormGeneral ? D::kLog2Table : 1];
     mwsep::f64::load_theta(th, thetas + blockIdx.y);
     for (int j = threadIdx.x; j < D::kExp2Table; j += kBlock)
     {
         thi[j] = c_exp2_tab[j].x;
         tlo[j] = c_exp2_tab[j].y;
     }
+    if (FORM == kFormGeneral)
+        for (int j = threadIdx.x; j < D::kLog2Table; j += kBlock) ltab[j] = c_log2_tab[j];
     __syncthreads();
+    if (!df_form_is(th, FORM)) return; /* the other form's launch covers this theta (whole block) */
     double acc[1 + S];
 #pragma unroll
     for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
     const int warp = threadIdx.x >> 5;
     const long long warps = (long long)gridDim.x * (kBlock / 32);
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
-        warp_tile_df<S>(A, th, wt, cs[warp], kf[warp], thi, tlo, acc);
-    /* block reduction into compensated pairs */
+        warp_tile_df<S, FORM>(A, th, wt, cs[warp], kf[warp], thi, tlo, ltab, acc);
+    /* block reduction into compensated pairs, in cs once every warp is done
+     * with its tiles */
+    __syncthreads();
+    double* red = reinterpret_cast<double*>(&cs[0][0]);
     mwsep::comp_sum cacc[1 + S];
 #pragma unroll
     for (int k = 0; k < 1 + S; ++k)
@@ -293,14 +317,24 @@ int launch(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_la
     const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
     double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
-    integral_df_kernel<S><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+    if (sh->bg_form == 2)
+        integral_df_kernel<S, kFormGeneral><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+    else
+        integral_df_kernel<S, kFormHern><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
     return (int)cudaGetLastError();
 }
 
+/* Resident blocks per SM: the smaller of the two forms' (one grid serves both). */
 template <int S>
 cudaError_t occupancy(int* b)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, integral_df_kernel<S>, DfShape<S>::block, 0);
+    int b0 = 0, b2 = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, integral_df_kernel<S, kFormHern>,
+                                                                  DfShape<S>::block, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, integral_df_kernel<S, kFormGeneral>, DfShape<S>::block, 0);
+    *b = b0 < b2 ? b0 : b2;
+    return e;
 }
 
 /* Per-star double-float table [C][N]: {r_hi, r_lo, qw_hi, qw_lo}. */
@@ -322,7 +356,7 @@ __global__ void star_df_table_kernel(long long total, const double* __restrict__
  * nearest the stream's closest approach, found in FP32), the points' terms
  * summed in runs of eight, and the mixture weights and log10 sums in FP64
  * (likelihood_finish, shared with the FP64 kernel). */
-template <int S>
+template <int S, int FORM>
 __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_dev St, const float4* __restrict__ pdf,
                                                             const mwsep_theta_consts* __restrict__ thetas,
                                                             const double* __restrict__ integrals,
@@ -332,9 +366,13 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (3 + SP) * 32];
     __shared__ float2 tab[D::kExp2Table];
+    __shared__ float4 ltab[FORM == kFormGeneral ? D::kLog2Table : 1];
     mwsep::f64::load_theta(th, thetas + blockIdx.y);
     for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x) tab[j] = c_exp2_tab[j];
+    if (FORM == kFormGeneral)
+        for (int j = threadIdx.x; j < D::kLog2Table; j += blockDim.x) ltab[j] = c_log2_tab[j];
     __syncthreads();
+    if (!df_form_is(th, FORM)) return; /* the other form's launch covers this theta (whole block) */
     const double* I = integrals + (size_t)blockIdx.y * (1 + th.n_streams);
     mwsep::comp_sum acc[3 + SP];
 #pragma unroll
@@ -342,6 +380,7 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
     constexpr double kLog2e = 1.4426950408889634073599246810018921;
     const int N = St.n_stars, C = St.convolve;
     const df r0 = D::from_double(th.r0);
+    const df al = D::from_double(th.alpha), ad3 = D::from_double(th.alpha_delta3);
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
     {
         const double* g = St.geom + 4 * (size_t)s0;
@@ -394,7 +433,13 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
                 const df r = D::mk(v.x, v.y), w = D::mk(v.z, v.w);
                 const df rg = D::sqrt(D::sq_scale_add(B2, D::add_fast(r, nrb), Db));
                 const df sum = D::add_fast(rg, r0);
-                D::lazy_add(pb, D::div(w, D::mul(rg, D::mul(sum, D::sqr(sum)))));
+                if constexpr (FORM == kFormHern)
+                    D::lazy_add(pb, D::div(w, D::mul(rg, D::mul(sum, D::sqr(sum)))));
+                else
+                {
+                    const df E = D::add_fast(D::mul(al, D::log2(rg, ltab)), D::mul(ad3, D::log2(sum, ltab)));
+                    D::lazy_add(pb, D::mul_raw(w, D::exp2(D::neg(E), tab)));
+                }
 #pragma unroll
                 for (int s = 0; s < S; ++s)
                 {
@@ -440,7 +485,10 @@ int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_
 {
     const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
     dim3 g(sh->grid, sh->n_theta);
-    likelihood_df_kernel<S><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
+    if (sh->bg_form == 2)
+        likelihood_df_kernel<S, kFormGeneral><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
+    else
+        likelihood_df_kernel<S, kFormHern><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
     return (int)cudaGetLastError();
 }
 
@@ -486,20 +534,23 @@ __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts
 }
 
 /* Element-wise evaluation of the double-float primitives for the tests:
- * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker), 5 x y^2 + z;
- * ops 10-15 the same through the packed (two values at once) versions;
+ * op 0 exp2(x), 1 sqrt(x), 2 x / y, 3 x * y, 4 x + y (Dekker), 5 x y^2 + z,
+ * 6 log2(x); ops 10-16 the same through the packed (two values at once)
+ * versions;
  * inputs are doubles split into pairs, results returned as hi + lo in FP64. */
 __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, const double* __restrict__ y,
                                const double* __restrict__ z, double* __restrict__ out)
 {
     __shared__ float2 tab[D::kExp2Table];
     __shared__ float thi[D::kExp2Table], tlo[D::kExp2Table];
+    __shared__ float4 ltab[D::kLog2Table];
     for (int j = threadIdx.x; j < D::kExp2Table; j += blockDim.x)
     {
         tab[j] = c_exp2_tab[j];
         thi[j] = c_exp2_tab[j].x;
         tlo[j] = c_exp2_tab[j].y;
     }
+    for (int j = threadIdx.x; j < D::kLog2Table; j += blockDim.x) ltab[j] = c_log2_tab[j];
     __syncthreads();
     if (op >= 10)
     {
@@ -521,7 +572,8 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
             case 12: r = D::div2(a, b); break;
             case 13: r = D::mul2(a, b); break;
             case 14: r = D::add_fast2(a, b); break;
-            default: r = D::sq_scale_add2(a, b, c); break;
+            case 15: r = D::sq_scale_add2(a, b, c); break;
+            default: r = D::log2_2(a, ltab); break;
             }
             out[ia] = (double)r.hi.x + (double)r.lo.x;
             out[ib] = (double)r.hi.y + (double)r.lo.y;
@@ -539,7 +591,8 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
         case 2: r = D::div(a, b); break;
         case 3: r = D::mul(a, b); break;
         case 4: r = D::add_fast(a, b); break;
-        default: r = D::sq_scale_add(a, b, D::from_double(z[i])); break;
+        case 5: r = D::sq_scale_add(a, b, D::from_double(z[i])); break;
+        default: r = D::log2(a, ltab); break;
         }
         out[i] = (double)r.hi + (double)r.lo;
     }
@@ -550,8 +603,8 @@ std::mutex g_table_mu;
 
 } // namespace
 
-/* Upload the 2^(j/1024) table to `device` (once per device; contexts on
- * other threads may ask at the same time). */
+/* Upload the 2^(j/1024) and log2 tables to `device` (once per device;
+ * contexts on other threads may ask at the same time). */
 extern "C" int mwsep_df_prepare(int device)
 {
     if (device < 0 || device >= 64) return 1;
@@ -564,9 +617,17 @@ extern "C" int mwsep_df_prepare(int device)
         const mwsep::dfl::df v = mwsep::dfl::from_double(exp2((double)j / D::kExp2Table));
         t[j] = make_float2(v.hi, v.lo);
     }
+    float4 lt[D::kLog2Table];
+    for (int j = 0; j < D::kLog2Table; ++j)
+    {
+        const double c = 1.0 + (double)j / D::kLog2Table;
+        const mwsep::dfl::df l = mwsep::dfl::from_double(log2(c)), r = mwsep::dfl::from_double(1.0 / c);
+        lt[j] = make_float4(l.hi, l.lo, r.hi, r.lo);
+    }
     int prev = 0;
     if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) return 1;
-    const cudaError_t e = cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t));
+    cudaError_t e = cudaMemcpyToSymbol(c_exp2_tab, t, sizeof(t));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_log2_tab, lt, sizeof(lt));
     cudaSetDevice(prev);
     if (e != cudaSuccess) return 1;
     g_table_ready[device].store(true, std::memory_order_release);
@@ -621,7 +682,7 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
 extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z,
                              double* out)
 {
-    if (op < 0 || (op > 5 && op < 10) || op > 15 || n < 0 || (n > 0 && (!x || !y || !z || !out)))
+    if (op < 0 || (op > 6 && op < 10) || op > 16 || n < 0 || (n > 0 && (!x || !y || !z || !out)))
         return MWSEP_ERR_ARG;
     if (n == 0) return MWSEP_OK;
     if (cudaSetDevice(device) != cudaSuccess || mwsep_df_prepare(device)) return MWSEP_ERR_CUDA;

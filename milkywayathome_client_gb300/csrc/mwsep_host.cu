@@ -794,17 +794,20 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     if (c->h_theta.ensure(th_bytes)) return mwsep_fail(MWSEP_ERR_NOMEM);
     mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
     for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
-    /* the double-float integral covers the alpha = delta = 1 background,
-     * with or without the aux profile (any stream count), its likelihood up
-     * to 4 streams (the FP64 likelihood beyond); any other background form
-     * runs in native FP64 */
-    bool df_aux = false;
+    /* the double-float kernels cover alpha = delta = 1 (with or without the
+     * aux profile) and general alpha/delta, any stream count (the likelihood
+     * kernel up to 4 streams, the FP64 likelihood beyond); a batch with a
+     * q = 0 theta runs in native FP64.  One launch per form present, each
+     * skipping the other form's thetas. */
+    bool df_aux = false, df_hern = false, df_general = false;
     if (precision == MWSEP_PLAIN_DF)
         for (int i = 0; i < B; ++i)
         {
             const int form = mwsep_bg_form(&hth[i]);
-            if (form > 1) precision = MWSEP_PLAIN_F64;
+            if (form == 3) precision = MWSEP_PLAIN_F64;
             df_aux = df_aux || form == 1;
+            df_hern = df_hern || form <= 1;
+            df_general = df_general || form == 2;
         }
     const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4;
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
@@ -863,9 +866,14 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         }
         else if (precision == MWSEP_PLAIN_DF)
         {
-            CK(mwsep_launch_integral_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
-                                        c->d_partials.as<double2>(), st));
-            ++launches;
+            for (int form = 0; form <= 2; form += 2)
+            {
+                if (!(form == 0 ? df_hern : df_general)) continue;
+                sh.bg_form = form;
+                CK(mwsep_launch_integral_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
+                                            c->d_partials.as<double2>(), st));
+                ++launches;
+            }
             if (df_aux)
             {
                 CK(mwsep_launch_aux_area_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
@@ -894,8 +902,16 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     lk.grid = t.lk_grid;
     lk.area_index = 0;
     if (df_likelihood)
-        CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
-                                      &lk, d_ints, c->d_lkpartials.as<double2>(), st));
+    {
+        for (int form = 0; form <= 2; form += 2)
+        {
+            if (!(form == 0 ? df_hern : df_general)) continue;
+            lk.bg_form = form;
+            CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
+                                          &lk, d_ints, c->d_lkpartials.as<double2>(), st));
+            if (form == 0 && df_general) ++launches; /* the second one is counted below */
+        }
+    }
     else if (precision != MWSEP_MIXED_F32)
         CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));

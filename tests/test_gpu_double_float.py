@@ -3,8 +3,9 @@ outputs at the plain form's tolerances (1e-12 relative on every integral,
 1e-12 absolute on the log-likelihood) -- every golden case, the aux profile
 included -- against the native FP64 kernel at full size, batch == single,
 engine requests and gradients, first use from several threads, the device
-memory budget, and its limits (general alpha/delta and q = 0 run in native
-FP64, beyond 4 streams the likelihood does; the autotuner refuses it)."""
+memory budget, a batch mixing the two background forms, and its limits
+(q = 0 runs in native FP64, beyond 4 streams the likelihood does; the
+autotuner refuses it)."""
 import math
 import os
 
@@ -76,11 +77,7 @@ def test_double_float_matches_native_fp64_at_full_size(gpu_ctx):
 def test_double_float_limits(gpu_ctx):
     import milkywayathome_client_gb300 as mw
     from milkywayathome_client_gb300 import native as N
-    # general alpha/delta and q = 0 run in native FP64: identical bits
-    g = _setup(gpu_ctx, "general_alpha_delta")
-    a = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64)
-    b = gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF)
-    assert a.integrals == b.integrals and a.likelihood == b.likelihood
+    # q = 0 runs in native FP64: identical bits
     g = _setup(gpu_ctx, "three_streams")
     theta = list(g["theta"])
     theta[0] = 0.0  # q
@@ -227,3 +224,25 @@ def test_double_float_first_use_from_threads():
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     assert r.stdout.startswith("ok")
+
+
+def test_double_float_mixed_forms_batch(gpu_ctx):
+    """General alpha/delta and alpha = delta = 1 thetas in one batch: each
+    form's kernel skips the other's thetas, so every result equals its
+    single evaluation bit for bit and stays within the plain bounds of the
+    native FP64 kernel."""
+    import milkywayathome_client_gb300 as mw
+    g = _setup(gpu_ctx, "general_alpha_delta")
+    base = np.asarray(g["theta"], dtype=np.float64)
+    hern = base.copy()
+    hern[0], hern[3] = 1.0, 1.0  # alpha, delta
+    thetas = [base, hern, base * (1 + 1e-3), hern * (1 - 1e-3)]
+    thetas[3][0], thetas[3][3] = 1.0, 1.0
+    batch = gpu_ctx.evaluate_batch(thetas, mw.MWSEP_PLAIN_DF)
+    for t, b in zip(thetas, batch):
+        one = gpu_ctx.evaluate(t, mw.MWSEP_PLAIN_DF)
+        assert one.integrals == b.integrals and one.likelihood == b.likelihood
+        f64 = gpu_ctx.evaluate(t, mw.MWSEP_PLAIN_F64)
+        for x, y in zip(b.integrals, f64.integrals):
+            assert _close_rel(x, y, REL), (x, y)
+        assert abs(b.likelihood - f64.likelihood) <= ABS_LOGL
