@@ -175,10 +175,9 @@ enum
     MWSEP_MIXED_F32 = 1,
     /* The plain form's accuracy (1e-12 relative on the integrals) computed in
      * double-float arithmetic -- pairs of FP32 values, about 48 bits -- on
-     * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Covers the
-     * alpha = delta = 1 background with or without the aux profile and
-     * general alpha/delta (its likelihood in double-float up to 4 streams,
-     * in FP64 beyond); q = 0 is evaluated as MWSEP_PLAIN_F64.
+     * the FP32 pipes, which GB300 runs ~74x faster than FP64.  Every
+     * background form; the likelihood in double-float up to 4 streams, in
+     * FP64 beyond.
      * Single-wedge evaluations and
      * batches, engine requests (each wedge's requests as one batch), the
      * server and the gradient/Hessian calls; the engine autotuner takes the

@@ -23,10 +23,11 @@
  * Per lane the group sums are double-float; per group they go to FP64
  * (times ids), across blocks the usual compensated FP64 reduction.
  *
- * Background forms: alpha = delta = 1, with or without the aux profile
- * (whose column-independent share aux_area_kernel adds), up to 8 streams
- * (the likelihood kernel below up to 4; the host runs the FP64 likelihood
- * beyond); the host runs any other form through the native FP64 kernels.
+ * Background forms: alpha = delta = 1 with or without the aux profile,
+ * general alpha/delta, and q = 0 (the aux share and the q = 0 background
+ * are column-independent: aux_area_kernel adds them), up to 8 streams (the
+ * likelihood kernel below up to 4; the host runs the FP64 likelihood
+ * beyond).
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -56,12 +57,14 @@ struct DfShape
     static constexpr int min_blocks = S >= 4 ? 4 : 2;
 };
 /* Background forms of the double-float kernels: alpha = delta = 1 (the aux
- * profile's share added separately) or general alpha/delta; each launch
- * skips the thetas of the other form. */
-constexpr int kFormHern = 0, kFormGeneral = 2;
+ * profile's share added separately), general alpha/delta, or none (q = 0:
+ * the background is -1 per cell, added separately); each launch skips the
+ * thetas of the other forms. */
+constexpr int kFormHern = 0, kFormGeneral = 2, kFormNone = 3;
 __device__ __forceinline__ bool df_form_is(const mwsep_theta_consts& th, int form)
 {
-    return (mwsep_bg_form(&th) == 2) == (form == kFormGeneral);
+    const int f = mwsep_bg_form(&th);
+    return form == kFormHern ? f <= 1 : f == form;
 }
 static_assert(MWSEP_DF_TILE_P % 2 == 0, "points are taken in pairs");
 
@@ -211,6 +214,8 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
         {
             const float* c = cs + j * CW;
             const D::df2 B2 = D::dup(get<S>(c, 0)), nrb = D::dup(D::neg(get<S>(c, 1))), Db = D::dup(get<S>(c, 2));
+            if constexpr (FORM != kFormNone)
+            {
             D::lazy_sum2 pb;
 #pragma unroll
             for (int q = 0; q < NPR; ++q)
@@ -231,6 +236,7 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
                     D::lazy_add2(pb, v);
             }
             bg = D::add_fast2(bg, D::lazy_end2(pb));
+            }
 #pragma unroll 1
             for (int s = 0; s < S; ++s)
             {
@@ -317,23 +323,28 @@ int launch(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_la
     const long long theta_stride = (long long)sh->n_areas * sh->grid * ncomp;
     double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
-    if (sh->bg_form == 2)
+    if (sh->bg_form == kFormGeneral)
         integral_df_kernel<S, kFormGeneral><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+    else if (sh->bg_form == kFormNone)
+        integral_df_kernel<S, kFormNone><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
     else
         integral_df_kernel<S, kFormHern><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
     return (int)cudaGetLastError();
 }
 
-/* Resident blocks per SM: the smaller of the two forms' (one grid serves both). */
+/* Resident blocks per SM: the smallest of the forms' (one grid serves all). */
 template <int S>
 cudaError_t occupancy(int* b)
 {
-    int b0 = 0, b2 = 0;
+    int b0 = 0, b2 = 0, b3 = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, integral_df_kernel<S, kFormHern>,
                                                                   DfShape<S>::block, 0);
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, integral_df_kernel<S, kFormGeneral>, DfShape<S>::block, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, integral_df_kernel<S, kFormNone>, DfShape<S>::block, 0);
     *b = b0 < b2 ? b0 : b2;
+    *b = *b < b3 ? *b : b3;
     return e;
 }
 
@@ -435,7 +446,7 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
                 const df sum = D::add_fast(rg, r0);
                 if constexpr (FORM == kFormHern)
                     D::lazy_add(pb, D::div(w, D::mul(rg, D::mul(sum, D::sqr(sum)))));
-                else
+                else if constexpr (FORM == kFormGeneral)
                 {
                     const df E = D::add_fast(D::mul(al, D::log2(rg, ltab)), D::mul(ad3, D::log2(sum, ltab)));
                     D::lazy_add(pb, D::mul_raw(w, D::exp2(D::neg(E), tab)));
@@ -451,8 +462,9 @@ __global__ void __launch_bounds__(256) likelihood_df_kernel(const mwsep_stars_de
 #pragma unroll
             for (int s = 0; s < S; ++s) st[s] = D::add_fast(st[s], D::lazy_end(ps[s]));
         }
-        /* the aux profile, point by point in FP64 as the reference adds it */
-        double bgd = (double)bg.hi + (double)bg.lo;
+        /* the aux profile, point by point in FP64 as the reference adds it;
+         * q = 0: the background is -1 (cpu/evaluation_optimized.c:213-216) */
+        double bgd = FORM == kFormNone ? -1.0 : (double)bg.hi + (double)bg.lo;
         if (th.aux && th.bg_mode == 0)
         {
             double v = 0.0;
@@ -485,27 +497,33 @@ int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_
 {
     const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
     dim3 g(sh->grid, sh->n_theta);
-    if (sh->bg_form == 2)
+    if (sh->bg_form == kFormGeneral)
         likelihood_df_kernel<S, kFormGeneral><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
+    else if (sh->bg_form == kFormNone)
+        likelihood_df_kernel<S, kFormNone><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
     else
         likelihood_df_kernel<S, kFormHern><<<g, sh->block, 0, st>>>(*St, pdf, th, integrals, partials, theta_stride);
     return (int)cudaGetLastError();
 }
 
-/* The aux profile's share of an area integral (form-1 problems: alpha =
- * delta = 1 plus qw (a g^2 + b g + c), cpu/evaluation_optimized.c:234-239).
- * That term does not depend on the column, so summed over the area's cells
- * as :498-520 does (times reff, times V = irv_k ids_j) it is
- *   mu_steps * sum_j ids_j * sum_k irv_k reff_k sum_n qw_kn (a g2_kn + b g_kn + c),
+/* The column-independent background shares of an area integral, summed
+ * over the area's cells as cpu/evaluation_optimized.c:498-520 does (times
+ * V = irv_k ids_j):
+ *  - the aux profile (form 1: alpha = delta = 1 plus qw (a g^2 + b g + c),
+ *    :234-239, times reff):
+ *      mu_steps * sum_j ids_j * sum_k irv_k reff_k sum_n qw_kn (a g2_kn + b g_kn + c);
+ *  - q = 0 (form 3: bg = -1 per cell, no reff, :213-216):
+ *      mu_steps * sum_j ids_j * sum_k irv_k * (-1).
  * O(R C) work in FP64, added (TwoSum) to block 0's background partial of
  * the area after the double-float kernel has written it.  One block per
- * theta; thetas without the aux profile are left alone. */
+ * theta; thetas of the other forms are left alone. */
 __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts* __restrict__ thetas,
                                 double2* __restrict__ partials, long long theta_stride)
 {
     __shared__ double red[2 * 2 * 32];
     const mwsep_theta_consts* th = thetas + blockIdx.y;
-    if (!th->aux || th->bg_mode != 0) return; /* uniform per block */
+    const int form = mwsep_bg_form(th);
+    if (form != 1 && form != 3) return; /* uniform per block */
     const double a = th->bg_a, b = th->bg_b, c = th->bg_c;
     mwsep::comp_sum acc[2];
     acc[0].zero();
@@ -513,6 +531,11 @@ __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts
     const int C = A.convolve;
     for (int k = threadIdx.x; k < A.r_steps; k += blockDim.x)
     {
+        if (form == 3)
+        {
+            acc[0].add(-A.irv[k]);
+            continue;
+        }
         const size_t row = (size_t)k * C;
         double v = 0.0;
         for (int n = 0; n < C; ++n)

@@ -794,20 +794,20 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     if (c->h_theta.ensure(th_bytes)) return mwsep_fail(MWSEP_ERR_NOMEM);
     mwsep_theta_consts* hth = c->h_theta.as<mwsep_theta_consts>();
     for (int i = 0; i < B; ++i) theta_consts(p, thetas + (size_t)i * P, hth[i]);
-    /* the double-float kernels cover alpha = delta = 1 (with or without the
-     * aux profile) and general alpha/delta, any stream count (the likelihood
-     * kernel up to 4 streams, the FP64 likelihood beyond); a batch with a
-     * q = 0 theta runs in native FP64.  One launch per form present, each
-     * skipping the other form's thetas. */
-    bool df_aux = false, df_hern = false, df_general = false;
+    /* the double-float kernels cover every background form (alpha = delta
+     * = 1 with or without the aux profile, general alpha/delta, q = 0) and
+     * any stream count (the likelihood kernel up to 4 streams, the FP64
+     * likelihood beyond).  One launch per form present, each skipping the
+     * other forms' thetas. */
+    bool df_aux = false, df_hern = false, df_general = false, df_none = false;
     if (precision == MWSEP_PLAIN_DF)
         for (int i = 0; i < B; ++i)
         {
             const int form = mwsep_bg_form(&hth[i]);
-            if (form == 3) precision = MWSEP_PLAIN_F64;
             df_aux = df_aux || form == 1;
             df_hern = df_hern || form <= 1;
             df_general = df_general || form == 2;
+            df_none = df_none || form == 3;
         }
     const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4;
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
@@ -866,15 +866,15 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         }
         else if (precision == MWSEP_PLAIN_DF)
         {
-            for (int form = 0; form <= 2; form += 2)
+            for (int form : {0, 2, 3})
             {
-                if (!(form == 0 ? df_hern : df_general)) continue;
+                if (!(form == 0 ? df_hern : form == 2 ? df_general : df_none)) continue;
                 sh.bg_form = form;
                 CK(mwsep_launch_integral_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
                                             c->d_partials.as<double2>(), st));
                 ++launches;
             }
-            if (df_aux)
+            if (df_aux || df_none)
             {
                 CK(mwsep_launch_aux_area_df(&v, c->d_theta.as<mwsep_theta_consts>(), &sh,
                                             c->d_partials.as<double2>(), st));
@@ -903,13 +903,14 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     lk.area_index = 0;
     if (df_likelihood)
     {
-        for (int form = 0; form <= 2; form += 2)
+        int n_forms = 0;
+        for (int form : {0, 2, 3})
         {
-            if (!(form == 0 ? df_hern : df_general)) continue;
+            if (!(form == 0 ? df_hern : form == 2 ? df_general : df_none)) continue;
             lk.bg_form = form;
             CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
                                           &lk, d_ints, c->d_lkpartials.as<double2>(), st));
-            if (form == 0 && df_general) ++launches; /* the second one is counted below */
+            if (n_forms++) ++launches; /* the first one is counted below */
         }
     }
     else if (precision != MWSEP_MIXED_F32)

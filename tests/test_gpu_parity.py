@@ -178,6 +178,10 @@ def test_q_zero_background_integral(gpu_ctx, oracle_built, name):
     want = oracle_built.Oracle(pf, sf).integrals(theta)[0][0]
     r64 = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_F64)
     r32 = gpu_ctx.evaluate(theta, mw.MWSEP_MIXED_F32)
+    rdf = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_DF)
     assert _close_rel(r64.background_integral, want, REL_INT_F64), (r64.background_integral, want)
+    assert _close_rel(rdf.background_integral, want, REL_INT_F64), (rdf.background_integral, want)
+    for x, y in zip(rdf.stream_integrals, r64.stream_integrals):  # same (current-point) stream terms
+        assert _close_rel(x, y, REL_INT_F64), (x, y)
     # the compensated form sums the volumes rounded to FP32 once each
     assert _close_rel(r32.background_integral, want, 1e-6), (r32.background_integral, want)
