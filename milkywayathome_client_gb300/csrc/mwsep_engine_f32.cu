@@ -40,8 +40,7 @@ __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta
     if (A.warp_items)
     {
         const int warp = threadIdx.x >> 5;
-        constexpr int CW = PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N;
-        float* mine = cs + warp * mwsep::kTileCols * CW;
+        float* mine = cs + warp * TileSmem<S>::N;
         for (long long wt = t.item_begin + warp; wt < t.item_end; wt += blockDim.x >> 5)
         {
             if constexpr (PackedTile<S>::ok)
@@ -84,8 +83,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
     __shared__ double red[2 * (1 + S) * 32];
-    __shared__ __align__(16) float cs[(kBlock / 32) * mwsep::kTileCols *
-                                      (PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N)];
+    __shared__ __align__(16) float cs[(kBlock / 32) * TileSmem<S>::N];
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * G + 2];
     for (;;)

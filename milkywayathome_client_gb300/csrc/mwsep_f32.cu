@@ -56,8 +56,7 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
 {
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (1 + S) * 32];
-    constexpr int CW = PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N;
-    __shared__ __align__(16) float cs[kBlock / 32][mwsep::kTileCols * CW];
+    __shared__ __align__(16) float cs[kBlock / 32][TileSmem<S>::N];
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     if (mwsep_bg_form(&th) != FORM) return;

@@ -116,8 +116,117 @@ struct Col
  *               L = -2 B2 rb_lo (kept in the rb_lo slot), D = Db + B2 rb_lo^2;
  *   streams     offsets d = rb_hi - rs.
  * The same quadratics, with the small rb_lo folded into the constants. */
+/* Range of the stream exponents: FP32 holds 2^+-126, an FP64 integral goes
+ * far lower, and a stream whose closest approach is far from a wedge has
+ * every term below 2^-126 (a zero integral, a NaN likelihood).  So per item
+ * (a column run, a warp tile or a star) each stream's base-2 exponent is
+ * shifted by eref = floor of its largest value over the item's r range --
+ * k2 (r* - rs)^2 + k0 at r* = rs clamped into [r_lo, r_hi] -- formed in FP64
+ * before the constant is rounded to float, and the item's sums are scaled
+ * back by 2^eref in FP64.  StreamExp carries the two FP64 values. */
+template <int S>
+struct StreamExp
+{
+    double amax[SArr<S>::N], k0c[SArr<S>::N];
+};
+
+constexpr int kErefFloor = -1100; /* 2^-1100 is 0 in FP64 */
+
+/* floor(a) clamped at kErefFloor (also for -inf and NaN) */
+__device__ __forceinline__ int exp_ref(double a) { return (a > (double)kErefFloor) ? (int)floor(a) : kErefFloor; }
+/* 2^e: a normal double from its exponent bits, ldexp below that */
+__device__ __forceinline__ double exp_scale(int e)
+{
+    return e > -1023 ? __longlong_as_double((long long)(e + 1023) << 52) : (e > kErefFloor ? ldexp(1.0, e) : 0.0);
+}
+
+/* The shifted constants into cc (switched-off streams keep -1e30). */
+template <int S>
+__device__ __forceinline__ void shift_exponents(const mwsep_theta_consts& th, const StreamExp<S>& se,
+                                                const int (&eref)[SArr<S>::N], Col<S>& cc)
+{
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+        if (s < th.n_streams && th.stream_on[s]) cc.k0c[s] = (float)fmax(se.k0c[s] - (double)eref[s], -1.0e30);
+}
+
+/* r range of the convolution points of r-bins [k0, k1) of an area: the
+ * points increase with the bin and, within a bin, with the Gauss-Legendre
+ * node, so the chunk's corner points bound it. */
+__device__ __forceinline__ void chunk_r_range(const mwsep_area_dev& A, int k0, int k1, double& lo, double& hi)
+{
+    const int C = A.convolve;
+    const size_t n = (size_t)A.r_steps * C;
+    (void)n; /* used by the index checks only */
+    const double a = A.r_point[MWSEP_IDX((size_t)k0 * C, n, 5)];
+    const double b = A.r_point[MWSEP_IDX((size_t)k0 * C + C - 1, n, 5)];
+    const double c = A.r_point[MWSEP_IDX((size_t)(k1 - 1) * C, n, 5)];
+    const double d = A.r_point[MWSEP_IDX((size_t)(k1 - 1) * C + C - 1, n, 5)];
+    lo = fmin(fmin(a, b), fmin(c, d));
+    hi = fmax(fmax(a, b), fmax(c, d));
+}
+
+/* The warp tiles' estimate of each stream's largest exponent over an r
+ * range, in FP32: the stream geometry of column_consts below at single
+ * precision (error well below 1 in the exponent for |k0| < 2^20; only its
+ * floor is used, and a term up to 2^5 stays in range). */
+template <int S>
+__device__ __forceinline__ void stream_amax_f32(const double* g, const mwsep_theta_consts& th, float r_lo,
+                                                float r_hi, float (&amax)[SArr<S>::N])
+{
+    const float bsin = (float)g[0], bcos = (float)g[1], lsin = (float)g[2], lcos = (float)g[3];
+    const float u0 = bcos * lcos, u1 = bcos * lsin, u2 = bsin;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        amax[s] = -INFINITY;
+        if (s < th.n_streams && th.stream_on[s])
+        {
+            const float a0 = th.af[s][0], a1 = th.af[s][1], a2 = th.af[s][2];
+            const float c0 = th.cf[s][0], c1 = th.cf[s][1], c2 = th.cf[s][2];
+            const float au = a0 * u0 + a1 * u1 + a2 * u2;
+            const float p0 = u0 - au * a0, p1 = u1 - au * a1, p2 = u2 - au * a2;
+            const float ac = a0 * c0 + a1 * c1 + a2 * c2;
+            const float q0 = c0 - ac * a0, q1 = c1 - ac * a1, q2 = c2 - ac * a2;
+            const float A2 = p0 * p0 + p1 * p1 + p2 * p2;
+            const float rs = (A2 > 1e-30f) ? (p0 * q0 + p1 * q1 + p2 * q2) / A2 : 0.f;
+            const float e0 = q0 - rs * p0, e1 = q1 - rs * p1, e2 = q2 - rs * p2;
+            const float rc = fminf(fmaxf(rs, r_lo), r_hi) - rs;
+            amax[s] = th.kf[s] * (A2 * rc * rc + (e0 * e0 + e1 * e1 + e2 * e2));
+        }
+    }
+}
+
+/* A warp tile's per-stream eref: the FP32 estimate on each live column (one
+ * per lane), the warp's maximum, floored; lane 0 also leaves ids_nu 2^eref
+ * in shared memory for the group hand-offs. */
+template <int S>
+__device__ __forceinline__ void tile_erefs(const mwsep_area_dev& A, const mwsep_theta_consts& th, int k0, int k1,
+                                           const double* g, bool live, int lane, double idsv, double* tscale,
+                                           int (&eref)[SArr<S>::N])
+{
+    double r_lo, r_hi;
+    chunk_r_range(A, k0, k1, r_lo, r_hi);
+    float am[SArr<S>::N];
+#pragma unroll
+    for (int s = 0; s < S; ++s) am[s] = -INFINITY;
+    if (live) stream_amax_f32<S>(g, th, (float)r_lo, (float)r_hi, am);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        float m = am[s];
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        eref[s] = exp_ref((double)m);
+        if (lane == 0) tscale[s] = idsv * exp_scale(eref[s]);
+    }
+}
+
+/* eref: when given, each stream's exponent constant is shifted by it
+ * (formed in FP64 before the rounding to float). */
 template <int S, bool FROM_HI = false>
-__device__ __forceinline__ void column_consts(const double* g, const mwsep_theta_consts& th, Col<S>& cc)
+__device__ __forceinline__ void column_consts(const double* g, const mwsep_theta_consts& th, Col<S>& cc,
+                                              StreamExp<S>* se = nullptr, double r_lo = 0.0, double r_hi = 0.0,
+                                              const int* eref = nullptr)
 {
     const double bsin = g[0], bcos = g[1], lsin = g[2], lcos = g[3];
     const double u0 = bcos * lcos, u1 = bcos * lsin, u2 = bsin;
@@ -161,7 +270,14 @@ __device__ __forceinline__ void column_consts(const double* g, const mwsep_theta
             cc.k2[s] = (float)k2;
             cc.k2dl[s] = (float)(2.0 * k2 * (double)d_lo);
             /* a switched-off stream gets an exponent far below the FTZ range */
-            cc.k0c[s] = th.stream_on[s] ? (float)(Ds * f + k2 * (double)d_lo * (double)d_lo) : -1.0e30f;
+            const double k0c = Ds * f + k2 * (double)d_lo * (double)d_lo;
+            cc.k0c[s] = th.stream_on[s] ? (float)fmax(k0c - (eref ? (double)eref[s] : 0.0), -1.0e30) : -1.0e30f;
+            if (se)
+            {
+                const double rc = fmin(fmax(rs, r_lo), r_hi) - rs;
+                se->amax[s] = th.stream_on[s] ? k2 * rc * rc + Ds * f : -INFINITY;
+                se->k0c[s] = k0c;
+            }
         }
         else
         {
@@ -169,6 +285,11 @@ __device__ __forceinline__ void column_consts(const double* g, const mwsep_theta
             cc.k2dl[s] = 0.f;
             cc.k0c[s] = -1.0e30f;
             cc.d_hi[s] = 0.f;
+            if (se)
+            {
+                se->amax[s] = -INFINITY;
+                se->k0c[s] = -1.0e30;
+            }
         }
     }
 }
@@ -292,10 +413,17 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const int C = A.convolve;
     const int kc = (int)(item / A.n_cols);
     const int col = (int)(item - (long long)kc * A.n_cols);
-    Col<S> cc;
-    column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1), th, cc);
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    Col<S> cc;
+    StreamExp<S> se;
+    double r_lo, r_hi;
+    chunk_r_range(A, k0, k1, r_lo, r_hi);
+    column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1), th, cc, &se, r_lo, r_hi);
+    int eref[SArr<S>::N];
+#pragma unroll
+    for (int s = 0; s < S; ++s) eref[s] = exp_ref(se.amax[s]);
+    shift_exponents<S>(th, se, eref, cc);
     fkahan kb, ks[SArr<S>::N];
     kb.zero();
 #pragma unroll
@@ -315,7 +443,7 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const double idsj = A.ids[MWSEP_IDX(col % A.nu_steps, A.nu_steps, 3)];
     acc[0] += kb.value() * idsj;
 #pragma unroll
-    for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * idsj;
+    for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * (idsj * exp_scale(eref[s]));
 }
 
 /* ---- warp tiles ----
@@ -397,18 +525,28 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
     const int nu = (int)(rest - (long long)kc * A.nu_steps);
     const int mu0 = mb * mwsep::kTileCols;
     const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
-    if (lane < ncols)
-    {
-        Col<S> cc;
-        column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1), th, cc);
-        store_col<S>(cs + lane * CW, cc);
-    }
-    __syncwarp();
     const int C = A.convolve;
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
-    const int nf = (k1 - k0) * C;
+    /* the column constants, each stream's exponent shifted by the tile's
+     * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
+    double* const tscale = reinterpret_cast<double*>(cs + mwsep::kTileCols * CW);
+    {
+        const bool live = lane < ncols;
+        const double* g =
+            A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + (live ? lane : 0)) * A.nu_steps + nu, A.n_cols, 1);
+        int eref[SArr<S>::N];
+        tile_erefs<S>(A, th, k0, k1, g, live, lane, idsv, tscale, eref);
+        if (live)
+        {
+            Col<S> cc;
+            column_consts<S>(g, th, cc, nullptr, 0.0, 0.0, eref);
+            store_col<S>(cs + lane * CW, cc);
+        }
+    }
+    __syncwarp();
+    const int nf = (k1 - k0) * C;
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
     {
         /* this lane's points of the group; past the tile's end a copy of its
@@ -437,7 +575,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
         }
         if (FORM != BG_NONE) acc[0] += (double)(gb0 + gb1) * idsv;
 #pragma unroll
-        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs0[s] + gs1[s]) * idsv;
+        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs0[s] + gs1[s]) * tscale[s];
     }
     /* q == 0: every cell's background is -irv[k] (times ids, not reff;
      * :213-216, :504), the same for all the tile's columns */
@@ -474,6 +612,17 @@ struct PackedTile
     static constexpr bool ok = S <= 4;
     static constexpr int W = 2 * (4 + 4 * S); /* floats per column: every constant twice */
     static constexpr int P = mwsep::TileP<S>::P; /* points per lane per group */
+};
+
+/* Floats of shared memory per warp for one tile: the columns' constants,
+ * then the tile's per-stream factors ids_nu 2^eref (doubles), read at each
+ * group's hand-off to FP64 instead of held in registers or recomputed (an
+ * FP64 multiply costs ~64 FP32 operations here). */
+template <int S>
+struct TileSmem
+{
+    static constexpr int CW = PackedTile<S>::ok ? PackedTile<S>::W : ColWords<S>::N;
+    static constexpr int N = mwsep::kTileCols * CW + (2 * SArr<S>::N + 3) / 4 * 4;
 };
 
 template <int S>
@@ -585,8 +734,8 @@ __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, c
     }
 }
 
-/* warp_tile with packed arithmetic; cs holds kTileCols * PackedTile<S>::W
- * floats for this warp. */
+/* warp_tile with packed arithmetic; cs holds TileSmem<S>::N floats for
+ * this warp. */
 template <int S, int FORM>
 __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_theta_consts& th,
                                            const BgConsts& bc, long long wt, float* __restrict__ cs,
@@ -604,19 +753,28 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     const int nu = (int)(rest - (long long)kc * A.nu_steps);
     const int mu0 = mb * mwsep::kTileCols;
     const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
-    if (lane < ncols)
-    {
-        Col<S> cc;
-        column_consts<S, true>(A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + lane) * A.nu_steps + nu, A.n_cols, 1),
-                               th, cc);
-        store_col2<S>(cs + lane * CW, cc);
-    }
-    __syncwarp();
     const int C = A.convolve;
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
-    const int nf = (k1 - k0) * C;
+    /* the column constants, each stream's exponent shifted by the tile's
+     * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
+    double* const tscale = reinterpret_cast<double*>(cs + mwsep::kTileCols * CW);
+    {
+        const bool live = lane < ncols;
+        const double* g =
+            A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + (live ? lane : 0)) * A.nu_steps + nu, A.n_cols, 1);
+        int eref[SArr<S>::N];
+        tile_erefs<S>(A, th, k0, k1, g, live, lane, idsv, tscale, eref);
+        if (live)
+        {
+            Col<S> cc;
+            column_consts<S, true>(g, th, cc, nullptr, 0.0, 0.0, eref);
+            store_col2<S>(cs + lane * CW, cc);
+        }
+    }
+    __syncwarp();
+    const int nf = (k1 - k0) * C;
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
     {
         /* pair m = this lane's points g0 + 64 m + lane and g0 + 64 m + 32 + lane;
@@ -654,7 +812,7 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
         for (int s = 0; s < S; ++s) gs[s] = add2(gs[s], gs2[s]);
         if (FORM != BG_NONE) acc[0] += (double)(gb.x + gb.y) * idsv;
 #pragma unroll
-        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs[s].x + gs[s].y) * idsv;
+        for (int s = 0; s < S; ++s) acc[1 + s] += (double)(gs[s].x + gs[s].y) * tscale[s];
     }
     if (FORM == BG_NONE && lane == 0)
     {
@@ -695,7 +853,14 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     const int N = St.n_stars;
     Col<S> cc;
     s0 = (int)MWSEP_IDX(s0, N, 7);
-    column_consts<S>(St.geom + 4 * (size_t)s0, th, cc);
+    /* the star's convolution points span [r_point[0], r_point[C-1]] */
+    StreamExp<S> se;
+    const double ra = St.r_point[s0], rb = St.r_point[(size_t)(St.convolve - 1) * N + s0];
+    column_consts<S>(St.geom + 4 * (size_t)s0, th, cc, &se, fmin(ra, rb), fmax(ra, rb));
+    int eref[SArr<S>::N];
+#pragma unroll
+    for (int s = 0; s < S; ++s) eref[s] = exp_ref(se.amax[s]);
+    shift_exponents<S>(th, se, eref, cc);
     float bgf = 0.f, stf[SArr<S>::N];
     switch (mwsep_bg_form(&th))
     {
@@ -714,7 +879,7 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     {
         if (s < NS)
         {
-            double st_only = (double)stf[s] * ks.st[s];
+            double st_only = (double)stf[s] * exp_scale(eref[s]) * ks.st[s];
             star_prob += st_only;
             acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only * ks.inv_sw);
         }

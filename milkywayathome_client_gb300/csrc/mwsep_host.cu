@@ -325,6 +325,12 @@ void theta_consts(const ProblemHost& base, const double* theta, mwsep_theta_cons
         th.a[s][0] = sin(p.st[s][2]) * cos(p.st[s][3]);
         th.a[s][1] = sin(p.st[s][2]) * sin(p.st[s][3]);
         th.a[s][2] = cos(p.st[s][2]);
+        for (int i = 0; i < 3; ++i)
+        {
+            th.af[s][i] = (float)th.a[s][i];
+            th.cf[s][i] = (float)(th.c[s][i] + (i == 0 ? MW_LBR_R : 0.0));
+        }
+        th.kf[s] = th.stream_on[s] ? (float)(-1.4426950408889634 / th.sigma_sq2[s]) : 0.f;
     }
     th.exp_bg_weight = exp(p.bg_weight);
     double sum = th.exp_bg_weight;

@@ -47,6 +47,12 @@ typedef struct
     double exp_bg_weight;
     double exp_stream_weight[MWSEP_KMAX_STREAMS];
     double sum_exp_weights;           /* already * 0.001 */
+    /* single-precision copies for the compensated warp tiles' estimate of
+     * each stream's exponent range: a_s, c_s + (Sun offset, 0, 0) and
+     * -log2(e) / sigma2_s (0 for a switched-off stream) */
+    float af[MWSEP_KMAX_STREAMS][3];
+    float cf[MWSEP_KMAX_STREAMS][3];
+    float kf[MWSEP_KMAX_STREAMS];
 } mwsep_theta_consts;
 
 /* One integral area on the device. */

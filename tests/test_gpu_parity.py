@@ -185,3 +185,28 @@ def test_q_zero_background_integral(gpu_ctx, oracle_built, name):
         assert _close_rel(x, y, REL_INT_F64), (x, y)
     # the compensated form sums the volumes rounded to FP32 once each
     assert _close_rel(r32.background_integral, want, 1e-6), (r32.background_integral, want)
+
+
+@pytest.mark.parametrize("mu,sigma", [(150.0, 1.0), (200.0, 1.0), (250.0, 0.5), (340.0, 0.5)])
+def test_compensated_far_stream(gpu_ctx, mu, sigma):
+    """A narrow stream moved far from the wedge (integrals down to 1e-120,
+    every density below FP32 range): the compensated form shifts each
+    stream's exponents per tile and per star, so its integrals keep their
+    FP64 magnitude and the log-likelihood stays within 1e-7 of the plain
+    form (without the shift: a zero integral and a NaN likelihood).  The
+    engine path as well."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case("three_streams")
+    _setup(gpu_ctx, "three_streams")
+    theta = np.asarray(g["theta"], dtype=np.float64).copy()
+    theta[3] = mu     # stream 1: mu (degrees)
+    theta[7] = sigma  # stream 1: sigma
+    a = gpu_ctx.evaluate(theta, mw.MWSEP_PLAIN_F64)
+    b = gpu_ctx.evaluate(theta, mw.MWSEP_MIXED_F32)
+    for x, y in zip(b.integrals, a.integrals):
+        assert abs(x - y) <= 2e-6 * abs(y), (x, y)
+    assert abs(b.likelihood - a.likelihood) <= ABS_LOGL_F32, (b.likelihood, a.likelihood)
+    with mw.Context(0) as ctx:
+        wid = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
+        e = ctx.evaluate_requests([(wid, theta)], mw.MWSEP_MIXED_F32)[0]
+    assert abs(e.likelihood - a.likelihood) <= ABS_LOGL_F32, (e.likelihood, a.likelihood)
