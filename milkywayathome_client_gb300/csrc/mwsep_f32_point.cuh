@@ -404,6 +404,23 @@ __device__ __forceinline__ void reduce_and_store(const double (&v)[NC], int ncom
 }
 
 
+/* A thread item's column constants with each stream's exponent shifted by
+ * the item's own eref, out of line (once per item) so its FP64
+ * temporaries do not add to the register pressure of the kernels that
+ * inline the point loops. */
+template <int S>
+__device__ __noinline__ void item_prologue(const mwsep_area_dev& A, const mwsep_theta_consts& th, int col, int k0,
+                                           int k1, Col<S>& cc, int (&eref)[SArr<S>::N])
+{
+    StreamExp<S> se;
+    double r_lo, r_hi;
+    chunk_r_range(A, k0, k1, r_lo, r_hi);
+    column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1), th, cc, &se, r_lo, r_hi);
+#pragma unroll
+    for (int s = 0; s < S; ++s) eref[s] = exp_ref(se.amax[s]);
+    shift_exponents<S>(th, se, eref, cc);
+}
+
 /* One item of an integral: a (mu, nu) column and its run of k_chunk r-bins.
  * Adds the item's background and stream integrals (FP64) into acc. */
 template <int S, int FORM>
@@ -416,14 +433,8 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     const int k0 = kc * A.k_chunk;
     const int k1 = min(k0 + A.k_chunk, A.r_steps);
     Col<S> cc;
-    StreamExp<S> se;
-    double r_lo, r_hi;
-    chunk_r_range(A, k0, k1, r_lo, r_hi);
-    column_consts<S>(A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1), th, cc, &se, r_lo, r_hi);
     int eref[SArr<S>::N];
-#pragma unroll
-    for (int s = 0; s < S; ++s) eref[s] = exp_ref(se.amax[s]);
-    shift_exponents<S>(th, se, eref, cc);
+    item_prologue<S>(A, th, col, k0, k1, cc, eref);
     fkahan kb, ks[SArr<S>::N];
     kb.zero();
 #pragma unroll
@@ -734,6 +745,28 @@ __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, c
     }
 }
 
+/* A packed tile's column constants (one column per lane) and per-stream
+ * factors (inline: out of line, the call's register saves cost 1.5% of the
+ * full-size integral). */
+template <int S>
+__device__ __forceinline__ void tile_prologue2(const mwsep_area_dev& A, const mwsep_theta_consts& th, int k0, int k1,
+                                            int mu0, int nu, int ncols, int lane, double idsv, float* cs,
+                                            double* tscale)
+{
+    constexpr int CW = PackedTile<S>::W;
+    const bool live = lane < ncols;
+    const double* g =
+        A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + (live ? lane : 0)) * A.nu_steps + nu, A.n_cols, 1);
+    int eref[SArr<S>::N];
+    tile_erefs<S>(A, th, k0, k1, g, live, lane, idsv, tscale, eref);
+    if (live)
+    {
+        Col<S> cc;
+        column_consts<S, true>(g, th, cc, nullptr, 0.0, 0.0, eref);
+        store_col2<S>(cs + lane * CW, cc);
+    }
+}
+
 /* warp_tile with packed arithmetic; cs holds TileSmem<S>::N floats for
  * this warp. */
 template <int S, int FORM>
@@ -760,19 +793,7 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
      * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     double* const tscale = reinterpret_cast<double*>(cs + mwsep::kTileCols * CW);
-    {
-        const bool live = lane < ncols;
-        const double* g =
-            A.geom + 4 * (size_t)MWSEP_IDX((size_t)(mu0 + (live ? lane : 0)) * A.nu_steps + nu, A.n_cols, 1);
-        int eref[SArr<S>::N];
-        tile_erefs<S>(A, th, k0, k1, g, live, lane, idsv, tscale, eref);
-        if (live)
-        {
-            Col<S> cc;
-            column_consts<S, true>(g, th, cc, nullptr, 0.0, 0.0, eref);
-            store_col2<S>(cs + lane * CW, cc);
-        }
-    }
+    tile_prologue2<S>(A, th, k0, k1, mu0, nu, ncols, lane, idsv, cs, tscale);
     __syncwarp();
     const int nf = (k1 - k0) * C;
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
