@@ -48,8 +48,9 @@ namespace {
 using mwsep::dfl::df;
 namespace D = mwsep::dfl;
 
-/* Integral blocks: 8 warps up to 4 streams, 4 warps for 5-8 streams (the
- * columns' constants then take twice the shared memory per warp). */
+/* Integral blocks: 8 warps up to 3 streams, 4 warps for 4-8 streams (the
+ * columns' constants and the log2 table of the general form then fit the
+ * static shared memory). */
 template <int S>
 struct DfShape
 {

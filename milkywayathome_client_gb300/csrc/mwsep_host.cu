@@ -416,7 +416,7 @@ void default_tune(mwsep_ctx* c, Wedge& w)
     for (int prec = 0; prec < 3; ++prec)
     {
         Tune& t = w.tune[prec];
-        t.block = (prec == MWSEP_PLAIN_DF && p.n_streams > 4) ? 128 : 256; /* the DF kernel's own blocks */
+        t.block = (prec == MWSEP_PLAIN_DF && p.n_streams >= 4) ? 128 : 256; /* the DF kernel's own blocks */
         t.warp_items = (prec == MWSEP_PLAIN_DF ||
                         (prec == MWSEP_MIXED_F32 && env_long("MWSEP_F32_WARP_TILES", 1) != 0)) ? 1 : 0;
         const int per_sm = prec == MWSEP_PLAIN_F64   ? mwsep_integral_f64_blocks_per_sm(p.n_streams, t.block)
