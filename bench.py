@@ -21,6 +21,11 @@ milkywayathome_client_gb300/synthetic.py).  A step is one evaluation
   cpu_baseline  the reference CPU evaluator (or its C restatement where the
              reference is not compiled on this host) on a bounded slice of
              the same evaluation, all host cores
+  extras     population_batch (256 parameter vectors of one wedge, one
+             engine batch), mixed_size_batch (64 evaluations over 6 wedges
+             of log-uniform sizes, per-wedge autotuned tiles, one engine
+             batch replayed as a CUDA graph), serving (Poisson arrivals),
+             catalogue_load (text vs binary catalogue)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -402,6 +407,7 @@ def run_gb300_arm(args, ws, rank, local):
         ctx.close()
         ctx = None
         out["population_batch"] = population_batch(args)
+        out["mixed_size_batch"] = mixed_size_batch(args)
         out["serving"] = serving(args)
         out["catalogue_load"] = catalogue_load(args, files)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -477,6 +483,53 @@ def catalogue_load(args, files):
             out[kind] = (time.perf_counter() - t0) * 1e3
     return {"stars": f["n_stars"], "text_ms": out["text"], "binary_ms": out["binary"],
             "speedup": out["text"] / out["binary"]}
+
+
+def mixed_size_batch(args):
+    """64 evaluations spread over the 6 mixed-size wedges (log-uniform sizes,
+    the serving wedges), each wedge's tile shape from the autotuner, one
+    engine batch replayed as a CUDA graph, compensated FP32; and one
+    evaluation per wedge in the plain FP64 and double-float forms, for their
+    rates and the compensated form's error."""
+    import numpy as np
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import synthetic as syn
+    m = syn.materialise(3, os.path.join(args.data_dir, "serving"))
+    rng = np.random.default_rng(3)
+    with mw.Context(0) as ctx:
+        wedges = []
+        for f in m["files"]:
+            wid = ctx.add_wedge(mw.AstronomyParameters.read(f["params"]), mw.StarPoints.read(f["stars"]))
+            wedges.append((wid, np.asarray(f["theta"], dtype=np.float64), f["n_stars"]))
+        for wid, _, _ in wedges:
+            ctx.autotune(wid, mw.MWSEP_MIXED_F32)
+        p = np.array([w[2] for w in wedges], float)
+        p /= p.sum()
+        reqs = []
+        for _ in range(64):
+            wid, th, _ = wedges[rng.choice(len(wedges), p=p)]
+            reqs.append((wid, th * (1.0 + 0.002 * rng.standard_normal(th.size))))
+        ctx.evaluate_requests(reqs, mw.MWSEP_MIXED_F32)  # graph capture
+        times = []
+        for _ in range(3):
+            ctx.evaluate_requests(reqs, mw.MWSEP_MIXED_F32)
+            times.append(ctx.last_timings()["total_ms"])
+        sweep = [(wid, th) for wid, th, _ in wedges]
+        mixed = ctx.evaluate_requests(sweep, mw.MWSEP_MIXED_F32)
+        rates = {}
+        out = {}
+        for name, prec in (("plain_f64", mw.MWSEP_PLAIN_F64), ("double_float", mw.MWSEP_PLAIN_DF)):
+            out[name] = ctx.evaluate_requests(sweep, prec)
+            rates[name] = len(sweep) / (ctx.last_timings()["total_ms"] * 1e-3)
+    ms = statistics.median(times)
+    return {"workload": "64 evaluations over 6 wedges (mu 200-1600, nu 80-640, r 70-700, convolve 30-120, "
+                        "1-4 streams, 20k-200k stars), wedge chosen by star count",
+            "value": len(reqs) / (ms * 1e-3), "unit": "evals/s", "ms_per_batch": ms, "graph": True,
+            "autotuned": True,
+            "plain_f64_evals_per_s": rates["plain_f64"], "double_float_evals_per_s": rates["double_float"],
+            "max_dlogL_mixed_vs_plain": max(abs(a.likelihood - b.likelihood) for a, b in zip(mixed, out["plain_f64"])),
+            "max_dlogL_double_float_vs_plain": max(abs(a.likelihood - b.likelihood)
+                                                   for a, b in zip(out["double_float"], out["plain_f64"]))}
 
 
 def serving(args):
