@@ -533,13 +533,20 @@ def mixed_size_batch(args):
 
 
 def serving(args):
-    """Poisson arrivals over the 6 mixed-size wedges, compensated FP32."""
+    """Poisson arrivals over the 6 mixed-size wedges: compensated FP32 at 50,
+    200 and 800 requests/s; the plain FP64 form at 1 request/s and the
+    double-float form at 10 requests/s (their throughputs on these wedges
+    are ~2 and ~33 evaluations/s)."""
     from milkywayathome_client_gb300 import native as N
     from milkywayathome_client_gb300 import serve_bench
-    res = serve_bench.run([50.0, 200.0, 800.0], 2.0, N.MWSEP_MIXED_F32, 2, 256,
-                          os.path.join(args.data_dir, "serving"))
+    d = os.path.join(args.data_dir, "serving")
+    res = serve_bench.run([50.0, 200.0, 800.0], 2.0, N.MWSEP_MIXED_F32, 2, 256, d)
+    plain = serve_bench.run([1.0], 4.0, N.MWSEP_PLAIN_F64, 2, 256, d, autotune=False)
+    dfl = serve_bench.run([10.0], 3.0, N.MWSEP_PLAIN_DF, 2, 256, d, autotune=False)
     return {"workload": "Poisson arrivals over 6 resident wedges (log-uniform sizes), wedge chosen by star count",
-            "lanes": 2, "precision": "mixed", "results": res}
+            "lanes": 2, "precision": "mixed", "results": res,
+            "plain_f64": {"precision": "plain FP64", "results": plain},
+            "double_float": {"precision": "double-float", "results": dfl}}
 
 
 def main():

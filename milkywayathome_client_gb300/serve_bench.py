@@ -1,6 +1,6 @@
 """Serving benchmark: Poisson arrivals over resident wedges.
 
-    python -m milkywayathome_client_gb300.serve_bench --rates 50,200,800 --seconds 4 --precision mixed
+    python -m milkywayathome_client_gb300.serve_bench --rates 50,200,800 --seconds 4 --precision mixed|plain|df
 
 The wedges are those of the mixed-size workload (6 seeded synthetic wedges,
 log-uniform sizes; synthetic.config(3)), all resident at once; each arrival
@@ -76,15 +76,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="50,200,800")
     ap.add_argument("--seconds", type=float, default=4.0)
-    ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--precision", choices=["plain", "mixed", "df"], default="mixed")
     ap.add_argument("--lanes", type=int, default=2)
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--star-scale", type=float, default=1.0)
     ap.add_argument("--data-dir", default=os.path.join(tempfile.gettempdir(), "mwsep_serve_data"))
     a = ap.parse_args()
-    prec = N.MWSEP_MIXED_F32 if a.precision == "mixed" else N.MWSEP_PLAIN_F64
+    prec = {"mixed": N.MWSEP_MIXED_F32, "plain": N.MWSEP_PLAIN_F64, "df": N.MWSEP_PLAIN_DF}[a.precision]
     rates = [float(x) for x in a.rates.split(",")]
-    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale)
+    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale,
+              autotune=prec != N.MWSEP_PLAIN_DF)  # the autotuner takes the other two forms
     print(json.dumps({"precision": a.precision, "lanes": a.lanes, "results": res}))
 
 
