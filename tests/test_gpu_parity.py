@@ -7,6 +7,7 @@ absolute on the log-likelihood.  Compensated-FP32 form: 1e-7 absolute on the
 log-likelihood.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -210,3 +211,42 @@ def test_compensated_far_stream(gpu_ctx, mu, sigma):
         wid = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
         e = ctx.evaluate_requests([(wid, theta)], mw.MWSEP_MIXED_F32)[0]
     assert abs(e.likelihood - a.likelihood) <= ABS_LOGL_F32, (e.likelihood, a.likelihood)
+
+
+def test_compensated_thread_items():
+    """The compensated form's thread-item kernels (one column and r-run per
+    thread, MWSEP_F32_WARP_TILES=0) against the reference's goldens within
+    1e-7 on the log-likelihood, a far stream included (a fresh process: the
+    switch is read when a wedge's launch shape is chosen)."""
+    import subprocess
+    import sys
+    import textwrap
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = textwrap.dedent(f"""
+        import sys, json, math
+        sys.path.insert(0, {root!r}); sys.path.insert(0, {os.path.join(root, "tests")!r})
+        import numpy as np
+        from conftest import load_case
+        import milkywayathome_client_gb300 as mw
+        worst = 0.0
+        with mw.Context(0) as ctx:
+            for name in ("basic_1stream", "three_streams", "cut_area", "aux_profile", "general_alpha_delta"):
+                pf, sf, g = load_case(name)
+                ctx.set_problem(mw.AstronomyParameters.read(pf)); ctx.set_stars(mw.StarPoints.read(sf))
+                r = ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32)
+                worst = max(worst, abs(r.likelihood - g["likelihood"]))
+            pf, sf, g = load_case("three_streams")
+            ctx.set_problem(mw.AstronomyParameters.read(pf)); ctx.set_stars(mw.StarPoints.read(sf))
+            th = np.asarray(g["theta"], float); th[3] = 200.0; th[7] = 1.0
+            a = ctx.evaluate(th, mw.MWSEP_PLAIN_F64); b = ctx.evaluate(th, mw.MWSEP_MIXED_F32)
+            far = abs(a.likelihood - b.likelihood)
+            rel = abs(b.integrals[2] - a.integrals[2]) / a.integrals[2]
+        print(json.dumps({{"worst": worst, "far": far, "rel": rel}}))
+    """)
+    env = dict(os.environ, MWSEP_F32_WARP_TILES="0")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr
+    import json
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["worst"] <= ABS_LOGL_F32, res
+    assert res["far"] <= ABS_LOGL_F32 and res["rel"] <= 2e-6, res
