@@ -203,7 +203,9 @@ int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, 
  * versions the integral kernel uses (elements taken two at a time).  Inputs
  * are doubles (split into FP32 pairs on the device), outputs the pairs'
  * values as doubles; host arrays of n elements (y and z unused by the ops
- * that do not take them), synchronous. */
+ * that do not take them), synchronous.  Ops 20 e^x and 21 1/x are the
+ * FP64 integral kernel's own table-driven exponential and Newton-Raphson
+ * reciprocal, in plain FP64. */
 int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z, double* out);
 
 /* ------------------------------------------------------------------ */

@@ -574,8 +574,17 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
         thi[j] = c_exp2_tab[j].x;
         tlo[j] = c_exp2_tab[j].y;
     }
+    __shared__ double etab[256];
     for (int j = threadIdx.x; j < D::kLog2Table; j += blockDim.x) ltab[j] = c_log2_tab[j];
+    mwsep::f64::exp_tang_table(etab);
     __syncthreads();
+    if (op >= 20)
+    {
+        /* the FP64 integral kernel's own exp and reciprocal */
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            out[i] = (op == 20) ? mwsep::f64::exp_tang(x[i], etab) : mwsep::f64::rcp_nr(x[i]);
+        return;
+    }
     if (op >= 10)
     {
         /* element pairs (2i, 2i + 1); an odd last element is paired with itself */
@@ -706,7 +715,8 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
 extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z,
                              double* out)
 {
-    if (op < 0 || (op > 6 && op < 10) || op > 16 || n < 0 || (n > 0 && (!x || !y || !z || !out)))
+    if (op < 0 || (op > 6 && op < 10) || (op > 16 && op < 20) || op > 21 || n < 0 ||
+        (n > 0 && (!x || !y || !z || !out)))
         return MWSEP_ERR_ARG;
     if (n == 0) return MWSEP_OK;
     if (cudaSetDevice(device) != cudaSuccess || mwsep_df_prepare(device)) return MWSEP_ERR_CUDA;

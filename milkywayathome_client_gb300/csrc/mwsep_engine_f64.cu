@@ -33,14 +33,14 @@ __device__ __forceinline__ void store_partial(comp_sum (&acc)[NC], int ncomp, do
 }
 
 template <int SMAX>
-__device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const mwsep_itile& t,
-                                      double* red, double2* out)
+__device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const double* etab,
+                                      const mwsep_itile& t, double* red, double2* out)
 {
     comp_sum acc[1 + SMAX];
 #pragma unroll
     for (int k = 0; k < 1 + SMAX; ++k) acc[k].zero();
     for (long long item = t.item_begin + threadIdx.x; item < t.item_end; item += blockDim.x)
-        integral_item<SMAX>(A, th, item, acc);
+        integral_item<SMAX>(A, th, etab, item, acc);
     store_partial<1 + SMAX>(acc, 1 + th.n_streams, red, out);
 }
 
@@ -59,8 +59,10 @@ __global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
     __shared__ double red[2 * (1 + SMAX) * 32];
+    __shared__ double etab[256];
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * G + 2];
+    exp_tang_table(etab);
     for (;;)
     {
         if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 0], 1);
@@ -72,7 +74,7 @@ __global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep
         load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
         __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
-        itile<SMAX>(A, th, tile, red, out);
+        itile<SMAX>(A, th, etab, tile, red, out);
         __syncthreads();
     }
 }

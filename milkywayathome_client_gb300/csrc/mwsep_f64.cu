@@ -34,7 +34,9 @@ __global__ void __launch_bounds__(256) integral_f64_kernel(const mwsep_area_dev 
 {
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (1 + SMAX) * 32];
+    __shared__ double etab[256];
     load_theta(th, thetas + blockIdx.y);
+    exp_tang_table(etab);
     __syncthreads();
 
     comp_sum acc[1 + SMAX];
@@ -44,7 +46,7 @@ __global__ void __launch_bounds__(256) integral_f64_kernel(const mwsep_area_dev 
     const int S = th.n_streams;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < A.n_items; item += stride)
-        integral_item<SMAX>(A, th, item, acc);
+        integral_item<SMAX>(A, th, etab, item, acc);
     mwsep::block_reduce<1 + SMAX>(acc, red);
     if (threadIdx.x == 0)
     {

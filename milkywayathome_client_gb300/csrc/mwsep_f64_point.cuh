@@ -95,6 +95,61 @@ __device__ __forceinline__ void convolve_f64(const double* __restrict__ rp, cons
     }
 }
 
+/* e^x for x <= 709 in FP64 by Tang's table-driven method (ACM TOMS
+ * 15(2), 1989): m = rint(256 x / ln2), r = x - m ln2/256 with ln2/256
+ * split Cody-Waite style (a 29-bit high part, so m times it is exact for
+ * |m| < 2^24), then e^x = 2^(m >> 8) 2^((m & 255)/256) e^r with
+ * |r| <= ln2/512 and e^r - 1 the degree-5 Taylor polynomial (remainder
+ * below 1e-20).  Ten FP64 operations; within 1 ulp of 2^-52 relative on a
+ * CPU restatement over [-745, 0].  tab[j] = 2^(j/256).  The range check
+ * is on the integer bits (|x| > 745.2 or NaN): NaN stays NaN, below -745.2
+ * the result is 0 as FP64 underflows there, above +745.2 it is +inf. */
+__device__ __forceinline__ double exp_tang(double x, const double* __restrict__ tab)
+{
+    constexpr unsigned long long kMaxMag = 0x408749999999999aull; /* bits of 745.2 */
+    if ((__double_as_longlong(x) & 0x7fffffffffffffffll) > (long long)kMaxMag)
+        return (x != x) ? x : (x < 0.0 ? 0.0 : __longlong_as_double(0x7ff0000000000000ll));
+    constexpr double kInvL = 369.3299304675746;          /* 256 / ln2 */
+    constexpr double kL1 = 0x1.62e42ff000000p-9;          /* ln2/256, high part */
+    constexpr double kL2 = -0x1.718432a1b0e26p-43;        /* ln2/256 - kL1 */
+    constexpr double kShift = 6755399441055744.0;         /* 1.5 * 2^52 */
+    const double t = fma(x, kInvL, kShift);
+    const long long m = __double_as_longlong(t) - __double_as_longlong(kShift);
+    const double md = t - kShift;
+    const double r = fma(-md, kL2, fma(-md, kL1, x));
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(r, q, 1.0 / 6.0);
+    q = fma(r, q, 0.5);
+    const double em1 = fma(r * r, q, r);
+    const double T = tab[m & 255];
+    const double v = fma(T, em1, T);
+    const int n = (int)(m >> 8);
+    return n >= -1021 ? __longlong_as_double(__double_as_longlong(v) + ((long long)n << 52)) : ldexp(v, n);
+}
+
+/* 1/x for positive x with x and 1/x normal, by two Newton-Raphson steps
+ * y' = y + y (1 - x y) (each squares the relative error; Markstein, IBM J.
+ * Res. Dev. 34(1), 1990) from the hardware's approximate FP64 reciprocal:
+ * four FMAs and one SFU operation, within 1 ulp of the quotient.  No
+ * special-case handling: the approximation flushes subnormals to zero, so
+ * x or 1/x subnormal, zero, infinite or NaN is outside its domain (in the
+ * halo term x = rg (rg + r0)^3 lies between about 1e-3 and 1e12). */
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+/* The 2^(j/256) table for exp_tang, filled by a block into its shared memory. */
+__device__ __forceinline__ void exp_tang_table(double* tab)
+{
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) tab[j] = exp2((double)j / 256.0);
+}
+
 /* Per-column constants of the integral's density in completed-square form,
  * in FP64.  With u = (cos b cos l, cos b sin l, sin b) the column's unit
  * vector, a point at distance r sits at x = r u - (R, 0, 0)
@@ -154,7 +209,7 @@ template <int SMAX>
 __device__ __forceinline__ void convolve_f64_cs(const double* __restrict__ rp, const double* __restrict__ qwt,
                                                 const double* __restrict__ gm, const double* __restrict__ gm2,
                                                 int C, const ColF64<SMAX>& cc, const mwsep_theta_consts& th,
-                                                double& bg, double (&st)[SMAX])
+                                                const double* __restrict__ etab, double& bg, double (&st)[SMAX])
 {
     const int S = th.n_streams;
     bg = (th.bg_mode == 2) ? -1.0 : 0.0;
@@ -167,11 +222,11 @@ __device__ __forceinline__ void convolve_f64_cs(const double* __restrict__ rp, c
         if (th.bg_mode != 2)
         {
             const double t = r - cc.rb;
-            const double rg = sqrt(cc.B2 * t * t + cc.Db);
+            const double rg = sqrt(fma(cc.B2 * t, t, cc.Db));
             if (th.bg_mode == 0)
             {
                 const double rs = rg + th.r0;
-                bg += qw / (rg * rs * rs * rs);
+                bg = fma(qw, rcp_nr(rg * rs * rs * rs), bg);
                 if (th.aux) bg += qw * (th.bg_a * gm2[n] + th.bg_b * gm[n] + th.bg_c);
             }
             else
@@ -183,7 +238,7 @@ __device__ __forceinline__ void convolve_f64_cs(const double* __restrict__ rp, c
             if (s < S && th.stream_on[s])
             {
                 const double u = r - cc.rs[s];
-                st[s] += qw * exp(cc.k2[s] * u * u + cc.k0[s]);
+                st[s] = fma(qw, exp_tang(fma(cc.k2[s] * u, u, cc.k0[s]), etab), st[s]);
             }
         }
     }
@@ -193,7 +248,8 @@ __device__ __forceinline__ void convolve_f64_cs(const double* __restrict__ rp, c
  * each cell's bg*V and st*V into acc (cpu/evaluation_optimized.c:498-520). */
 template <int SMAX>
 __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                              long long item, comp_sum (&acc)[1 + SMAX])
+                                              const double* __restrict__ etab, long long item,
+                                              comp_sum (&acc)[1 + SMAX])
 {
     const int S = th.n_streams;
     const int C = A.convolve;
@@ -211,7 +267,8 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
         const double V = A.irv[MWSEP_IDX(k, A.r_steps, 4)] * idsj;
         double bg, st[SMAX];
         const size_t row = (size_t)MWSEP_IDX(k, A.r_steps, 5) * C;
-        convolve_f64_cs<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, C, cc, th, bg, st);
+        convolve_f64_cs<SMAX>(A.r_point + row, A.qw + row, A.r_in_mag + row, A.r_in_mag2 + row, C, cc, th, etab, bg,
+                              st);
         const double rf = A.reff[MWSEP_IDX(k, A.r_steps, 6)];
         if (th.bg_mode != 2) bg *= rf;
         bg *= V;

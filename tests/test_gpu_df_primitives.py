@@ -144,3 +144,37 @@ def test_log2(rng, base):
     want = np.log2(_split(x))
     err = np.abs(got - want) / (np.abs(want) + 1.0)
     assert err.max() <= 2.0 ** -46, err.max()
+
+
+def test_fp64_exp(rng):
+    """The FP64 integral kernel's e^x (Tang's table method, op 20) against
+    numpy's FP64 exp: within 2^-51 relative over the normal range, within
+    one subnormal step below it, and the range edges (0, underflow, NaN,
+    +-inf, large positive) handled."""
+    x = np.concatenate([rng.uniform(-708.0, 0.0, 400000), rng.uniform(-40.0, 0.0, 200000),
+                        rng.uniform(-1e-6, 0.0, 20000), rng.uniform(0.0, 700.0, 20000),
+                        -np.arange(0, 2049) * (np.log(2.0) / 256.0),        # table knots
+                        np.array([-0.0, 0.0, -1.0, -708.39, 709.0])])
+    got = _eval(20, x)
+    want = np.exp(x)
+    rel = np.abs(got - want) / want
+    assert rel.max() <= 2.0 ** -51, (rel.max(), x[np.argmax(rel)])
+    sub = np.concatenate([rng.uniform(-745.1, -708.4, 20000), np.array([-744.0, -745.0, -745.2])])
+    assert np.abs(_eval(20, sub) - np.exp(sub)).max() <= 2.0 ** -1073
+    edges = np.array([-745.3, -1000.0, -1e300, -np.inf, np.nan, 746.0, np.inf])
+    got = _eval(20, edges)
+    np.testing.assert_array_equal(got[:4], 0.0)
+    assert np.isnan(got[4]) and got[5] == np.inf and got[6] == np.inf
+
+
+def test_fp64_reciprocal(rng):
+    """The FP64 integral kernel's 1/x (two Newton-Raphson steps from the
+    SFU approximation, op 21) against the correctly rounded quotient:
+    within 2^-51 relative for positive x with x and 1/x normal (the
+    approximation flushes a subnormal reciprocal, e.g. of 1e308, to 0)."""
+    x = np.concatenate([np.exp(rng.uniform(-700.0, 700.0, 200000)), rng.uniform(1.0, 2.0, 200000),
+                        2.0 ** np.arange(-1021, 1022, dtype=np.float64), np.array([1.0, 3.0, 4.4e307, 2.3e-308])])
+    got = _eval(21, x)
+    want = 1.0 / x
+    rel = np.abs(got - want) / want
+    assert rel.max() <= 2.0 ** -51, (rel.max(), x[np.argmax(rel)])
