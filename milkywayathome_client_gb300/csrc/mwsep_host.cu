@@ -403,6 +403,33 @@ int fill_kchunk(int max_r, int convolve, int group, long long tiles_per_chunk, i
     return best;
 }
 
+/* Modelled time of one warp-tile launch of the compensated kernel, which
+ * strides statically (warp w of W takes tiles w, w + W, ...; tiles in
+ * r-chunk-major order; block b on SM b % sms): the largest per-SM sum of
+ * tile costs, a tile costing its lane groups of points plus a per-tile
+ * column prologue of `prologue` groups.  With prologue 0.5 it reproduces
+ * the measured full-size integral (1600 x 640 x 140 cells, convolve 120,
+ * 3 streams) within 0.6% for r-chunks of 28 to 140 bins. */
+double static_tile_cost(int max_r, int convolve, int group, long long tiles_per_chunk, int kc, int sms,
+                        int blocks_per_sm, int warps_per_block, double prologue)
+{
+    const long long W = (long long)sms * blocks_per_sm * warps_per_block;
+    const int nk = (max_r + kc - 1) / kc;
+    std::vector<double> sm(sms, 0.0);
+    double all = 0.0; /* added to every SM */
+    for (int k = 0; k < nk; ++k)
+    {
+        const long long pts = (long long)std::min(kc, max_r - k * kc) * std::max(convolve, 1);
+        const double cost = (double)((pts + group - 1) / group) + prologue;
+        const long long lo = (long long)k * tiles_per_chunk;
+        const long long full = tiles_per_chunk / W, rem = tiles_per_chunk - full * W;
+        all += (double)full * cost * blocks_per_sm * warps_per_block;
+        for (long long i = 0; i < rem; ++i)
+            sm[(size_t)((((lo + full * W + i) % W) / warps_per_block) % sms)] += cost;
+    }
+    return all + *std::max_element(sm.begin(), sm.end());
+}
+
 void default_tune(mwsep_ctx* c, Wedge& w)
 {
     const ProblemHost& p = w.prob;
@@ -454,9 +481,23 @@ void default_tune(mwsep_ctx* c, Wedge& w)
              * minimises the modelled time instead (lane groups per tile, a
              * per-tile prologue, and one warp's sequential chain) */
             const long long slots = threads / 32;
-            if (tiles_per_chunk * ((max_r + kc - 1) / kc) < slots)
-                kc = fill_kchunk(max_r, p.convolve, group, tiles_per_chunk, c->sm_count, slots,
-                                 prec == MWSEP_PLAIN_DF ? 0.1 : 0.8, kc);
+            if (prec == MWSEP_MIXED_F32)
+            {
+                /* the r-chunk of least modelled time, from the four-group floor up */
+                double best = 1e300;
+                for (int k = std::max(1, std::min(max_r, kmin)); k <= max_r; ++k)
+                {
+                    const double cost = static_tile_cost(max_r, p.convolve, group, tiles_per_chunk, k, c->sm_count,
+                                                         per_sm, t.block / 32, 0.5);
+                    if (cost < best * (1.0 - 1e-12))
+                    {
+                        best = cost;
+                        kc = k;
+                    }
+                }
+            }
+            else if (tiles_per_chunk * ((max_r + kc - 1) / kc) < slots)
+                kc = fill_kchunk(max_r, p.convolve, group, tiles_per_chunk, c->sm_count, slots, 0.1, kc);
             t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", kc);
             long long g = (long long)c->sm_count * per_sm;
             g = env_long("MWSEP_TUNE_GRID_F32", g);
