@@ -405,7 +405,10 @@ int mwsep_ctx_evaluate_requests(mwsep_ctx* ctx, int n, const mwsep_request* reqs
 
 /* The autotuner: time candidate tile shapes (r-bins per item, items per
  * tile) for one wedge and precision and keep the fastest; *predicted_ms is
- * the predicted integral time of one evaluation with the chosen shape. */
+ * the predicted integral time of one evaluation with the chosen shape.  For
+ * MWSEP_PLAIN_DF (whose requests run per wedge, not in the engine) it times
+ * whole single evaluations over candidate r-chunks, and *predicted_ms is
+ * the chosen one's measured integral time. */
 int mwsep_ctx_autotune(mwsep_ctx* ctx, int wedge_id, int precision, double* predicted_ms);
 /* The tile shape a wedge uses for one precision. */
 int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* ctx, int wedge_id, int precision, int* k_chunk, int* tile_items);

@@ -565,13 +565,76 @@ extern "C" int mwsep_ctx_evaluate_requests(mwsep_ctx* c, int n, const mwsep_requ
 
 extern "C" int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* c, int id, int precision, int* k_chunk, int* tile_items)
 {
-    if (!c || id < 0 || id >= (int)c->wedges.size() || (precision != 0 && precision != 1) || !k_chunk ||
+    if (!c || id < 0 || id >= (int)c->wedges.size() || precision < 0 || precision > 2 || !k_chunk ||
         !tile_items)
         return mwsep_fail(MWSEP_ERR_ARG);
     *k_chunk = c->wedges[id]->tune[precision].k_chunk;
     *tile_items = c->wedges[id]->tune[precision].tile_items;
     return MWSEP_OK;
 }
+
+namespace {
+
+/* The double-float form runs its requests per wedge (evaluate_wedge), so
+ * its tuner times whole single evaluations: r-chunks of whole lane groups
+ * (1, 2, 3, 4, 6 or 8 of the chunk that fills them), the r range split
+ * evenly in 1 to 4 chunks, and the current one; the integral's device time,
+ * best of two, picks the chunk. */
+int autotune_df(mwsep_ctx* c, int id, const double* theta, double* predicted_ms)
+{
+    Wedge& w = *c->wedges[id];
+    int R = 1;
+    for (int a = 0; a < w.prob.n_areas; ++a) R = std::max(R, w.prob.area[a].r_steps);
+    const int group = 32 * mwsep_df_tile_p(w.prob.n_streams);
+    int g = group;
+    for (int b = std::max(w.prob.convolve, 1); b;)
+    {
+        const int t = g % b;
+        g = b;
+        b = t;
+    }
+    const int ks = group / g;
+    const Tune saved = w.tune[MWSEP_PLAIN_DF];
+    std::vector<int> kcs{saved.k_chunk};
+    auto add = [&](int kc) {
+        kc = std::max(1, std::min(R, kc));
+        if (std::find(kcs.begin(), kcs.end(), kc) == kcs.end()) kcs.push_back(kc);
+    };
+    for (int m : {1, 2, 3, 4, 6, 8}) add(ks * m);
+    for (int d = 1; d <= 4; ++d) add((R + d - 1) / d);
+    double best = 1e300;
+    Tune best_t = saved;
+    mwsep_result r;
+    for (int kc : kcs)
+    {
+        Tune& t = w.tune[MWSEP_PLAIN_DF];
+        t = saved;
+        t.k_chunk = kc;
+        double ms = 1e300;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+            const int rc = mwsep::evaluate_wedge(c, id, 1, theta, MWSEP_PLAIN_DF, &r);
+            if (rc)
+            {
+                w.tune[MWSEP_PLAIN_DF] = saved;
+                return rc;
+            }
+            ms = std::min(ms, c->last_ms[0]);
+        }
+        if (ms < best)
+        {
+            best = ms;
+            best_t = t;
+        }
+    }
+    w.tune[MWSEP_PLAIN_DF] = best_t;
+    w.tune[MWSEP_PLAIN_DF].tuned = true;
+    ++w.tune_gen;
+    if (predicted_ms) *predicted_ms = best < 1e299 ? best : -1.0;
+    return MWSEP_OK;
+}
+
+} // namespace
 
 /* The project autotuner: for one wedge and precision, time the integral
  * tiles of a truncated single request (the first few waves of tiles) for
@@ -581,8 +644,8 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
 {
     mwsep::Range nvtx_range("mwsep.autotune");
     if (!c || id < 0 || id >= (int)c->wedges.size()) return mwsep_fail(MWSEP_ERR_ARG);
-    if (precision == MWSEP_PLAIN_DF) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
-    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32) return mwsep_fail(MWSEP_ERR_ARG);
+    if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
+        return mwsep_fail(MWSEP_ERR_ARG);
     Wedge& w = *c->wedges[id];
     if (!w.has_problem || !w.has_stars) return mwsep_fail(MWSEP_ERR_STATE);
     CU(cudaSetDevice(c->device));
@@ -599,6 +662,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
                 if (w.prob.st_opt[s][j]) theta[k++] = w.prob.st[s][j];
         }
     }
+    if (precision == MWSEP_PLAIN_DF) return autotune_df(c, id, theta.data(), predicted_ms);
     mwsep_request rq;
     rq.wedge = id;
     rq.theta = theta.data();

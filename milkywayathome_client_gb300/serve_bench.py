@@ -84,8 +84,7 @@ def main():
     a = ap.parse_args()
     prec = {"mixed": N.MWSEP_MIXED_F32, "plain": N.MWSEP_PLAIN_F64, "df": N.MWSEP_PLAIN_DF}[a.precision]
     rates = [float(x) for x in a.rates.split(",")]
-    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale,
-              autotune=prec != N.MWSEP_PLAIN_DF)  # the autotuner takes the other two forms
+    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale)
     print(json.dumps({"precision": a.precision, "lanes": a.lanes, "results": res}))
 
 

@@ -3,9 +3,9 @@ outputs at the plain form's tolerances (1e-12 relative on every integral,
 1e-12 absolute on the log-likelihood) -- every golden case, the aux profile
 included -- against the native FP64 kernel at full size, batch == single,
 engine requests and gradients, first use from several threads, the device
-memory budget, a batch mixing the background forms, and its limits
-(beyond 4 streams the likelihood runs in native FP64; the autotuner refuses
-it).  q = 0 is checked with the plain form in test_gpu_parity."""
+memory budget, a batch mixing the background forms, the autotuner, and its
+limits (beyond 4 streams the likelihood runs in native FP64).  q = 0 is
+checked with the plain form in test_gpu_parity."""
 import math
 import os
 
@@ -85,12 +85,25 @@ def test_double_float_limits(gpu_ctx):
     for x, y in zip(b.integrals, a.integrals):
         assert _close_rel(x, y, REL), (x, y)
     assert abs(a.likelihood - b.likelihood) <= ABS_LOGL
-    pf, sf, g = load_case("basic_1stream")
+
+
+def test_double_float_autotune():
+    """The autotuner times double-float evaluations over candidate r-chunks
+    and keeps one; results with the chosen chunk stay within the plain
+    form's tolerance of the reference."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case("config0")
     with mw.Context(0) as ctx:
-        ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
-        with pytest.raises(mw.MwsepError) as e:
-            ctx.autotune(0, mw.MWSEP_PLAIN_DF)
-        assert e.value.status == N.MWSEP_ERR_UNSUPPORTED
+        wid = ctx.add_wedge(mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf))
+        ms = ctx.autotune(wid, mw.MWSEP_PLAIN_DF)
+        assert ms > 0
+        kc, _ = ctx.tile_shape(wid, mw.MWSEP_PLAIN_DF)
+        assert kc >= 1
+        r = ctx.evaluate_requests([(wid, g["theta"])], mw.MWSEP_PLAIN_DF)[0]
+        assert abs(r.likelihood - g["likelihood"]) <= ABS_LOGL
+        for x, y in zip([r.background_integral] + list(r.stream_integrals),
+                        [g["background_integral"]] + list(g["stream_integrals"])):
+            assert _close_rel(x, y, REL), (x, y)
 
 
 def test_double_float_engine_requests():
