@@ -574,17 +574,8 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
         thi[j] = c_exp2_tab[j].x;
         tlo[j] = c_exp2_tab[j].y;
     }
-    __shared__ double etab[256];
     for (int j = threadIdx.x; j < D::kLog2Table; j += blockDim.x) ltab[j] = c_log2_tab[j];
-    mwsep::f64::exp_tang_table(etab);
     __syncthreads();
-    if (op >= 20)
-    {
-        /* the FP64 integral kernel's own exp and reciprocal */
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            out[i] = (op == 20) ? mwsep::f64::exp_tang(x[i], etab) : mwsep::f64::rcp_nr(x[i]);
-        return;
-    }
     if (op >= 10)
     {
         /* element pairs (2i, 2i + 1); an odd last element is paired with itself */
@@ -629,6 +620,16 @@ __global__ void df_eval_kernel(int op, int n, const double* __restrict__ x, cons
         }
         out[i] = (double)r.hi + (double)r.lo;
     }
+}
+
+/* The FP64 integral kernel's own exp (op 20) and reciprocal (op 21). */
+__global__ void f64_eval_kernel(int op, int n, const double* __restrict__ x, double* __restrict__ out)
+{
+    __shared__ double etab[mwsep::f64::kExpTable];
+    mwsep::f64::exp_tang_table(etab);
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (op == 20) ? mwsep::f64::exp_tang(x[i], etab) : mwsep::f64::rcp_nr(x[i]);
 }
 
 std::atomic<bool> g_table_ready[64];
@@ -733,7 +734,10 @@ extern "C" int mwsep_df_eval(int device, int op, int n, const double* x, const d
     if (e == cudaSuccess)
     {
         const int grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
-        df_eval_kernel<<<grid, 256>>>(op, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+        if (op >= 20)
+            f64_eval_kernel<<<grid, 256>>>(op, n, d, d + 3 * (size_t)n);
+        else
+            df_eval_kernel<<<grid, 256>>>(op, n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost);

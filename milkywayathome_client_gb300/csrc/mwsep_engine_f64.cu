@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kBlock) engine_integral_f64_kernel(const mwsep
     __shared__ mwsep_theta_consts th;
     __shared__ mwsep_area_dev A;
     __shared__ double red[2 * (1 + SMAX) * 32];
-    __shared__ double etab[256];
+    __shared__ double etab[kExpTable];
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * G + 2];
     exp_tang_table(etab);

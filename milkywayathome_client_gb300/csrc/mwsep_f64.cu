@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) integral_f64_kernel(const mwsep_area_dev 
 {
     __shared__ mwsep_theta_consts th;
     __shared__ double red[2 * (1 + SMAX) * 32];
-    __shared__ double etab[256];
+    __shared__ double etab[kExpTable];
     load_theta(th, thetas + blockIdx.y);
     exp_tang_table(etab);
     __syncthreads();

@@ -96,34 +96,35 @@ __device__ __forceinline__ void convolve_f64(const double* __restrict__ rp, cons
 }
 
 /* e^x for x <= 709 in FP64 by Tang's table-driven method (ACM TOMS
- * 15(2), 1989): m = rint(256 x / ln2), r = x - m ln2/256 with ln2/256
+ * 15(2), 1989): m = rint(4096 x / ln2), r = x - m ln2/4096 with ln2/4096
  * split Cody-Waite style (a 29-bit high part, so m times it is exact for
- * |m| < 2^24), then e^x = 2^(m >> 8) 2^((m & 255)/256) e^r with
- * |r| <= ln2/512 and e^r - 1 the degree-5 Taylor polynomial (remainder
- * below 1e-20).  Ten FP64 operations; within 1 ulp of 2^-52 relative on a
- * CPU restatement over [-745, 0].  tab[j] = 2^(j/256).  The range check
- * is on the integer bits (|x| > 745.2 or NaN): NaN stays NaN, below -745.2
- * the result is 0 as FP64 underflows there, above +745.2 it is +inf. */
+ * |m| < 2^24), then e^x = 2^(m >> 12) 2^((m & 4095)/4096) e^r with
+ * |r| <= ln2/8192 and e^r - 1 = r + r^2 (1/2 + r/6) (remainder below
+ * 3e-18 relative).  Eight FP64 operations; within 1 ulp of 2^-52 relative
+ * on a CPU restatement over [-745, 0].  tab[j] = 2^(j/4096) (kExpTable
+ * doubles, 32 KB of shared memory).  The range check is on the integer
+ * bits (|x| > 745.2 or NaN): NaN stays NaN, below -745.2 the result is 0
+ * as FP64 underflows there, above +745.2 it is +inf. */
+constexpr int kExpBits = 12;
+constexpr int kExpTable = 1 << kExpBits;
+
 __device__ __forceinline__ double exp_tang(double x, const double* __restrict__ tab)
 {
     constexpr unsigned long long kMaxMag = 0x408749999999999aull; /* bits of 745.2 */
     if ((__double_as_longlong(x) & 0x7fffffffffffffffll) > (long long)kMaxMag)
         return (x != x) ? x : (x < 0.0 ? 0.0 : __longlong_as_double(0x7ff0000000000000ll));
-    constexpr double kInvL = 369.3299304675746;          /* 256 / ln2 */
-    constexpr double kL1 = 0x1.62e42ff000000p-9;          /* ln2/256, high part */
-    constexpr double kL2 = -0x1.718432a1b0e26p-43;        /* ln2/256 - kL1 */
+    constexpr double kInvL = 5909.278887481194;           /* 4096 / ln2 */
+    constexpr double kL1 = 0x1.62e42ff000000p-13;         /* ln2/4096, high part */
+    constexpr double kL2 = -0x1.718432a1b0e26p-47;        /* ln2/4096 - kL1 */
     constexpr double kShift = 6755399441055744.0;         /* 1.5 * 2^52 */
     const double t = fma(x, kInvL, kShift);
     const long long m = __double_as_longlong(t) - __double_as_longlong(kShift);
     const double md = t - kShift;
     const double r = fma(-md, kL2, fma(-md, kL1, x));
-    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
-    q = fma(r, q, 1.0 / 6.0);
-    q = fma(r, q, 0.5);
-    const double em1 = fma(r * r, q, r);
-    const double T = tab[m & 255];
+    const double em1 = fma(r * r, fma(r, 1.0 / 6.0, 0.5), r);
+    const double T = tab[m & (kExpTable - 1)];
     const double v = fma(T, em1, T);
-    const int n = (int)(m >> 8);
+    const int n = (int)(m >> kExpBits);
     return n >= -1021 ? __longlong_as_double(__double_as_longlong(v) + ((long long)n << 52)) : ldexp(v, n);
 }
 
@@ -144,10 +145,10 @@ __device__ __forceinline__ double rcp_nr(double x)
     return fma(y, e, y);
 }
 
-/* The 2^(j/256) table for exp_tang, filled by a block into its shared memory. */
+/* The 2^(j/4096) table for exp_tang, filled by a block into its shared memory. */
 __device__ __forceinline__ void exp_tang_table(double* tab)
 {
-    for (int j = threadIdx.x; j < 256; j += blockDim.x) tab[j] = exp2((double)j / 256.0);
+    for (int j = threadIdx.x; j < kExpTable; j += blockDim.x) tab[j] = exp2((double)j / (double)kExpTable);
 }
 
 /* Per-column constants of the integral's density in completed-square form,
