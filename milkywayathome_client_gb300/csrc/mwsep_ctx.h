@@ -169,6 +169,13 @@ struct mwsep_ctx
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6] = {};
+    /* The EvalFunc entries upload the catalogue on a side stream while the
+     * integral runs; star-table readers on `stream` wait for ev_stars while
+     * stars_pending (created on first use). */
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_main = nullptr, ev_stars = nullptr;
+    bool stars_pending = false;
+    mwsep::Wedge* stars_build = nullptr; /* its star-table build not yet launched */
     size_t dev_bytes = 0;
     size_t hbm_budget = 0; /* 0: no budget */
 
@@ -191,7 +198,7 @@ struct mwsep_ctx
 
 namespace mwsep {
 
-cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes);
+cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st = nullptr);
 cudaError_t d2h(mwsep_ctx* c, void* dst, const void* src, size_t bytes);
 int check_problem(const ASTRONOMY_PARAMETERS* ap);
 void theta_consts(const ProblemHost& base, const double* theta, mwsep_theta_consts& th);
@@ -199,8 +206,18 @@ long env_long(const char* name, long dflt);
 /* (Re)build a wedge's problem tables from *ap. */
 int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap);
 /* Upload a catalogue (SoA, host) and build its per-star tables. */
-int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r);
-int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp);
+/* Upload a catalogue and build its star tables on stream st. */
+int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
+                    cudaStream_t st);
+/* From STAR_POINTS rows: synchronously on the context's stream, or (on_side)
+ * on the side stream with ev_stars recorded and stars_pending set. */
+int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side);
+/* Make st wait for a pending side-stream catalogue upload. */
+int wait_stars(mwsep_ctx* c, cudaStream_t st);
+/* Launch a deferred side-stream star-table build (after event `after`, if
+ * given) and record ev_stars. */
+int launch_star_build(mwsep_ctx* c, cudaEvent_t after);
+int launch_star_tables_for(mwsep_ctx* c, Wedge& w, cudaStream_t st);
 void wedge_release(mwsep_ctx* c, Wedge& w);
 void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items);
 /* r-bins per warp tile that make a tile's points whole lane groups. */

@@ -492,7 +492,7 @@ extern "C" int mwsep_ctx_add_wedge(mwsep_ctx* c, const ASTRONOMY_PARAMETERS* ap,
     Wedge* w = new (std::nothrow) Wedge();
     if (!w) return mwsep_fail(MWSEP_ERR_NOMEM);
     rc = wedge_set_problem(c, *w, ap);
-    if (!rc) rc = wedge_set_stars_rows(c, *w, sp);
+    if (!rc) rc = wedge_set_stars_rows(c, *w, sp, false);
     if (rc)
     {
         wedge_release(c, *w);

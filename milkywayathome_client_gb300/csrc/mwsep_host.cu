@@ -155,10 +155,10 @@ void HostPinned::release()
 }
 
 /* cudaMemcpyAsync with transfer accounting */
-cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
+cudaError_t h2d(mwsep_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st)
 {
     c->xfer_h2d += bytes;
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st ? st : c->stream);
 }
 cudaError_t d2h(mwsep_ctx* c, void* dst, const void* src, size_t bytes)
 {
@@ -647,7 +647,17 @@ int warp_tile_kstep(int convolve, int n_streams)
     return group / a;
 }
 
-int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r)
+int launch_star_tables_for(mwsep_ctx* c, Wedge& w, cudaStream_t st)
+{
+    CK(mwsep_launch_star_tables(w.n_stars, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(),
+                                w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
+                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
+                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
+    return MWSEP_OK;
+}
+
+int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
+                    cudaStream_t st)
 {
     mwsep::Range nvtx_range("mwsep.set_stars");
     if (!w.has_problem) return mwsep_fail(MWSEP_ERR_STATE);
@@ -669,14 +679,17 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     rc |= w.s_pts.ensure(NC * sizeof(float4), tot);
     w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
-    cudaStream_t st = c->stream;
-    CU(h2d(c, w.s_l.p, l, (size_t)n * 8));
-    CU(h2d(c, w.s_b.p, b, (size_t)n * 8));
-    CU(h2d(c, w.s_r.p, r, (size_t)n * 8));
-    CK(mwsep_launch_star_tables(n, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(), C,
-                                w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
-                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
-                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
+    CU(h2d(c, w.s_l.p, l, (size_t)n * 8, st));
+    CU(h2d(c, w.s_b.p, b, (size_t)n * 8, st));
+    CU(h2d(c, w.s_r.p, r, (size_t)n * 8, st));
+    w.n_stars = n;
+    if (st == c->side)
+        c->stars_build = &w; /* launched by launch_star_build once the integral is queued */
+    else
+    {
+        int rc2 = launch_star_tables_for(c, w, st);
+        if (rc2) return rc2;
+    }
     mwsep_stars_dev& v = w.stars_view;
     v.n_stars = n;
     v.convolve = C;
@@ -698,10 +711,12 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     return MWSEP_OK;
 }
 
-int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp)
+int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side)
 {
     if (!sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
     const int n = sp->number_stars;
+    /* an earlier side-stream upload may still read the staging buffer */
+    if (c->ev_stars) CU(cudaEventSynchronize(c->ev_stars));
     if (w.h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
     double* l = w.h_stars.as<double>();
     double* b = l + n;
@@ -714,10 +729,55 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp)
         b[i] = row[1];
         r[i] = row[2];
     }
-    int rc = wedge_set_stars(c, w, n, l, b, r);
+    if (!on_side)
+    {
+        /* an earlier side-stream upload still writing the star tables */
+        if (c->ev_stars) CU(cudaStreamWaitEvent(c->stream, c->ev_stars, 0));
+        int rc = wedge_set_stars(c, w, n, l, b, r, c->stream);
+        if (rc) return rc;
+        /* the pinned staging buffer is reused: wait for the copies */
+        CU(cudaStreamSynchronize(c->stream));
+        return MWSEP_OK;
+    }
+    /* on the side stream, after everything already queued on the context's
+     * stream (the problem tables the star tables are built from, earlier
+     * readers of the star tables): the copies now, the table build when
+     * launch_star_build is called; the readers of this upload wait for
+     * ev_stars */
+    if (!c->side)
+    {
+        CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&c->ev_stars, cudaEventDisableTiming));
+    }
+    CU(cudaEventRecord(c->ev_main, c->stream));
+    CU(cudaStreamWaitEvent(c->side, c->ev_main, 0));
+    int rc = wedge_set_stars(c, w, n, l, b, r, c->side);
     if (rc) return rc;
-    /* the pinned staging buffer is reused: wait for the copies */
-    CU(cudaStreamSynchronize(c->stream));
+    c->stars_pending = true;
+    return MWSEP_OK;
+}
+
+int launch_star_build(mwsep_ctx* c, cudaEvent_t after)
+{
+    if (!c->stars_build) return MWSEP_OK;
+    Wedge& w = *c->stars_build;
+    c->stars_build = nullptr;
+    if (after) CU(cudaStreamWaitEvent(c->side, after, 0));
+    int rc = launch_star_tables_for(c, w, c->side);
+    if (rc) return rc;
+    CU(cudaEventRecord(c->ev_stars, c->side));
+    return MWSEP_OK;
+}
+
+/* Readers of the star tables on the context's stream: wait for a pending
+ * side-stream upload (launching its table build first if nothing has). */
+int wait_stars(mwsep_ctx* c, cudaStream_t st)
+{
+    if (!c->stars_pending) return MWSEP_OK;
+    int rc = launch_star_build(c, nullptr);
+    if (rc) return rc;
+    CU(cudaStreamWaitEvent(st, c->ev_stars, 0));
     return MWSEP_OK;
 }
 
@@ -875,9 +935,6 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         if (c->hbm_budget && tot + need > c->hbm_budget) return mwsep_fail(MWSEP_ERR_BUDGET);
         if (w.s_ptsdf.ensure(need, tot)) return mwsep_fail(MWSEP_ERR_NOMEM);
         w.bytes += tot - before;
-        CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
-                                      w.s_ptsdf.as<float4>(), c->stream));
-        w.has_star_df = true;
     }
 
     double* d_areas = c->d_out.as<double>();
@@ -940,10 +997,24 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
             }
         }
     }
+    /* a catalogue uploaded on the side stream: its table build released
+     * with the integral (after the parameter upload), so it fills SMs the
+     * integral's blocks leave */
+    rc = launch_star_build(c, c->ev[1]);
+    if (rc) return rc;
     CU(cudaEventRecord(c->ev[2], st));
     CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
     ++launches;
     CU(cudaEventRecord(c->ev[3], st));
+    /* from here on the star tables are read */
+    rc = wait_stars(c, st);
+    if (rc) return rc;
+    if (df_likelihood && !w.has_star_df)
+    {
+        CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
+                                      w.s_ptsdf.as<float4>(), st));
+        w.has_star_df = true;
+    }
     mwsep_launch_shape lk = sh;
     lk.block = t.lk_block;
     lk.grid = t.lk_grid;
@@ -1095,6 +1166,10 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     c->h_sep.release();
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->side) cudaStreamSynchronize(c->side);
+    if (c->ev_main) cudaEventDestroy(c->ev_main);
+    if (c->ev_stars) cudaEventDestroy(c->ev_stars);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MWSEP_OK;
@@ -1127,7 +1202,8 @@ extern "C" int mwsep_ctx_set_stars_soa(mwsep_ctx* c, int n, const double* l, con
     if (!c || !l || !b || !r) return mwsep_fail(MWSEP_ERR_ARG);
     CU(cudaSetDevice(c->device));
     if (c->wedges.empty()) return mwsep_fail(MWSEP_ERR_STATE);
-    int rc = wedge_set_stars(c, *c->wedges[0], n, l, b, r);
+    if (c->ev_stars) CU(cudaStreamWaitEvent(c->stream, c->ev_stars, 0));
+    int rc = wedge_set_stars(c, *c->wedges[0], n, l, b, r, c->stream);
     if (rc) return rc;
     c->eng.desc_dirty = true;
     CU(cudaStreamSynchronize(c->stream));
@@ -1139,7 +1215,7 @@ extern "C" int mwsep_ctx_set_stars(mwsep_ctx* c, const STAR_POINTS* sp)
     if (!c || !sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
     CU(cudaSetDevice(c->device));
     if (c->wedges.empty()) return mwsep_fail(MWSEP_ERR_STATE);
-    int rc = wedge_set_stars_rows(c, *c->wedges[0], sp);
+    int rc = wedge_set_stars_rows(c, *c->wedges[0], sp, false);
     if (rc) return rc;
     c->eng.desc_dirty = true;
     return MWSEP_OK;
@@ -1224,14 +1300,36 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
     const size_t h2d0 = g_default->xfer_h2d, d2h0 = g_default->xfer_d2h;
     if (mwsep_set_astronomy_parameters(ap, parameters) != MWSEP_OK) return nan;
     if (mwsep_ctx_set_problem(g_default, ap) != MWSEP_OK) return nan;
-    if (mwsep_ctx_set_stars(g_default, sp) != MWSEP_OK) return nan;
     if (es->number_integrals != ap->number_integrals || es->number_streams != ap->number_streams || !es->integral)
     {
         mwsep_fail(MWSEP_ERR_STATE);
         return nan;
     }
+    /* the catalogue goes up on the side stream while the integral (which
+     * does not read it) runs; the likelihood waits for it */
+    mwsep_ctx* c = g_default;
+    if (!sp->stars || sp->number_stars < 1)
+    {
+        mwsep_fail(MWSEP_ERR_ARG);
+        return nan;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess)
+    {
+        mwsep_fail(MWSEP_ERR_CUDA);
+        return nan;
+    }
+    int rc = wedge_set_stars_rows(c, *c->wedges[0], sp, true);
+    c->eng.desc_dirty = true;
     mwsep_result r;
-    if (mwsep_ctx_evaluate(g_default, parameters, precision, &r) != MWSEP_OK) return nan;
+    if (rc == MWSEP_OK) rc = mwsep_ctx_evaluate(c, parameters, precision, &r);
+    if (c->stars_pending)
+    {
+        /* an evaluation that stopped early still leaves valid star tables */
+        const int rc2 = launch_star_build(c, nullptr);
+        if (cudaEventSynchronize(c->ev_stars) != cudaSuccess || rc2) rc = rc ? rc : mwsep_fail(MWSEP_ERR_CUDA);
+        c->stars_pending = false;
+    }
+    if (rc != MWSEP_OK) return nan;
     g_last_h2d = g_default->xfer_h2d - h2d0;
     g_last_d2h = g_default->xfer_d2h - d2h0;
 

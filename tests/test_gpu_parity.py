@@ -108,6 +108,29 @@ def test_evalfunc_dropin(built_library, name):
     assert _close_rel(es2.prob_sum, g["prob_sum"], 1e-12)
 
 
+def test_evalfunc_alternating_catalogues(gpu_ctx):
+    """The EvalFunc entries upload each call's catalogue on a side stream
+    while the integral runs: alternating two problems whose catalogues
+    differ in size and content, every call in every form gives the same bits
+    as the context API, which uploads synchronously."""
+    import milkywayathome_client_gb300 as mw
+    cases = []
+    for name in ("three_streams", "basic_1stream"):
+        pf, sf, g = load_case(name)
+        ap, sp = mw.AstronomyParameters.read(pf), mw.StarPoints.read(sf)
+        gpu_ctx.set_problem(ap)
+        gpu_ctx.set_stars(sp)
+        want = {p: gpu_ctx.evaluate(g["theta"], p).likelihood for p in (0, 1, 2)}
+        cases.append((ap, sp, g, want))
+    assert cases[0][1].number_stars != cases[1][1].number_stars
+    fns = {0: mw.evaluate, 1: mw.evaluate_mixed, 2: mw.evaluate_df}
+    for _ in range(3):
+        for ap, sp, g, want in cases:
+            for p, fn in fns.items():
+                es = mw.EvaluationState(ap, sp)
+                assert fn(g["theta"], ap, es, sp) - 3.0 == want[p], (p, want[p])
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_equals_single_bitwise(gpu_ctx, precision):
     """Each result of a batch is bit-identical to the same theta alone."""
