@@ -303,7 +303,7 @@ double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUA
 
 /* Same contract in the double-float form (MWSEP_PLAIN_DF): the plain form's
  * bounds (1e-12 relative on the integrals, 1e-12 absolute on the
- * log-likelihood) at about 13x its speed; problems outside that form's
+ * log-likelihood) at about 12x its speed; problems outside that form's
  * coverage are evaluated as mwsep_evaluate does. */
 double mwsep_evaluate_df(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
 
