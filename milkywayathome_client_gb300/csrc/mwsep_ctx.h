@@ -175,7 +175,8 @@ struct mwsep_ctx
     cudaStream_t side = nullptr;
     cudaEvent_t ev_main = nullptr, ev_stars = nullptr;
     bool stars_pending = false;
-    mwsep::Wedge* stars_build = nullptr; /* its star-table build not yet launched */
+    mwsep::Wedge* stars_build = nullptr;    /* its rows not yet gathered, uploaded and built from */
+    const STAR_POINTS* stars_rows = nullptr;
     size_t dev_bytes = 0;
     size_t hbm_budget = 0; /* 0: no budget */
 
@@ -210,14 +211,14 @@ int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap);
 int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
                     cudaStream_t st);
 /* From STAR_POINTS rows: synchronously on the context's stream, or (on_side)
- * on the side stream with ev_stars recorded and stars_pending set. */
+ * deferred to launch_star_build with stars_pending set (sp must stay valid
+ * until then). */
 int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side);
 /* Make st wait for a pending side-stream catalogue upload. */
 int wait_stars(mwsep_ctx* c, cudaStream_t st);
-/* Launch a deferred side-stream star-table build (after event `after`, if
- * given) and record ev_stars. */
+/* Gather, upload and build from a deferred catalogue on the side stream
+ * (the build after event `after`, if given) and record ev_stars. */
 int launch_star_build(mwsep_ctx* c, cudaEvent_t after);
-int launch_star_tables_for(mwsep_ctx* c, Wedge& w, cudaStream_t st);
 void wedge_release(mwsep_ctx* c, Wedge& w);
 void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items);
 /* r-bins per warp tile that make a tile's points whole lane groups. */

@@ -647,19 +647,10 @@ int warp_tile_kstep(int convolve, int n_streams)
     return group / a;
 }
 
-int launch_star_tables_for(mwsep_ctx* c, Wedge& w, cudaStream_t st)
+/* Device buffers and views of an n-star catalogue (contents uploaded by
+ * upload_stars). */
+int prepare_stars(mwsep_ctx* c, Wedge& w, int n)
 {
-    CK(mwsep_launch_star_tables(w.n_stars, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(),
-                                w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
-                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
-                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
-    return MWSEP_OK;
-}
-
-int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
-                    cudaStream_t st)
-{
-    mwsep::Range nvtx_range("mwsep.set_stars");
     if (!w.has_problem) return mwsep_fail(MWSEP_ERR_STATE);
     if (n < 1) return mwsep_fail(MWSEP_ERR_ARG);
     const int C = w.prob.convolve;
@@ -679,17 +670,6 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     rc |= w.s_pts.ensure(NC * sizeof(float4), tot);
     w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
-    CU(h2d(c, w.s_l.p, l, (size_t)n * 8, st));
-    CU(h2d(c, w.s_b.p, b, (size_t)n * 8, st));
-    CU(h2d(c, w.s_r.p, r, (size_t)n * 8, st));
-    w.n_stars = n;
-    if (st == c->side)
-        c->stars_build = &w; /* launched by launch_star_build once the integral is queued */
-    else
-    {
-        int rc2 = launch_star_tables_for(c, w, st);
-        if (rc2) return rc2;
-    }
     mwsep_stars_dev& v = w.stars_view;
     v.n_stars = n;
     v.convolve = C;
@@ -711,29 +691,63 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     return MWSEP_OK;
 }
 
-int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side)
+/* The catalogue's columns to the device and the star tables built from
+ * them, on stream st (the build after event `after`, if given). */
+int upload_stars(mwsep_ctx* c, Wedge& w, const double* l, const double* b, const double* r, cudaStream_t st,
+                 cudaEvent_t after)
 {
-    if (!sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
+    const size_t bytes = (size_t)w.n_stars * 8;
+    CU(h2d(c, w.s_l.p, l, bytes, st));
+    CU(h2d(c, w.s_b.p, b, bytes, st));
+    CU(h2d(c, w.s_r.p, r, bytes, st));
+    if (after) CU(cudaStreamWaitEvent(st, after, 0));
+    CK(mwsep_launch_star_tables(w.n_stars, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(),
+                                w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
+                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
+                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
+    return MWSEP_OK;
+}
+
+int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
+                    cudaStream_t st)
+{
+    mwsep::Range nvtx_range("mwsep.set_stars");
+    int rc = prepare_stars(c, w, n);
+    if (rc) return rc;
+    return upload_stars(c, w, l, b, r, st, nullptr);
+}
+
+/* STAR_POINTS rows (l, b, r) into the wedge's pinned staging columns. */
+static void gather_rows(Wedge& w, const STAR_POINTS* sp)
+{
     const int n = sp->number_stars;
-    /* an earlier side-stream upload may still read the staging buffer */
-    if (c->ev_stars) CU(cudaEventSynchronize(c->ev_stars));
-    if (w.h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
     double* l = w.h_stars.as<double>();
     double* b = l + n;
     double* r = b + n;
     for (int i = 0; i < n; ++i)
     {
         const double* row = sp->stars[i];
-        if (!row) return mwsep_fail(MWSEP_ERR_ARG);
         l[i] = row[0];
         b[i] = row[1];
         r[i] = row[2];
     }
+}
+
+int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side)
+{
+    if (!sp || !sp->stars || sp->number_stars < 1) return mwsep_fail(MWSEP_ERR_ARG);
+    const int n = sp->number_stars;
+    for (int i = 0; i < n; ++i)
+        if (!sp->stars[i]) return mwsep_fail(MWSEP_ERR_ARG);
+    /* an earlier side-stream upload may still read the staging buffer or
+     * write the star tables */
+    if (c->ev_stars) CU(cudaEventSynchronize(c->ev_stars));
+    if (w.h_stars.ensure((size_t)n * 3 * sizeof(double))) return mwsep_fail(MWSEP_ERR_NOMEM);
     if (!on_side)
     {
-        /* an earlier side-stream upload still writing the star tables */
-        if (c->ev_stars) CU(cudaStreamWaitEvent(c->stream, c->ev_stars, 0));
-        int rc = wedge_set_stars(c, w, n, l, b, r, c->stream);
+        gather_rows(w, sp);
+        const double* l = w.h_stars.as<double>();
+        int rc = wedge_set_stars(c, w, n, l, l + n, l + 2 * (size_t)n, c->stream);
         if (rc) return rc;
         /* the pinned staging buffer is reused: wait for the copies */
         CU(cudaStreamSynchronize(c->stream));
@@ -741,19 +755,21 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_
     }
     /* on the side stream, after everything already queued on the context's
      * stream (the problem tables the star tables are built from, earlier
-     * readers of the star tables): the copies now, the table build when
-     * launch_star_build is called; the readers of this upload wait for
-     * ev_stars */
+     * readers of the star tables); the rows are gathered, copied and built
+     * from when launch_star_build is called, and the readers of this upload
+     * wait for ev_stars */
     if (!c->side)
     {
         CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
         CU(cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
         CU(cudaEventCreateWithFlags(&c->ev_stars, cudaEventDisableTiming));
     }
+    int rc = prepare_stars(c, w, n);
+    if (rc) return rc;
     CU(cudaEventRecord(c->ev_main, c->stream));
     CU(cudaStreamWaitEvent(c->side, c->ev_main, 0));
-    int rc = wedge_set_stars(c, w, n, l, b, r, c->side);
-    if (rc) return rc;
+    c->stars_build = &w;
+    c->stars_rows = sp;
     c->stars_pending = true;
     return MWSEP_OK;
 }
@@ -762,9 +778,13 @@ int launch_star_build(mwsep_ctx* c, cudaEvent_t after)
 {
     if (!c->stars_build) return MWSEP_OK;
     Wedge& w = *c->stars_build;
+    const STAR_POINTS* sp = c->stars_rows;
     c->stars_build = nullptr;
-    if (after) CU(cudaStreamWaitEvent(c->side, after, 0));
-    int rc = launch_star_tables_for(c, w, c->side);
+    c->stars_rows = nullptr;
+    gather_rows(w, sp);
+    const double* l = w.h_stars.as<double>();
+    const size_t n = (size_t)w.n_stars;
+    int rc = upload_stars(c, w, l, l + n, l + 2 * n, c->side, after);
     if (rc) return rc;
     CU(cudaEventRecord(c->ev_stars, c->side));
     return MWSEP_OK;
