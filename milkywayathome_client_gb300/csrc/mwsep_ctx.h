@@ -173,7 +173,7 @@ struct mwsep_ctx
      * integral runs; star-table readers on `stream` wait for ev_stars while
      * stars_pending (created on first use). */
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_main = nullptr, ev_stars = nullptr;
+    cudaEvent_t ev_main = nullptr, ev_stars = nullptr, ev_dens = nullptr;
     bool stars_pending = false;
     mwsep::Wedge* stars_build = nullptr;    /* its rows not yet gathered, uploaded and built from */
     const STAR_POINTS* stars_rows = nullptr;
@@ -185,6 +185,7 @@ struct mwsep_ctx
 
     /* single-problem path (wedge 0) */
     mwsep::DevBuf d_theta, d_partials, d_lkpartials, d_out;
+    mwsep::DevBuf d_dens; /* compensated likelihood: per-star densities of the batch */
     mwsep::HostPinned h_theta, h_out;
     /* separation output of wedge 0 (mwsep_separation.cu) */
     mwsep::DevBuf d_sprob, d_assign, d_xyz;
@@ -214,6 +215,8 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
  * deferred to launch_star_build with stars_pending set (sp must stay valid
  * until then). */
 int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_side);
+/* The side stream and its events (created on first use). */
+int ensure_side(mwsep_ctx* c);
 /* Make st wait for a pending side-stream catalogue upload. */
 int wait_stars(mwsep_ctx* c, cudaStream_t st);
 /* Gather, upload and build from a deferred catalogue on the side stream

@@ -109,6 +109,64 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
                             partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }
 
+/* The likelihood in two launches: the per-star densities, which need no
+ * integral (so they can run beside the integral kernel), into
+ * dens[theta][1 + S][star]; then the epilogue over the integrals, with the
+ * fused kernel's grid, star order and reduction (the same bits). */
+template <int S>
+__global__ void __launch_bounds__(kBlock) likelihood_f32_density_kernel(const mwsep_stars_dev St,
+                                                                        const mwsep_theta_consts* __restrict__ thetas,
+                                                                        double* __restrict__ dens)
+{
+    __shared__ mwsep_theta_consts th;
+    load_theta(th, thetas + blockIdx.y);
+    __syncthreads();
+    const BgConsts bc = bg_consts(th);
+    const int N = St.n_stars, NS = th.n_streams;
+    double* d = dens + (size_t)blockIdx.y * (1 + S) * N;
+    for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
+    {
+        double bg, st[SArr<S>::N];
+        star_density<S>(St, th, bc, s0, bg, st);
+        d[s0] = bg;
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+            if (s < NS) d[(size_t)(1 + s) * N + s0] = st[s];
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) likelihood_f32_finish_kernel(int N,
+                                                                       const mwsep_theta_consts* __restrict__ thetas,
+                                                                       const double* __restrict__ integrals,
+                                                                       const double* __restrict__ dens,
+                                                                       double2* __restrict__ partials,
+                                                                       long long theta_stride)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ double red[2 * (3 + S) * 32];
+    __shared__ LkScale<S> ks;
+    load_theta(th, thetas + blockIdx.y);
+    __syncthreads();
+    const int NS = th.n_streams;
+    if (threadIdx.x == 0) lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
+    __syncthreads();
+
+    double acc[3 + S];
+#pragma unroll
+    for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
+    const double* d = dens + (size_t)blockIdx.y * (1 + S) * N;
+    for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
+    {
+        double st[SArr<S>::N];
+#pragma unroll
+        for (int s = 0; s < S; ++s) st[s] = (s < NS) ? d[(size_t)(1 + s) * N + s0] : 0.0;
+        star_epilogue<S>(th, ks, d[s0], st, acc);
+    }
+    reduce_and_store<3 + S>(acc, 3 + NS, red,
+                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
+}
+
 template <int S>
 int launch_integral(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
                     int form, double2* partials, cudaStream_t st)
@@ -147,6 +205,25 @@ int launch_likelihood(const mwsep_stars_dev* St, const mwsep_theta_consts* th, c
     const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
     dim3 g(sh->grid, sh->n_theta);
     likelihood_f32_kernel<S><<<g, kBlock, 0, st>>>(*St, th, integrals, partials, theta_stride);
+    return (int)cudaGetLastError();
+}
+
+template <int S>
+int launch_density(const mwsep_stars_dev* St, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
+                   double* dens, cudaStream_t st)
+{
+    dim3 g(sh->grid, sh->n_theta);
+    likelihood_f32_density_kernel<S><<<g, kBlock, 0, st>>>(*St, th, dens);
+    return (int)cudaGetLastError();
+}
+
+template <int S>
+int launch_finish(int n_stars, const mwsep_theta_consts* th, const mwsep_launch_shape* sh, const double* integrals,
+                  const double* dens, double2* partials, cudaStream_t st)
+{
+    const long long theta_stride = (long long)sh->grid * (3 + sh->n_streams);
+    dim3 g(sh->grid, sh->n_theta);
+    likelihood_f32_finish_kernel<S><<<g, kBlock, 0, st>>>(n_stars, th, integrals, dens, partials, theta_stride);
     return (int)cudaGetLastError();
 }
 
@@ -216,6 +293,37 @@ extern "C" int mwsep_launch_likelihood_f32(const mwsep_stars_dev* stars, const m
     case 3: return launch_likelihood<3>(stars, th_dev, sh, integrals, partials, st);
     case 4: return launch_likelihood<4>(stars, th_dev, sh, integrals, partials, st);
     default: return launch_likelihood<8>(stars, th_dev, sh, integrals, partials, st);
+    }
+}
+
+extern "C" int mwsep_launch_likelihood_f32_density(const mwsep_stars_dev* stars, const mwsep_theta_consts* th_dev,
+                                                   const mwsep_launch_shape* sh, double* dens, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_density<0>(stars, th_dev, sh, dens, st);
+    case 1: return launch_density<1>(stars, th_dev, sh, dens, st);
+    case 2: return launch_density<2>(stars, th_dev, sh, dens, st);
+    case 3: return launch_density<3>(stars, th_dev, sh, dens, st);
+    case 4: return launch_density<4>(stars, th_dev, sh, dens, st);
+    default: return launch_density<8>(stars, th_dev, sh, dens, st);
+    }
+}
+
+extern "C" int mwsep_launch_likelihood_f32_finish(int n_stars, const mwsep_theta_consts* th_dev,
+                                                  const mwsep_launch_shape* sh, const double* integrals,
+                                                  const double* dens, double2* partials, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_finish<0>(n_stars, th_dev, sh, integrals, dens, partials, st);
+    case 1: return launch_finish<1>(n_stars, th_dev, sh, integrals, dens, partials, st);
+    case 2: return launch_finish<2>(n_stars, th_dev, sh, integrals, dens, partials, st);
+    case 3: return launch_finish<3>(n_stars, th_dev, sh, integrals, dens, partials, st);
+    case 4: return launch_finish<4>(n_stars, th_dev, sh, integrals, dens, partials, st);
+    default: return launch_finish<8>(n_stars, th_dev, sh, integrals, dens, partials, st);
     }
 }
 

@@ -862,15 +862,14 @@ __device__ __forceinline__ void lk_scale(const mwsep_theta_consts& th, const dou
     k.inv_sw = 1.0 / th.sum_exp_weights;
 }
 
-/* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717):
- * the density sums in FP32, everything after them in FP64.  acc slots:
- * [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
+/* One star's densities (cpu/evaluation_optimized.c:672-690): the
+ * background's (-1 for q = 0) and each stream's, summed over the star's
+ * convolution points in FP32 and returned in FP64 with the stream's exponent
+ * shift undone (the star weights carry its reff_xr_rp3). */
 template <int S>
-__device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                                const BgConsts& bc, const LkScale<S>& ks, int s0,
-                                                double (&acc)[3 + S])
+__device__ __forceinline__ void star_density(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
+                                             const BgConsts& bc, int s0, double& bg, double (&st)[SArr<S>::N])
 {
-    const int NS = th.n_streams;
     const int N = St.n_stars;
     Col<S> cc;
     s0 = (int)MWSEP_IDX(s0, N, 7);
@@ -890,8 +889,19 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     case BG_GENERAL: convolve<S, BG_GENERAL>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
     default: convolve<S, BG_NONE>(St.pts + s0, N, St.convolve, cc, bc, bgf, stf); break;
     }
-    /* the star weights carry its reff_xr_rp3 */
-    const double bg = (th.bg_mode == 2) ? -1.0 : (double)bgf;
+    bg = (th.bg_mode == 2) ? -1.0 : (double)bgf;
+#pragma unroll
+    for (int s = 0; s < S; ++s) st[s] = (double)stf[s] * exp_scale(eref[s]);
+}
+
+/* The rest of calculate_likelihood for one star (cpu/evaluation_optimized.c:
+ * 692-717), in FP64: the mixture weights over the integrals, log10 sums.
+ * acc slots: [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
+template <int S>
+__device__ __forceinline__ void star_epilogue(const mwsep_theta_consts& th, const LkScale<S>& ks, double bg,
+                                              const double (&st)[SArr<S>::N], double (&acc)[3 + S])
+{
+    const int NS = th.n_streams;
     double bg_only = bg * ks.bg;
     double star_prob = bg_only;
     acc[2] += (bg_only == 0.0) ? -238.0 : log10(bg_only * ks.inv_sw);
@@ -900,7 +910,7 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
     {
         if (s < NS)
         {
-            double st_only = (double)stf[s] * exp_scale(eref[s]) * ks.st[s];
+            double st_only = st[s] * ks.st[s];
             star_prob += st_only;
             acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only * ks.inv_sw);
         }
@@ -913,6 +923,18 @@ __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const
         acc[0] += -238.0;
         acc[1] += 1.0;
     }
+}
+
+/* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717):
+ * the density sums in FP32, everything after them in FP64. */
+template <int S>
+__device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
+                                                const BgConsts& bc, const LkScale<S>& ks, int s0,
+                                                double (&acc)[3 + S])
+{
+    double bg, st[SArr<S>::N];
+    star_density<S>(St, th, bc, s0, bg, st);
+    star_epilogue<S>(th, ks, bg, st, acc);
 }
 
 } // namespace f32

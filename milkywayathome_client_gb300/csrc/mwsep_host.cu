@@ -758,19 +758,25 @@ int wedge_set_stars_rows(mwsep_ctx* c, Wedge& w, const STAR_POINTS* sp, bool on_
      * readers of the star tables); the rows are gathered, copied and built
      * from when launch_star_build is called, and the readers of this upload
      * wait for ev_stars */
-    if (!c->side)
-    {
-        CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-        CU(cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
-        CU(cudaEventCreateWithFlags(&c->ev_stars, cudaEventDisableTiming));
-    }
-    int rc = prepare_stars(c, w, n);
+    int rc = ensure_side(c);
+    if (rc) return rc;
+    rc = prepare_stars(c, w, n);
     if (rc) return rc;
     CU(cudaEventRecord(c->ev_main, c->stream));
     CU(cudaStreamWaitEvent(c->side, c->ev_main, 0));
     c->stars_build = &w;
     c->stars_rows = sp;
     c->stars_pending = true;
+    return MWSEP_OK;
+}
+
+int ensure_side(mwsep_ctx* c)
+{
+    if (c->side) return MWSEP_OK;
+    CU(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->ev_stars, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->ev_dens, cudaEventDisableTiming));
     return MWSEP_OK;
 }
 
@@ -948,7 +954,16 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     rc |= c->d_lkpartials.ensure(lkpart_bytes, tot);
     rc |= c->d_out.ensure(out_doubles * 8, tot);
     rc |= c->h_out.ensure(out_doubles * 8);
+    /* the compensated likelihood's densities need no integral: computed on
+     * the side stream beside the integral kernel */
+    const bool split_lk = precision == MWSEP_MIXED_F32 && env_long("MWSEP_SPLIT_LIKELIHOOD", 1) != 0;
+    if (split_lk) rc |= c->d_dens.ensure((size_t)B * (1 + (S <= 4 ? S : 8)) * w.n_stars * sizeof(double), tot);
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
+    if (split_lk)
+    {
+        rc = ensure_side(c);
+        if (rc) return rc;
+    }
     if (df_likelihood && !w.has_star_df)
     {
         const size_t before = tot, need = (size_t)w.n_stars * p.convolve * sizeof(float4);
@@ -1022,6 +1037,20 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
      * integral's blocks leave */
     rc = launch_star_build(c, c->ev[1]);
     if (rc) return rc;
+    mwsep_launch_shape lk = sh;
+    lk.block = t.lk_block;
+    lk.grid = t.lk_grid;
+    lk.area_index = 0;
+    if (split_lk)
+    {
+        /* after the parameter upload (and everything before it on the
+         * context's stream, e.g. the last reader of the densities) */
+        CU(cudaStreamWaitEvent(c->side, c->ev[1], 0));
+        CK(mwsep_launch_likelihood_f32_density(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk,
+                                               c->d_dens.as<double>(), c->side));
+        CU(cudaEventRecord(c->ev_dens, c->side));
+        ++launches;
+    }
     CU(cudaEventRecord(c->ev[2], st));
     CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
     ++launches;
@@ -1035,10 +1064,6 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
                                       w.s_ptsdf.as<float4>(), st));
         w.has_star_df = true;
     }
-    mwsep_launch_shape lk = sh;
-    lk.block = t.lk_block;
-    lk.grid = t.lk_grid;
-    lk.area_index = 0;
     if (df_likelihood)
     {
         int n_forms = 0;
@@ -1054,6 +1079,12 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     else if (precision != MWSEP_MIXED_F32)
         CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
+    else if (split_lk)
+    {
+        CU(cudaStreamWaitEvent(st, c->ev_dens, 0));
+        CK(mwsep_launch_likelihood_f32_finish(w.n_stars, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                              c->d_dens.as<double>(), c->d_lkpartials.as<double2>(), st));
+    }
     else
         CK(mwsep_launch_likelihood_f32(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
                                        c->d_lkpartials.as<double2>(), st));
@@ -1169,6 +1200,7 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     if (!c) return mwsep_fail(MWSEP_ERR_ARG);
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     mwsep_engine_release(c);
     if (!c->shared_wedges)
         for (Wedge* w : c->wedges)
@@ -1179,16 +1211,16 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     c->wedges.clear();
     size_t& t = c->dev_bytes;
     DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out,
-                      &c->d_sprob, &c->d_assign, &c->d_xyz};
+                      &c->d_sprob, &c->d_assign, &c->d_xyz, &c->d_dens};
     for (DevBuf* b : bufs) b->release(t);
     c->h_theta.release();
     c->h_out.release();
     c->h_sep.release();
     for (int i = 0; i < 6; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-    if (c->side) cudaStreamSynchronize(c->side);
     if (c->ev_main) cudaEventDestroy(c->ev_main);
     if (c->ev_stars) cudaEventDestroy(c->ev_stars);
+    if (c->ev_dens) cudaEventDestroy(c->ev_dens);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -247,6 +247,15 @@ int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep_theta_cons
 int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
                                 const mwsep_launch_shape* shape, const double* integrals,
                                 double2* partials, void* stream);
+/* The same likelihood in two launches: per-star densities into
+ * dens[theta][1 + S_max][star] (S_max = 8 beyond 4 streams), needing no
+ * integral; then the epilogue and the per-block partials, bit for bit those
+ * of mwsep_launch_likelihood_f32 on the same shape. */
+int mwsep_launch_likelihood_f32_density(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
+                                        const mwsep_launch_shape* shape, double* dens, void* stream);
+int mwsep_launch_likelihood_f32_finish(int n_stars, const mwsep_theta_consts* th_dev,
+                                       const mwsep_launch_shape* shape, const double* integrals,
+                                       const double* dens, double2* partials, void* stream);
 /* Resident blocks per SM of the integral kernels (persistent-grid sizing). */
 int mwsep_integral_f32_blocks_per_sm(int n_streams, int warp_items);
 /* double-float integral (mwsep_df.cu) */

@@ -131,6 +131,29 @@ def test_evalfunc_alternating_catalogues(gpu_ctx):
                 assert fn(g["theta"], ap, es, sp) - 3.0 == want[p], (p, want[p])
 
 
+@pytest.mark.parametrize("name", ["three_streams", "aux_profile", "cut_area", "six_streams", "general_alpha_delta",
+                                  "stream_off"])
+def test_split_likelihood_equals_fused(gpu_ctx, name, monkeypatch):
+    """The compensated likelihood's two launches (per-star densities beside
+    the integral, then the epilogue) give the fused kernel's bits, alone and
+    in a batch."""
+    import milkywayathome_client_gb300 as mw
+    _, _, g = _setup(gpu_ctx, name)
+    base = np.asarray(g["theta"])
+    thetas = [base * (1 + 1e-3 * k) for k in range(3)]
+    split = [gpu_ctx.evaluate(t, mw.MWSEP_MIXED_F32) for t in thetas]
+    split_b = gpu_ctx.evaluate_batch(thetas, mw.MWSEP_MIXED_F32)
+    monkeypatch.setenv("MWSEP_SPLIT_LIKELIHOOD", "0")
+    fused = [gpu_ctx.evaluate(t, mw.MWSEP_MIXED_F32) for t in thetas]
+    def same(x, y):  # equal bits, or both NaN (stream_off's likelihood is NaN, as the reference's)
+        return x == y or (math.isnan(x) and math.isnan(y))
+    for a, b, c in zip(split, split_b, fused):
+        assert same(a.likelihood, b.likelihood) and same(a.likelihood, c.likelihood)
+        assert same(a.background_only_likelihood, c.background_only_likelihood)
+        assert all(same(x, y) for x, y in zip(a.stream_only_likelihood, c.stream_only_likelihood))
+        assert a.num_zero == c.num_zero
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_equals_single_bitwise(gpu_ctx, precision):
     """Each result of a batch is bit-identical to the same theta alone."""
