@@ -1,8 +1,8 @@
 /* mwsep_reduce.cu -- fixed-order reductions of the per-block compensated
- * partials.  One block per (theta); each thread walks a fixed stride of the
- * partials, then the block combines error-free.  The result of a theta
- * depends only on its own partials and the grid size, never on what else
- * shares the launch. */
+ * partials.  One block per (component, theta), so the components reduce
+ * side by side; each thread walks a fixed stride of the partials, then the
+ * block combines error-free.  The result of a theta depends only on its own
+ * partials and the grid size, never on what else shares the launch. */
 #include <cuda_runtime.h>
 #include "mwsep_internal.h"
 #include "mwsep_reduce.cuh"
@@ -19,54 +19,50 @@ __global__ void __launch_bounds__(kReduceThreads)
     reduce_integrals_kernel(const double2* __restrict__ partials, int n_areas, int grid, int ncomp,
                             double* __restrict__ out_areas, double* __restrict__ out_integrals)
 {
+    /* block (c, t): component c of parameter vector t, every area, then
+     * I_c = I_c(area 0) - sum of the cut areas' (each component's order is
+     * independent of the others') */
     __shared__ double red[2 * 32];
-    const int t = blockIdx.x;
+    const int c = blockIdx.x, t = blockIdx.y;
     const double2* base = partials + (size_t)t * n_areas * grid * ncomp;
     double* areas = out_areas + (size_t)t * n_areas * ncomp;
     for (int a = 0; a < n_areas; ++a)
     {
-        for (int c = 0; c < ncomp; ++c)
+        comp_sum acc[1];
+        acc[0].zero();
+        for (int b = threadIdx.x; b < grid; b += blockDim.x)
         {
-            comp_sum acc[1];
-            acc[0].zero();
-            for (int b = threadIdx.x; b < grid; b += blockDim.x)
-            {
-                const double2 v = base[((size_t)a * grid + b) * ncomp + c];
-                acc[0].merge(v.x, v.y);
-            }
-            mwsep::block_reduce<1>(acc, red);
-            if (threadIdx.x == 0) areas[a * ncomp + c] = acc[0].s + acc[0].c;
-            __syncthreads();
+            const double2 v = base[((size_t)a * grid + b) * ncomp + c];
+            acc[0].merge(v.x, v.y);
         }
+        mwsep::block_reduce<1>(acc, red);
+        if (threadIdx.x == 0) areas[a * ncomp + c] = acc[0].s + acc[0].c;
+        __syncthreads();
     }
     if (threadIdx.x == 0)
     {
-        double* I = out_integrals + (size_t)t * ncomp;
-        for (int c = 0; c < ncomp; ++c) I[c] = areas[c];
-        for (int a = 1; a < n_areas; ++a)
-            for (int c = 0; c < ncomp; ++c) I[c] -= areas[a * ncomp + c];
+        double I = areas[c];
+        for (int a = 1; a < n_areas; ++a) I -= areas[a * ncomp + c];
+        out_integrals[(size_t)t * ncomp + c] = I;
     }
 }
 
 __global__ void __launch_bounds__(kReduceThreads)
     reduce_likelihood_kernel(const double2* __restrict__ partials, int grid, int nslots, double* __restrict__ out)
 {
+    /* block (c, t): slot c of parameter vector t */
     __shared__ double red[2 * 32];
-    const int t = blockIdx.x;
+    const int c = blockIdx.x, t = blockIdx.y;
     const double2* base = partials + (size_t)t * grid * nslots;
-    for (int c = 0; c < nslots; ++c)
+    comp_sum acc[1];
+    acc[0].zero();
+    for (int b = threadIdx.x; b < grid; b += blockDim.x)
     {
-        comp_sum acc[1];
-        acc[0].zero();
-        for (int b = threadIdx.x; b < grid; b += blockDim.x)
-        {
-            const double2 v = base[(size_t)b * nslots + c];
-            acc[0].merge(v.x, v.y);
-        }
-        mwsep::block_reduce<1>(acc, red);
-        if (threadIdx.x == 0) out[(size_t)t * nslots + c] = acc[0].s + acc[0].c;
-        __syncthreads();
+        const double2 v = base[(size_t)b * nslots + c];
+        acc[0].merge(v.x, v.y);
     }
+    mwsep::block_reduce<1>(acc, red);
+    if (threadIdx.x == 0) out[(size_t)t * nslots + c] = acc[0].s + acc[0].c;
 }
 
 } // namespace
@@ -74,7 +70,7 @@ __global__ void __launch_bounds__(kReduceThreads)
 extern "C" int mwsep_launch_reduce_integrals(const double2* partials, const mwsep_launch_shape* sh,
                                              double* out_areas, double* out_integrals, void* stream)
 {
-    reduce_integrals_kernel<<<sh->n_theta, kReduceThreads, 0, (cudaStream_t)stream>>>(
+    reduce_integrals_kernel<<<dim3(1 + sh->n_streams, sh->n_theta), kReduceThreads, 0, (cudaStream_t)stream>>>(
         partials, sh->n_areas, sh->grid, 1 + sh->n_streams, out_areas, out_integrals);
     return (int)cudaGetLastError();
 }
@@ -82,8 +78,8 @@ extern "C" int mwsep_launch_reduce_integrals(const double2* partials, const mwse
 extern "C" int mwsep_launch_reduce_likelihood(const double2* partials, const mwsep_launch_shape* sh, double* out,
                                               void* stream)
 {
-    reduce_likelihood_kernel<<<sh->n_theta, kReduceThreads, 0, (cudaStream_t)stream>>>(partials, sh->grid,
-                                                                                      3 + sh->n_streams, out);
+    reduce_likelihood_kernel<<<dim3(3 + sh->n_streams, sh->n_theta), kReduceThreads, 0, (cudaStream_t)stream>>>(
+        partials, sh->grid, 3 + sh->n_streams, out);
     return (int)cudaGetLastError();
 }
 
