@@ -185,7 +185,9 @@ struct mwsep_ctx
 
     /* single-problem path (wedge 0) */
     mwsep::DevBuf d_theta, d_partials, d_lkpartials, d_out;
-    mwsep::DevBuf d_dens; /* compensated likelihood: per-star densities of the batch */
+    mwsep::DevBuf d_dens;    /* compensated likelihood: per-star densities of the batch */
+    mwsep::DevBuf d_tilectr; /* compensated integral: tile counters per (theta, area) */
+    mwsep::DevBuf d_segpart; /* and the first-level sums of its per-tile slots */
     mwsep::HostPinned h_theta, h_out;
     /* separation output of wedge 0 (mwsep_separation.cu) */
     mwsep::DevBuf d_sprob, d_assign, d_xyz;

@@ -79,6 +79,54 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
                             partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams));
 }
 
+/* The warp-tile integral with tiles handed out by a counter: the warp
+ * scheduler favours the older of an SM's two blocks (measured: ~0.42 against
+ * ~0.62 ms per tile on the full-size wedge), so a fixed share per warp left
+ * one block alone for the last third of the launch.  Each tile's sums are
+ * added across the warp in a fixed order and written to the tile's own slot
+ * (tile-major, 1 + S components), which the fixed-order reduction then sums:
+ * the result does not depend on which warp took which tile. */
+template <int S, int FORM>
+__global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_dyn_kernel(
+    const mwsep_area_dev A, const mwsep_theta_consts* __restrict__ thetas, double2* __restrict__ slots,
+    long long theta_stride, int* __restrict__ counters, int counter_stride)
+{
+    __shared__ mwsep_theta_consts th;
+    __shared__ __align__(16) float cs[kBlock / 32][TileSmem<S>::N];
+    load_theta(th, thetas + blockIdx.y);
+    __syncthreads();
+    if (mwsep_bg_form(&th) != FORM) return;
+    const BgConsts bc = bg_consts(th);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int NC = 1 + th.n_streams;
+    int* ctr = counters + (size_t)blockIdx.y * counter_stride;
+    double2* out = slots + (size_t)blockIdx.y * theta_stride;
+    for (;;)
+    {
+        int wt = 0;
+        if (lane == 0) wt = atomicAdd(ctr, 1);
+        wt = __shfl_sync(0xffffffffu, wt, 0);
+        if ((long long)wt >= A.n_items) break;
+        double acc[1 + S];
+#pragma unroll
+        for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
+        if constexpr (PackedTile<S>::ok)
+            warp_tile2<S, FORM>(A, th, bc, wt, cs[warp], acc);
+        else
+            warp_tile<S, FORM>(A, th, bc, wt, cs[warp], acc);
+#pragma unroll
+        for (int k = 0; k < 1 + S; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int k = 0; k < 1 + S; ++k)
+                if (k < NC) out[(size_t)wt * NC + k] = make_double2(acc[k], 0.0);
+        }
+    }
+}
+
 /* calculate_likelihood per star (cpu/evaluation_optimized.c:665-717); the
  * density sums in FP32, everything after them in FP64. */
 template <int S>
@@ -199,6 +247,34 @@ int launch_integral(const mwsep_area_dev* A, const mwsep_theta_consts* th, const
 }
 
 template <int S>
+int launch_integral_dyn(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
+                        long long n_slots, double2* slots, int* counters, cudaStream_t st)
+{
+    const long long ncomp = 1 + sh->n_streams;
+    const long long theta_stride = (long long)sh->n_areas * n_slots * ncomp;
+    double2* base = slots + (size_t)sh->area_index * n_slots * ncomp;
+    int* ctr = counters + sh->area_index;
+    dim3 g(sh->grid, sh->n_theta);
+    switch (sh->bg_form)
+    {
+    case BG_HERNQUIST:
+        integral_f32w_dyn_kernel<S, BG_HERNQUIST><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+        break;
+    case BG_HERNQUIST_AUX:
+        integral_f32w_dyn_kernel<S, BG_HERNQUIST_AUX>
+            <<<g, kBlock, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+        break;
+    case BG_GENERAL:
+        integral_f32w_dyn_kernel<S, BG_GENERAL><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+        break;
+    default:
+        integral_f32w_dyn_kernel<S, BG_NONE><<<g, kBlock, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+        break;
+    }
+    return (int)cudaGetLastError();
+}
+
+template <int S>
 int launch_likelihood(const mwsep_stars_dev* St, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
                       const double* integrals, double2* partials, cudaStream_t st)
 {
@@ -277,6 +353,23 @@ extern "C" int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep
     case 3: return launch_integral<3>(area, th_dev, sh, form, partials, st);
     case 4: return launch_integral<4>(area, th_dev, sh, form, partials, st);
     default: return launch_integral<8>(area, th_dev, sh, form, partials, st);
+    }
+}
+
+extern "C" int mwsep_launch_integral_f32_dyn(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                             const mwsep_launch_shape* sh, long long n_slots, double2* slots,
+                                             int* counters, void* stream)
+{
+    if (!area->warp_items) return (int)cudaErrorInvalidValue;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_integral_dyn<0>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 1: return launch_integral_dyn<1>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 2: return launch_integral_dyn<2>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 3: return launch_integral_dyn<3>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 4: return launch_integral_dyn<4>(area, th_dev, sh, n_slots, slots, counters, st);
+    default: return launch_integral_dyn<8>(area, th_dev, sh, n_slots, slots, counters, st);
     }
 }
 

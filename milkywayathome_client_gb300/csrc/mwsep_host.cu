@@ -945,7 +945,28 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4;
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
     const Tune& t = w.tune[precision];
-    const size_t part_bytes = sizeof(double2) * (size_t)B * A * t.grid * ncomp;
+    /* the compensated warp tiles with a tile counter write one slot per tile
+     * (per theta and area); batches go through in theta chunks whose slots
+     * fit kDynSlotBytes (each theta's sum is its own, whatever the chunk) */
+    long long n_slots = 0;
+    if (precision == MWSEP_MIXED_F32 && t.warp_items)
+        for (int a = 0; a < A; ++a)
+        {
+            mwsep_area_dev v = w.areas[a].view;
+            set_chunking(v, t.k_chunk, t.warp_items);
+            n_slots = std::max(n_slots, v.n_items);
+        }
+    const bool dyn = n_slots > 0 && n_slots < (1LL << 30) && env_long("MWSEP_F32_DYNAMIC", 1) != 0;
+    constexpr size_t kDynSlotBytes = (size_t)512 << 20;
+    const size_t slot_bytes_theta = sizeof(double2) * (size_t)A * n_slots * ncomp;
+    constexpr int kSegLen = 1024; /* slots per first-level reduction block */
+    const long long n_seg = (n_slots + kSegLen - 1) / kSegLen;
+    const int dyn_chunk =
+        dyn ? (int)std::max<size_t>(1, std::min<size_t>({(size_t)B, kDynSlotBytes / slot_bytes_theta,
+                                                         (size_t)(65535 / A)}))
+            : B;
+    const size_t part_bytes =
+        dyn ? slot_bytes_theta * dyn_chunk : sizeof(double2) * (size_t)B * A * t.grid * ncomp;
     const size_t lkpart_bytes = sizeof(double2) * (size_t)B * t.lk_grid * nslots;
     const size_t out_doubles = (size_t)B * (A * ncomp + ncomp + nslots);
     int rc = 0;
@@ -958,6 +979,11 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
      * the side stream beside the integral kernel */
     const bool split_lk = precision == MWSEP_MIXED_F32 && env_long("MWSEP_SPLIT_LIKELIHOOD", 1) != 0;
     if (split_lk) rc |= c->d_dens.ensure((size_t)B * (1 + (S <= 4 ? S : 8)) * w.n_stars * sizeof(double), tot);
+    if (dyn)
+    {
+        rc |= c->d_tilectr.ensure((size_t)dyn_chunk * A * sizeof(int), tot);
+        rc |= c->d_segpart.ensure(sizeof(double2) * (size_t)dyn_chunk * A * n_seg * ncomp, tot);
+    }
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
     if (split_lk)
     {
@@ -1020,7 +1046,7 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
                 ++launches;
             }
         }
-        else
+        else if (!dyn)
         {
             for (int form = 0; form < 4; ++form)
             {
@@ -1030,6 +1056,41 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
                                              c->d_partials.as<double2>(), st));
                 ++launches;
             }
+        }
+    }
+    if (dyn)
+    {
+        for (int b0 = 0; b0 < B; b0 += dyn_chunk)
+        {
+            const int nb = std::min(dyn_chunk, B - b0);
+            CU(cudaMemsetAsync(c->d_tilectr.p, 0, (size_t)nb * A * sizeof(int), st));
+            if (A > 1) CU(cudaMemsetAsync(c->d_partials.p, 0, slot_bytes_theta * nb, st)); /* unused slots */
+            mwsep_launch_shape ds = sh;
+            ds.n_theta = nb;
+            for (int a = 0; a < A; ++a)
+            {
+                mwsep_area_dev v = w.areas[a].view;
+                set_chunking(v, t.k_chunk, t.warp_items);
+                ds.area_index = a;
+                for (int form = 0; form < 4; ++form)
+                {
+                    bool present = false;
+                    for (int i = b0; i < b0 + nb; ++i) present |= mwsep_bg_form(&hth[i]) == form;
+                    if (!present) continue;
+                    ds.bg_form = form;
+                    CK(mwsep_launch_integral_f32_dyn(&v, c->d_theta.as<mwsep_theta_consts>() + b0, &ds, n_slots,
+                                                     c->d_partials.as<double2>(), c->d_tilectr.as<int>(), st));
+                    ++launches;
+                }
+            }
+            CK(mwsep_launch_reduce_slots(c->d_partials.as<double2>(), nb * A, n_slots, (int)ncomp, kSegLen,
+                                         c->d_segpart.as<double2>(), st));
+            mwsep_launch_shape rs = sh;
+            rs.n_theta = nb;
+            rs.grid = (int)n_seg;
+            CK(mwsep_launch_reduce_integrals(c->d_segpart.as<double2>(), &rs, d_areas + (size_t)b0 * A * ncomp,
+                                             d_ints + (size_t)b0 * ncomp, st));
+            launches += 2;
         }
     }
     /* a catalogue uploaded on the side stream: its table build released
@@ -1052,8 +1113,11 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         ++launches;
     }
     CU(cudaEventRecord(c->ev[2], st));
-    CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
-    ++launches;
+    if (!dyn)
+    {
+        CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
+        ++launches;
+    }
     CU(cudaEventRecord(c->ev[3], st));
     /* from here on the star tables are read */
     rc = wait_stars(c, st);
@@ -1211,7 +1275,7 @@ extern "C" int mwsep_ctx_destroy(mwsep_ctx* c)
     c->wedges.clear();
     size_t& t = c->dev_bytes;
     DevBuf* bufs[] = {&c->d_theta, &c->d_partials, &c->d_lkpartials, &c->d_out,
-                      &c->d_sprob, &c->d_assign, &c->d_xyz, &c->d_dens};
+                      &c->d_sprob, &c->d_assign, &c->d_xyz, &c->d_dens, &c->d_tilectr, &c->d_segpart};
     for (DevBuf* b : bufs) b->release(t);
     c->h_theta.release();
     c->h_out.release();

@@ -244,6 +244,19 @@ int mwsep_launch_likelihood_f64(const mwsep_stars_dev* st, const mwsep_theta_con
                                 double2* partials, void* stream);
 int mwsep_launch_integral_f32(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                               const mwsep_launch_shape* shape, double2* partials, void* stream);
+/* The warp-tile integral with tiles handed out by counters[theta * n_areas +
+ * area] (zeroed before the launch): per (theta, area) n_slots tile slots of
+ * 1 + S double2 (value, 0), tile-major, summed by mwsep_launch_reduce_integrals
+ * with grid = n_slots; slots past an area's tile count must be zero. */
+/* Sum per-tile slots (n_rows = theta * n_areas rows of n_slots x ncomp
+ * double2) in fixed segments of seg_len into seg (rows x n_seg x ncomp,
+ * n_seg = ceil(n_slots / seg_len)), for mwsep_launch_reduce_integrals with
+ * grid = n_seg. */
+int mwsep_launch_reduce_slots(const double2* slots, int n_rows, long long n_slots, int ncomp, int seg_len,
+                              double2* seg, void* stream);
+int mwsep_launch_integral_f32_dyn(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                  const mwsep_launch_shape* shape, long long n_slots, double2* slots,
+                                  int* counters, void* stream);
 int mwsep_launch_likelihood_f32(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,
                                 const mwsep_launch_shape* shape, const double* integrals,
                                 double2* partials, void* stream);

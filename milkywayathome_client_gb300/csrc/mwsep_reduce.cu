@@ -65,7 +65,42 @@ __global__ void __launch_bounds__(kReduceThreads)
     if (threadIdx.x == 0) out[(size_t)t * nslots + c] = acc[0].s + acc[0].c;
 }
 
+/* First level for per-tile slots: block (c + ncomp * g, row) sums component
+ * c of slots [g * seg_len, (g + 1) * seg_len) of row (theta * n_areas + area)
+ * into seg[(row * n_seg + g) * ncomp + c], a fixed segmentation. */
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_slots_kernel(const double2* __restrict__ slots, long long n_slots, int seg_len, int n_seg, int ncomp,
+                        double2* __restrict__ seg)
+{
+    __shared__ double red[2 * 32];
+    const int c = blockIdx.x % ncomp, g = blockIdx.x / ncomp;
+    const size_t row = blockIdx.y;
+    const double2* base = slots + row * (size_t)n_slots * ncomp;
+    const long long b0 = (long long)g * seg_len;
+    const long long b1 = b0 + seg_len < n_slots ? b0 + seg_len : n_slots;
+    comp_sum acc[1];
+    acc[0].zero();
+    for (long long b = b0 + threadIdx.x; b < b1; b += blockDim.x)
+    {
+        const double2 v = base[(size_t)b * ncomp + c];
+        acc[0].merge(v.x, v.y);
+    }
+    mwsep::block_reduce<1>(acc, red);
+    if (threadIdx.x == 0) seg[(row * n_seg + g) * ncomp + c] = make_double2(acc[0].s, acc[0].c);
+}
+
 } // namespace
+
+extern "C" int mwsep_launch_reduce_slots(const double2* slots, int n_rows, long long n_slots, int ncomp, int seg_len,
+                                         double2* seg, void* stream)
+{
+    const int n_seg = (int)((n_slots + seg_len - 1) / seg_len);
+    if (n_rows < 1 || n_rows > 65535 || n_seg < 1 || (long long)n_seg * ncomp > 2147483647LL)
+        return (int)cudaErrorInvalidValue;
+    reduce_slots_kernel<<<dim3(n_seg * ncomp, n_rows), kReduceThreads, 0, (cudaStream_t)stream>>>(
+        slots, n_slots, seg_len, n_seg, ncomp, seg);
+    return (int)cudaGetLastError();
+}
 
 extern "C" int mwsep_launch_reduce_integrals(const double2* partials, const mwsep_launch_shape* sh,
                                              double* out_areas, double* out_integrals, void* stream)
