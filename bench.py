@@ -360,7 +360,7 @@ def run_gb300_arm(args, ws, rank, local):
     achieved = cell_pts / integ_s / 1e9
     traffic = traffic_from_profiles("integral_f32w_config1")
     roofline = {"bound": "fma+sfu", "achieved": achieved, "peak": peak, "unit": "Gpoint/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "integral_f32w_kernel (packed warp tiles)",
+                "traffic": traffic, "kernel": "integral_f32w_dyn_kernel (packed warp tiles, tile counter)",
                 "peak_source": "measured (project pipe microbenchmark, mwsep_measure_pipe_peaks): FP32 FMA, "
                                "rsqrt, rcp and ex2 rates, at this kernel's per-point op mix",
                 "work_per_point": f"{fp32_ops} FP32 lane-ops + {1.25 + S} SFU ops",
