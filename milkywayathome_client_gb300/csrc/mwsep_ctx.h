@@ -134,6 +134,7 @@ struct Wedge
     bool has_stars = false;
     int n_stars = 0;
     DevBuf s_l, s_b, s_r, s_geom, s_r_point, s_qw, s_r_in_mag, s_r_in_mag2, s_reff, s_pts;
+    DevBuf s_head; /* per-star g' and distance factor, between the two star-table launches */
     /* double-float star table, built on the first double-float likelihood
      * of this catalogue */
     DevBuf s_ptsdf;

@@ -45,38 +45,49 @@ __global__ void geometry_kernel(double mu_min, double mu_step, int mu_steps, con
  * with nfac = {10^(dx_n/5)} then {gl_w_n coeff e^{-dx_n^2/2 sigma^2}} built
  * once per problem on the host: one multiply per point instead of a pow and
  * an exp, equal to the reference's values within a few ulp. */
-__global__ void star_tables_kernel(int n, const double* __restrict__ l, const double* __restrict__ b,
-                                   const double* __restrict__ r, int C, const double* __restrict__ dx,
-                                   const double* __restrict__ nfac, double* __restrict__ geom,
-                                   double* __restrict__ r_point, double* __restrict__ qw,
-                                   double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
-                                   double* __restrict__ reff, float4* __restrict__ pts)
+/* Per star: g', reff_xr_rp3, the distance factor 10^((g' - M)/5 + 1)/1000 and
+ * the star's sines/cosines; head[s] = g', head[n + s] = the factor. */
+__global__ void star_head_kernel(int n, const double* __restrict__ l, const double* __restrict__ b,
+                                 const double* __restrict__ r, double* __restrict__ geom, double* __restrict__ reff,
+                                 double* __restrict__ head)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
         double gPrime, rf;
         mwsep::prob_consts_head(r[s], gPrime, rf);
         reff[s] = rf;
-        const double base = pow(10.0, (gPrime - MW_ABSM) / 5.0 + 1.0) / 1000.0;
-        for (int i = 0; i < C; ++i)
-        {
-            const double g = gPrime + dx[i];
-            const double rp = base * nfac[i];
-            const double q = nfac[C + i] * (rp * rp * rp);
-            const size_t o = (size_t)i * n + s;
-            r_in_mag[o] = g;
-            r_in_mag2[o] = g * g;
-            r_point[o] = rp;
-            qw[o] = q;
-            const float hi = (float)rp;
-            pts[o] = make_float4(hi, (float)(rp - (double)hi), (float)(q * rf), (float)g);
-        }
+        head[s] = gPrime;
+        head[(size_t)n + s] = pow(10.0, (gPrime - MW_ABSM) / 5.0 + 1.0) / 1000.0;
         double* gg = geom + 4 * (size_t)s;
         gg[0] = sin(b[s] / MW_DEG);
         gg[1] = cos(b[s] / MW_DEG);
         gg[2] = sin(l[s] / MW_DEG);
         gg[3] = cos(l[s] / MW_DEG);
     }
+}
+
+/* Per (convolution point i = blockIdx.y, star): the tables at [i][s], one
+ * thread each, so the launch is as wide as the table (the per-star loop over
+ * the points left ~20 warps per SM on FP64 latency). */
+__global__ void star_points_kernel(int n, const double* __restrict__ dx, const double* __restrict__ nfac,
+                                   const double* __restrict__ head, const double* __restrict__ reff,
+                                   double* __restrict__ r_point, double* __restrict__ qw,
+                                   double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
+                                   float4* __restrict__ pts)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = blockIdx.y, C = gridDim.y;
+    const double g = head[s] + dx[i];
+    const double rp = head[(size_t)n + s] * nfac[i];
+    const double q = nfac[C + i] * (rp * rp * rp);
+    const size_t o = (size_t)i * n + s;
+    r_in_mag[o] = g;
+    r_in_mag2[o] = g * g;
+    r_point[o] = rp;
+    qw[o] = q;
+    const float hi = (float)rp;
+    pts[o] = make_float4(hi, (float)(rp - (double)hi), (float)(q * reff[s]), (float)g);
 }
 
 } // namespace
@@ -96,12 +107,15 @@ extern "C" int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps
 extern "C" int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
                                         const double* dx, const double* nfac, double* geom, double* r_point,
                                         double* qw, double* r_in_mag, double* r_in_mag2, double* reff, float4* pts,
-                                        void* stream)
+                                        double* head, void* stream)
 {
     if (n <= 0) return 0;
+    if (convolve < 1 || convolve > 65535) return (int)cudaErrorInvalidValue;
+    cudaStream_t st = (cudaStream_t)stream;
     int grid = (n + 127) / 128;
     if (grid > 152 * 32) grid = 152 * 32;
-    star_tables_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(n, l, b, r, convolve, dx, nfac, geom, r_point, qw,
-                                                               r_in_mag, r_in_mag2, reff, pts);
+    star_head_kernel<<<grid, 128, 0, st>>>(n, l, b, r, geom, reff, head);
+    star_points_kernel<<<dim3((n + 255) / 256, convolve), 256, 0, st>>>(n, dx, nfac, head, reff, r_point, qw,
+                                                                         r_in_mag, r_in_mag2, pts);
     return (int)cudaGetLastError();
 }

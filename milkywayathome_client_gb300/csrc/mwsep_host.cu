@@ -668,6 +668,7 @@ int prepare_stars(mwsep_ctx* c, Wedge& w, int n)
     rc |= w.s_r_in_mag2.ensure(NC * 8, tot);
     rc |= w.s_reff.ensure((size_t)n * 8, tot);
     rc |= w.s_pts.ensure(NC * sizeof(float4), tot);
+    rc |= w.s_head.ensure((size_t)n * 2 * sizeof(double), tot);
     w.bytes += tot - before;
     if (rc) return mwsep_fail(MWSEP_ERR_NOMEM);
     mwsep_stars_dev& v = w.stars_view;
@@ -704,7 +705,8 @@ int upload_stars(mwsep_ctx* c, Wedge& w, const double* l, const double* b, const
     CK(mwsep_launch_star_tables(w.n_stars, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(),
                                 w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
                                 w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
-                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(), st));
+                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(),
+                                w.s_head.as<double>(), st));
     return MWSEP_OK;
 }
 
@@ -896,7 +898,7 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
         for (DevBuf* b : bufs) b->release(t);
     }
     DevBuf* bufs[] = {&w.d_dx, &w.d_glw, &w.d_nfac, &w.s_l, &w.s_b, &w.s_r, &w.s_geom, &w.s_r_point, &w.s_qw,
-                      &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts, &w.s_ptsdf};
+                      &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts, &w.s_ptsdf, &w.s_head};
     for (DevBuf* b : bufs) b->release(t);
     w.has_star_df = false;
     w.h_stars.release();
