@@ -963,9 +963,10 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     const size_t slot_bytes_theta = sizeof(double2) * (size_t)A * n_slots * ncomp;
     constexpr int kSegLen = 1024; /* slots per first-level reduction block */
     const long long n_seg = (n_slots + kSegLen - 1) / kSegLen;
+    const long chunk_cap = env_long("MWSEP_F32_DYN_CHUNK", 65535); /* at most this many theta per chunk */
     const int dyn_chunk =
         dyn ? (int)std::max<size_t>(1, std::min<size_t>({(size_t)B, kDynSlotBytes / slot_bytes_theta,
-                                                         (size_t)(65535 / A)}))
+                                                         (size_t)(65535 / A), (size_t)std::max(1L, chunk_cap)}))
             : B;
     const size_t part_bytes =
         dyn ? slot_bytes_theta * dyn_chunk : sizeof(double2) * (size_t)B * A * t.grid * ncomp;

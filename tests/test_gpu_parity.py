@@ -154,6 +154,30 @@ def test_split_likelihood_equals_fused(gpu_ctx, name, monkeypatch):
         assert a.num_zero == c.num_zero
 
 
+@pytest.mark.parametrize("name", ["three_streams", "cut_area", "aux_profile", "general_alpha_delta", "six_streams"])
+def test_tile_counter_integral(gpu_ctx, name, monkeypatch):
+    """The compensated integral with tiles handed out by a counter against the
+    static schedule (sums in another order: within 1e-12), and a batch cut
+    into theta chunks equal to the single evaluations bit for bit (cut_area
+    has two areas of different tile counts)."""
+    import milkywayathome_client_gb300 as mw
+    _, _, g = _setup(gpu_ctx, name)
+    base = np.asarray(g["theta"])
+    thetas = [base * (1 + 1e-3 * k) for k in range(5)]
+    single = [gpu_ctx.evaluate(t, mw.MWSEP_MIXED_F32) for t in thetas]
+    monkeypatch.setenv("MWSEP_F32_DYN_CHUNK", "2")
+    chunked = gpu_ctx.evaluate_batch(thetas, mw.MWSEP_MIXED_F32)
+    monkeypatch.delenv("MWSEP_F32_DYN_CHUNK")
+    monkeypatch.setenv("MWSEP_F32_DYNAMIC", "0")
+    static = [gpu_ctx.evaluate(t, mw.MWSEP_MIXED_F32) for t in thetas]
+    for a, b, c in zip(single, chunked, static):
+        assert a.integrals == b.integrals and a.area_integrals == b.area_integrals
+        assert a.likelihood == b.likelihood or (math.isnan(a.likelihood) and math.isnan(b.likelihood))
+        for x, y in zip(a.integrals, c.integrals):
+            assert _close_rel(x, y, 1e-12), (x, y)
+        assert _close_abs(a.likelihood, c.likelihood, 1e-12)
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_equals_single_bitwise(gpu_ctx, precision):
     """Each result of a batch is bit-identical to the same theta alone."""
