@@ -266,10 +266,16 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     __syncwarp();
 }
 
-template <int S, int FORM>
+/* DYN: tiles handed out by counters[theta * counter_stride] instead of a
+ * fixed share per warp (the warp scheduler favours an SM's older block), each
+ * tile's sums added across the warp in a fixed order into the tile's own
+ * slot of `partials` (tile-major, 1 + S components) for the fixed-order slot
+ * reduction. */
+template <int S, int FORM, bool DYN>
 __global__ void __launch_bounds__(DfShape<S>::block, DfShape<S>::min_blocks) integral_df_kernel(const mwsep_area_dev A,
                                                                 const mwsep_theta_consts* __restrict__ thetas,
-                                                                double2* __restrict__ partials, long long theta_stride)
+                                                                double2* __restrict__ partials, long long theta_stride,
+                                                                int* __restrict__ counters, int counter_stride)
 {
     __shared__ mwsep_theta_consts th;
     constexpr int kBlock = DfShape<S>::block;
@@ -288,10 +294,39 @@ __global__ void __launch_bounds__(DfShape<S>::block, DfShape<S>::min_blocks) int
         for (int j = threadIdx.x; j < D::kLog2Table; j += kBlock) ltab[j] = c_log2_tab[j];
     __syncthreads();
     if (!df_form_is(th, FORM)) return; /* the other form's launch covers this theta (whole block) */
+    const int warp = threadIdx.x >> 5;
+    if constexpr (DYN)
+    {
+        const int lane = threadIdx.x & 31;
+        const int NC = 1 + th.n_streams;
+        int* ctr = counters + (size_t)blockIdx.y * counter_stride;
+        double2* out = partials + (size_t)blockIdx.y * theta_stride;
+        for (;;)
+        {
+            int wt = 0;
+            if (lane == 0) wt = atomicAdd(ctr, 1);
+            wt = __shfl_sync(0xffffffffu, wt, 0);
+            if ((long long)wt >= A.n_items) break;
+            double acc[1 + S];
+#pragma unroll
+            for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
+            warp_tile_df<S, FORM>(A, th, wt, cs[warp], kf[warp], thi, tlo, ltab, acc);
+#pragma unroll
+            for (int k = 0; k < 1 + S; ++k)
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int k = 0; k < 1 + S; ++k)
+                    if (k < NC) out[(size_t)wt * NC + k] = make_double2(acc[k], 0.0);
+            }
+        }
+        return;
+    }
     double acc[1 + S];
 #pragma unroll
     for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
-    const int warp = threadIdx.x >> 5;
     const long long warps = (long long)gridDim.x * (kBlock / 32);
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
         warp_tile_df<S, FORM>(A, th, wt, cs[warp], kf[warp], thi, tlo, ltab, acc);
@@ -325,11 +360,33 @@ int launch(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_la
     double2* base = partials + (size_t)sh->area_index * sh->grid * ncomp;
     dim3 g(sh->grid, sh->n_theta);
     if (sh->bg_form == kFormGeneral)
-        integral_df_kernel<S, kFormGeneral><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+        integral_df_kernel<S, kFormGeneral, false>
+            <<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, nullptr, 0);
     else if (sh->bg_form == kFormNone)
-        integral_df_kernel<S, kFormNone><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+        integral_df_kernel<S, kFormNone, false><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, nullptr, 0);
     else
-        integral_df_kernel<S, kFormHern><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride);
+        integral_df_kernel<S, kFormHern, false><<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, nullptr, 0);
+    return (int)cudaGetLastError();
+}
+
+template <int S>
+int launch_dyn(const mwsep_area_dev* A, const mwsep_theta_consts* th, const mwsep_launch_shape* sh,
+               long long n_slots, double2* slots, int* counters, cudaStream_t st)
+{
+    const long long ncomp = 1 + sh->n_streams;
+    const long long theta_stride = (long long)sh->n_areas * n_slots * ncomp;
+    double2* base = slots + (size_t)sh->area_index * n_slots * ncomp;
+    int* ctr = counters + sh->area_index;
+    dim3 g(sh->grid, sh->n_theta);
+    if (sh->bg_form == kFormGeneral)
+        integral_df_kernel<S, kFormGeneral, true>
+            <<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+    else if (sh->bg_form == kFormNone)
+        integral_df_kernel<S, kFormNone, true>
+            <<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
+    else
+        integral_df_kernel<S, kFormHern, true>
+            <<<g, DfShape<S>::block, 0, st>>>(*A, th, base, theta_stride, ctr, sh->n_areas);
     return (int)cudaGetLastError();
 }
 
@@ -338,12 +395,12 @@ template <int S>
 cudaError_t occupancy(int* b)
 {
     int b0 = 0, b2 = 0, b3 = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, integral_df_kernel<S, kFormHern>,
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, integral_df_kernel<S, kFormHern, false>,
                                                                   DfShape<S>::block, 0);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, integral_df_kernel<S, kFormGeneral>, DfShape<S>::block, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, integral_df_kernel<S, kFormGeneral, false>, DfShape<S>::block, 0);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, integral_df_kernel<S, kFormNone>, DfShape<S>::block, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, integral_df_kernel<S, kFormNone, false>, DfShape<S>::block, 0);
     *b = b0 < b2 ? b0 : b2;
     *b = *b < b3 ? *b : b3;
     return e;
@@ -707,6 +764,26 @@ extern "C" int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_
     case 6: return launch<6>(area, th_dev, sh, partials, st);
     case 7: return launch<7>(area, th_dev, sh, partials, st);
     case 8: return launch<8>(area, th_dev, sh, partials, st);
+    default: return (int)cudaErrorInvalidValue;
+    }
+}
+
+extern "C" int mwsep_launch_integral_df_dyn(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                            const mwsep_launch_shape* sh, long long n_slots, double2* slots,
+                                            int* counters, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (sh->n_streams)
+    {
+    case 0: return launch_dyn<0>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 1: return launch_dyn<1>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 2: return launch_dyn<2>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 3: return launch_dyn<3>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 4: return launch_dyn<4>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 5: return launch_dyn<5>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 6: return launch_dyn<6>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 7: return launch_dyn<7>(area, th_dev, sh, n_slots, slots, counters, st);
+    case 8: return launch_dyn<8>(area, th_dev, sh, n_slots, slots, counters, st);
     default: return (int)cudaErrorInvalidValue;
     }
 }

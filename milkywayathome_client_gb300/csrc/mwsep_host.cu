@@ -951,14 +951,15 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
      * (per theta and area); batches go through in theta chunks whose slots
      * fit kDynSlotBytes (each theta's sum is its own, whatever the chunk) */
     long long n_slots = 0;
-    if (precision == MWSEP_MIXED_F32 && t.warp_items)
+    if ((precision == MWSEP_MIXED_F32 || precision == MWSEP_PLAIN_DF) && t.warp_items)
         for (int a = 0; a < A; ++a)
         {
             mwsep_area_dev v = w.areas[a].view;
             set_chunking(v, t.k_chunk, t.warp_items);
             n_slots = std::max(n_slots, v.n_items);
         }
-    const bool dyn = n_slots > 0 && n_slots < (1LL << 30) && env_long("MWSEP_F32_DYNAMIC", 1) != 0;
+    const bool dyn = n_slots > 0 && n_slots < (1LL << 30) &&
+                     env_long(precision == MWSEP_PLAIN_DF ? "MWSEP_DF_DYNAMIC" : "MWSEP_F32_DYNAMIC", 1) != 0;
     constexpr size_t kDynSlotBytes = (size_t)512 << 20;
     const size_t slot_bytes_theta = sizeof(double2) * (size_t)A * n_slots * ncomp;
     constexpr int kSegLen = 1024; /* slots per first-level reduction block */
@@ -1032,7 +1033,7 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
                                          c->d_partials.as<double2>(), st));
             ++launches;
         }
-        else if (precision == MWSEP_PLAIN_DF)
+        else if (precision == MWSEP_PLAIN_DF && !dyn)
         {
             for (int form : {0, 2, 3})
             {
@@ -1075,14 +1076,35 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
                 mwsep_area_dev v = w.areas[a].view;
                 set_chunking(v, t.k_chunk, t.warp_items);
                 ds.area_index = a;
+                const mwsep_theta_consts* thb = c->d_theta.as<mwsep_theta_consts>() + b0;
+                if (precision == MWSEP_PLAIN_DF)
+                {
+                    for (int form : {0, 2, 3})
+                    {
+                        if (!(form == 0 ? df_hern : form == 2 ? df_general : df_none)) continue;
+                        ds.bg_form = form;
+                        CK(mwsep_launch_integral_df_dyn(&v, thb, &ds, n_slots, c->d_partials.as<double2>(),
+                                                        c->d_tilectr.as<int>(), st));
+                        ++launches;
+                    }
+                    if (df_aux || df_none)
+                    {
+                        /* into each (theta, area)'s slot 0, after the tiles wrote it */
+                        mwsep_launch_shape as = ds;
+                        as.grid = (int)n_slots;
+                        CK(mwsep_launch_aux_area_df(&v, thb, &as, c->d_partials.as<double2>(), st));
+                        ++launches;
+                    }
+                    continue;
+                }
                 for (int form = 0; form < 4; ++form)
                 {
                     bool present = false;
                     for (int i = b0; i < b0 + nb; ++i) present |= mwsep_bg_form(&hth[i]) == form;
                     if (!present) continue;
                     ds.bg_form = form;
-                    CK(mwsep_launch_integral_f32_dyn(&v, c->d_theta.as<mwsep_theta_consts>() + b0, &ds, n_slots,
-                                                     c->d_partials.as<double2>(), c->d_tilectr.as<int>(), st));
+                    CK(mwsep_launch_integral_f32_dyn(&v, thb, &ds, n_slots, c->d_partials.as<double2>(),
+                                                     c->d_tilectr.as<int>(), st));
                     ++launches;
                 }
             }

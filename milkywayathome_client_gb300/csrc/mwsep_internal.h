@@ -286,6 +286,11 @@ int mwsep_df_prepare(int device);
 int mwsep_integral_df_blocks_per_sm(int n_streams);
 int mwsep_launch_integral_df(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                              const mwsep_launch_shape* sh, double2* partials, void* stream);
+/* The double-float integral with a tile counter and per-tile slots, as
+ * mwsep_launch_integral_f32_dyn. */
+int mwsep_launch_integral_df_dyn(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
+                                 const mwsep_launch_shape* shape, long long n_slots, double2* slots,
+                                 int* counters, void* stream);
 /* Adds the aux profile's column-independent share of an area integral to
  * the double-float partials of the thetas that have it (after
  * mwsep_launch_integral_df for that area, same shape). */
