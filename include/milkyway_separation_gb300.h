@@ -412,6 +412,19 @@ int mwsep_ctx_evaluate_requests(mwsep_ctx* ctx, int n, const mwsep_request* reqs
 int mwsep_ctx_autotune(mwsep_ctx* ctx, int wedge_id, int precision, double* predicted_ms);
 /* The tile shape a wedge uses for one precision. */
 int mwsep_ctx_wedge_tile_shape(const mwsep_ctx* ctx, int wedge_id, int precision, int* k_chunk, int* tile_items);
+/* The launch model behind the compensated form's default r-chunk (host only,
+ * no device needed; no reference counterpart).  mwsep_model_tile_cost: the
+ * modelled time, in lane groups of points, of one warp-tile launch with a
+ * fixed share of tiles per warp (warp w of W takes tiles w, w + W, ... in
+ * r-chunk-major order, block b on SM b % sms): the largest per-SM sum of tile
+ * costs, a tile costing ceil(k_chunk' * convolve / group) + prologue for its
+ * chunk's k_chunk' bins; -1 on invalid input.  mwsep_model_kchunk: the chunk
+ * of least modelled time for a wedge of mu_steps x nu_steps x r_steps cells
+ * (the choice the library makes for MWSEP_MIXED_F32), and its cost. */
+double mwsep_model_tile_cost(int r_steps, int convolve, int group, long long tiles_per_chunk, int k_chunk, int sms,
+                             int blocks_per_sm, int warps_per_block, double prologue);
+int mwsep_model_kchunk(int r_steps, int convolve, int n_streams, long long mu_steps, long long nu_steps, int sms,
+                       int blocks_per_sm, int* k_chunk, double* cost);
 
 /* ---- Serving: continuous batching over the resident wedges ---- */
 

@@ -430,6 +430,45 @@ double static_tile_cost(int max_r, int convolve, int group, long long tiles_per_
     return all + *std::max_element(sm.begin(), sm.end());
 }
 
+/* The compensated form's r-chunk: the least modelled time (static_tile_cost,
+ * a 0.5-group column prologue) for chunks from kmin up to max_r bins. */
+int model_kchunk(int max_r, int convolve, int group, long long tiles_per_chunk, int kmin, int sms,
+                 int blocks_per_sm, int warps_per_block, double* cost_out)
+{
+    double best = 1e300;
+    int kc = max_r;
+    for (int k = std::max(1, std::min(max_r, kmin)); k <= max_r; ++k)
+    {
+        const double cost =
+            static_tile_cost(max_r, convolve, group, tiles_per_chunk, k, sms, blocks_per_sm, warps_per_block, 0.5);
+        if (cost < best * (1.0 - 1e-12))
+        {
+            best = cost;
+            kc = k;
+        }
+    }
+    if (cost_out) *cost_out = best;
+    return kc;
+}
+
+/* Warp-tile chunking inputs: points per lane group and the least chunk. */
+void warp_tile_groups(int prec, int n_streams, int convolve, int max_r, int& group, int& ks, int& kmin)
+{
+    group = prec == MWSEP_PLAIN_DF ? 32 * mwsep_df_tile_p(n_streams)
+                                   : 32 * (n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
+    ks = group;
+    for (int a = group, b = std::max(convolve, 1); b;)
+    {
+        const int t2 = a % b;
+        a = b;
+        b = t2;
+        ks = group / a;
+    }
+    /* at least four lane groups of points per column of a tile, so the
+     * column prologue and the last group's padding stay small */
+    kmin = std::min(max_r, ((4 * group + convolve - 1) / std::max(convolve, 1) + ks - 1) / ks * ks);
+}
+
 void default_tune(mwsep_ctx* c, Wedge& w)
 {
     const ProblemHost& p = w.prob;
@@ -461,20 +500,8 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             long long nk = (want + tiles_per_chunk - 1) / std::max<long long>(tiles_per_chunk, 1);
             nk = std::max<long long>(1, std::min<long long>(nk, max_r));
             int kc = (int)((max_r + nk - 1) / nk);
-            const int group = prec == MWSEP_PLAIN_DF
-                                  ? 32 * mwsep_df_tile_p(p.n_streams)
-                                  : 32 * (p.n_streams <= 4 ? mwsep::TileP<4>::P : mwsep::TileP<8>::P);
-            int ks = group;
-            for (int a = group, b = std::max(p.convolve, 1); b;)
-            {
-                const int t2 = a % b;
-                a = b;
-                b = t2;
-                ks = group / a;
-            }
-            /* at least four lane groups of points per column of a tile, so
-             * the column prologue and the last group's padding stay small */
-            const int kmin = std::min(max_r, ((4 * group + p.convolve - 1) / p.convolve + ks - 1) / ks * ks);
+            int group, ks, kmin;
+            warp_tile_groups(prec, p.n_streams, p.convolve, max_r, group, ks, kmin);
             kc = std::max(kc, kmin);
             if (kc >= ks) kc = kc / ks * ks;
             /* a small wedge whose tiles would leave warps idle: the chunk that
@@ -482,20 +509,8 @@ void default_tune(mwsep_ctx* c, Wedge& w)
              * per-tile prologue, and one warp's sequential chain) */
             const long long slots = threads / 32;
             if (prec == MWSEP_MIXED_F32)
-            {
-                /* the r-chunk of least modelled time, from the four-group floor up */
-                double best = 1e300;
-                for (int k = std::max(1, std::min(max_r, kmin)); k <= max_r; ++k)
-                {
-                    const double cost = static_tile_cost(max_r, p.convolve, group, tiles_per_chunk, k, c->sm_count,
-                                                         per_sm, t.block / 32, 0.5);
-                    if (cost < best * (1.0 - 1e-12))
-                    {
-                        best = cost;
-                        kc = k;
-                    }
-                }
-            }
+                kc = model_kchunk(max_r, p.convolve, group, tiles_per_chunk, kmin, c->sm_count, per_sm, t.block / 32,
+                                  nullptr);
             else if (tiles_per_chunk * ((max_r + kc - 1) / kc) < slots)
                 kc = fill_kchunk(max_r, p.convolve, group, tiles_per_chunk, c->sm_count, slots, 0.1, kc);
             t.k_chunk = (int)env_long("MWSEP_TUNE_KCHUNK", kc);
@@ -1401,6 +1416,29 @@ extern "C" int mwsep_ctx_last_launches(const mwsep_ctx* c, int* out)
 {
     if (!c || !out) return mwsep_fail(MWSEP_ERR_ARG);
     *out = c->last_launches;
+    return MWSEP_OK;
+}
+
+extern "C" double mwsep_model_tile_cost(int r_steps, int convolve, int group, long long tiles_per_chunk, int k_chunk,
+                                        int sms, int blocks_per_sm, int warps_per_block, double prologue)
+{
+    if (r_steps < 1 || convolve < 1 || group < 1 || tiles_per_chunk < 1 || k_chunk < 1 || sms < 1 ||
+        blocks_per_sm < 1 || warps_per_block < 1)
+        return -1.0;
+    return static_tile_cost(r_steps, convolve, group, tiles_per_chunk, k_chunk, sms, blocks_per_sm, warps_per_block,
+                            prologue);
+}
+
+extern "C" int mwsep_model_kchunk(int r_steps, int convolve, int n_streams, long long mu_steps, long long nu_steps,
+                                  int sms, int blocks_per_sm, int* k_chunk, double* cost)
+{
+    if (r_steps < 1 || convolve < 1 || n_streams < 0 || n_streams > 8 || mu_steps < 1 || nu_steps < 1 || sms < 1 ||
+        blocks_per_sm < 1 || !k_chunk)
+        return mwsep_fail(MWSEP_ERR_ARG);
+    int group, ks, kmin;
+    warp_tile_groups(MWSEP_MIXED_F32, n_streams, convolve, r_steps, group, ks, kmin);
+    const long long tiles_per_chunk = mwsep::warp_tile_count((int)mu_steps, (int)nu_steps, 1);
+    *k_chunk = model_kchunk(r_steps, convolve, group, tiles_per_chunk, kmin, sms, blocks_per_sm, 256 / 32, cost);
     return MWSEP_OK;
 }
 

@@ -246,6 +246,10 @@ _SIGS = {
                                               _P(mwsep_result)]),
     "mwsep_ctx_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_double)]),
     "mwsep_ctx_wedge_tile_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int)]),
+    "mwsep_model_tile_cost": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, C.c_double]),
+    "mwsep_model_kchunk": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int, C.c_int,
+                                     _P(C.c_int), _P(C.c_double)]),
     "mwsep_server_create": (C.c_int, [C.c_void_p, _P(mwsep_server_config), _P(C.c_void_p)]),
     "mwsep_server_submit": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double), C.c_int, _P(C.c_ulonglong)]),
     "mwsep_server_wait": (C.c_int, [C.c_void_p, C.c_ulonglong, C.c_double, _P(mwsep_result)]),
