@@ -32,6 +32,31 @@ def test_python_binding_covers_header(built_library):
     assert set(_declared_functions()) <= set(native.exported_symbols())
 
 
+def _prototype_arg_counts():
+    """name -> number of parameters, from the header's prototypes."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(mwsep_\w+)\s*\(([^;{]*?)\)\s*;", text):
+        args = m.group(2).strip()
+        depth, n = 0, (0 if args in ("", "void") else 1)
+        for ch in args:
+            depth += ch == "("
+            depth -= ch == ")"
+            n += ch == "," and depth == 0
+        out[m.group(1)] = n
+    return out
+
+
+def test_python_binding_argument_counts(built_library):
+    """Each ctypes signature has as many arguments as the header's prototype."""
+    from milkywayathome_client_gb300 import native
+    protos = _prototype_arg_counts()
+    assert set(protos) == set(_declared_functions())  # every declared function parsed
+    wrong = {n: (protos[n], len(native._SIGS[n][1])) for n in protos
+             if n in native._SIGS and protos[n] != len(native._SIGS[n][1])}
+    assert not wrong, wrong
+
+
 def test_struct_layouts_match_c(tmp_path, built_library):
     """sizeof/offsetof from a C compiler vs the ctypes mirror."""
     from milkywayathome_client_gb300 import native as N
