@@ -29,6 +29,52 @@ def load_case(name):
     return os.path.join(d, "params.txt"), os.path.join(d, "stars.txt"), g
 
 
+REF_FIXTURES = os.path.join(GOLDEN, "reference")
+SCALE = os.path.join(GOLDEN, "scale")
+
+
+def reference_fixture_ids():
+    """The reference's own test fixtures that have goldens (79, 86, 11, 12,
+    20, 21 and the -aux variants)."""
+    with open(os.path.join(REF_FIXTURES, "index.json")) as f:
+        return list(json.load(f))
+
+
+def _unpacked(xz_path, tmp_root):
+    """The decompressed star file of a committed .xz fixture (once per session)."""
+    import lzma
+    import shutil
+    out = os.path.join(tmp_root, os.path.relpath(xz_path, GOLDEN).replace(os.sep, "_")[: -len(".xz")])
+    if not os.path.exists(out):
+        with lzma.open(xz_path, "rb") as f, open(out + ".part", "wb") as g:
+            shutil.copyfileobj(f, g)
+        os.replace(out + ".part", out)
+    return out
+
+
+@pytest.fixture(scope="session")
+def golden_inputs(tmp_path_factory):
+    """Paths of the committed large fixtures: fn(kind, name) -> (params,
+    stars, golden) with kind "reference" (a reference test fixture) or
+    "scale" (a benchmark config, name "config1" / "config2")."""
+    root = str(tmp_path_factory.mktemp("golden_stars"))
+
+    def get(kind, name):
+        if kind == "reference":
+            d = os.path.join(REF_FIXTURES, name)
+            with open(os.path.join(d, "golden.json")) as f:
+                g = json.load(f)
+            xz = os.path.join(GOLDEN, g["stars_xz"])
+        else:
+            d = os.path.join(SCALE, name)
+            with open(os.path.join(d, "golden.json")) as f:
+                g = json.load(f)
+            xz = os.path.join(d, "stars.txt.xz")
+        return os.path.join(d, "params.txt"), _unpacked(xz, root), g
+
+    return get
+
+
 @pytest.fixture(scope="session")
 def built_library():
     from milkywayathome_client_gb300 import build

@@ -1,0 +1,114 @@
+"""GPU parity on the reference's own test fixtures and at the benchmark sizes.
+
+Goldens are the reference CPU evaluator's own outputs (compiled from its
+sources; tests/golden/make_scale_golden.py):
+  * its test fixtures tests/astronomy_parameters-{79,86,11,12,20,21}-small
+    and the -aux variants of 79, 86, 11, 12 (160 x 16..64 x 70..140 cells,
+    convolve 120, 1-3 streams, one cut, 59k-121k stars), the committed star
+    files being byte for byte the reference's;
+  * benchmark config 2 (400 x 160 x 140 cells, convolve 60, 3 streams, 50k
+    stars) at its base theta and four population members;
+  * benchmark config 1 (1600 x 640 x 140 cells, convolve 120, 3 streams, 100k
+    stars: 1.72e10 density points) at its base theta.
+
+Bounds, per form:
+  MWSEP_PLAIN_F64, MWSEP_PLAIN_DF  1e-12 relative on every area integral,
+                                   1e-12 absolute on the log-likelihood;
+  MWSEP_MIXED_F32                  1e-7 absolute on the log-likelihood and
+                                   MIXED_REL_INT relative on every integral.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import reference_fixture_ids
+
+pytestmark = pytest.mark.gpu
+
+REL_INT = 1e-12
+ABS_LOGL = 1e-12
+ABS_LOGL_MIXED = 1e-7
+# The compensated form sums FP32 densities (SFU exp2 / rsqrt / rcp, ~2^-22
+# relative each) in FP32 groups of 256 points before FP64; the error of an
+# integral is dominated by the group sums.  Measured on GB300 against these
+# goldens: 1.7e-8 (config 1) to 7.2e-8 (a config-2 population member).
+MIXED_REL_INT = 2e-7
+
+
+def _rel(a, b):
+    if b == 0.0:
+        return 0.0 if a == 0.0 else math.inf
+    return abs(a - b) / abs(b)
+
+
+def _check(r, g, rel_int, abs_logl, label):
+    worst = 0.0
+    for a, (got, want) in enumerate(zip(r.area_integrals, g["area_integrals"])):
+        for k, (x, y) in enumerate(zip(got, want)):
+            e = _rel(x, y)
+            worst = max(worst, e)
+            assert e <= rel_int, f"{label}: area {a} component {k}: {x!r} vs {y!r} ({e:.2e})"
+    dl = abs(r.likelihood - g["likelihood"])
+    assert dl <= abs_logl, f"{label}: logL {r.likelihood!r} vs {g['likelihood']!r} ({dl:.2e})"
+    assert r.num_zero == g["num_zero"], label
+    print(f"{label}: max integral rel err {worst:.3e}, |dlogL| {dl:.3e}")
+    return worst, dl
+
+
+def _ctx_for(gpu_ctx, pf, sf):
+    import milkywayathome_client_gb300 as mw
+    gpu_ctx.set_problem(mw.AstronomyParameters.read(pf))
+    gpu_ctx.set_stars(mw.StarPoints.read(sf))
+
+
+@pytest.mark.parametrize("fid", reference_fixture_ids())
+def test_reference_fixture_all_forms(gpu_ctx, golden_inputs, fid):
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = golden_inputs("reference", fid)
+    _ctx_for(gpu_ctx, pf, sf)
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64), g, REL_INT, ABS_LOGL, f"{fid} plain")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF), g, REL_INT, ABS_LOGL, f"{fid} double-float")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32), g, MIXED_REL_INT, ABS_LOGL_MIXED, f"{fid} mixed")
+
+
+@pytest.mark.parametrize("fid", ["86", "11-aux"])
+def test_reference_fixture_evalfunc(built_library, golden_inputs, fid):
+    """The EvalFunc entry on the reference's own files (86 has a cut)."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = golden_inputs("reference", fid)
+    ap = mw.AstronomyParameters.read(pf)
+    sp = mw.StarPoints.read(sf)
+    es = mw.EvaluationState(ap, sp)
+    v = mw.evaluate(g["theta"], ap, es, sp)
+    assert abs((v - 3.0) - g["likelihood"]) <= ABS_LOGL
+    for got, want in zip(es.area_integrals, g["area_integrals"]):
+        for x, y in zip(got, want):
+            assert _rel(x, y) <= REL_INT, (x, y)
+    assert _rel(es.prob_sum, g["prob_sum"]) <= 1e-12
+
+
+def test_config2_population_all_forms(gpu_ctx, golden_inputs):
+    """Config 2's base theta and four population members, as one batch per
+    form (each batch member is the same as that theta alone)."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, G = golden_inputs("scale", "config2")
+    _ctx_for(gpu_ctx, pf, sf)
+    evs = G["evaluations"]
+    thetas = np.array([e["theta"] for e in evs])
+    for prec, rel, dl, name in ((mw.MWSEP_PLAIN_F64, REL_INT, ABS_LOGL, "plain"),
+                                (mw.MWSEP_PLAIN_DF, REL_INT, ABS_LOGL, "double-float"),
+                                (mw.MWSEP_MIXED_F32, MIXED_REL_INT, ABS_LOGL_MIXED, "mixed")):
+        for i, (r, g) in enumerate(zip(gpu_ctx.evaluate_batch(thetas, prec), evs)):
+            _check(r, g, rel, dl, f"config2[{i}] {name}")
+
+
+def test_config1_all_forms(gpu_ctx, golden_inputs):
+    """The full-size wedge: 1.72e10 density points per evaluation."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, G = golden_inputs("scale", "config1")
+    _ctx_for(gpu_ctx, pf, sf)
+    g = G["evaluations"][0]
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64), g, REL_INT, ABS_LOGL, "config1 plain")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF), g, REL_INT, ABS_LOGL, "config1 double-float")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32), g, MIXED_REL_INT, ABS_LOGL_MIXED, "config1 mixed")
