@@ -546,7 +546,8 @@ int mwsep_write_errors(const char* path, int n, const double* hessian, const dou
 
 /* Device tables of one integral area, in the quantities the reference's
  * cpu__r_constants and calculate_probabilities use.  All pointers are device
- * memory owned by the caller; tables are row-major. */
+ * memory on the calling thread's current device, owned by the caller,
+ * 8-byte aligned; tables are row-major. */
 typedef struct
 {
     int mu_steps, nu_steps, r_steps, convolve;
@@ -559,6 +560,14 @@ typedef struct
     const double* reff_xr_rp3; /* [r_steps] */
     const double* irv;         /* [r_steps] */
     const double* ids;         /* [nu_steps] */
+    /* The cells integrated, as INTEGRAL_AREA's (cpu/evaluation_state.h:30-41):
+     * [min_calculation, max_calculation) of the linearised index
+     * (mu * nu_steps + nu) * r_steps + r -- 0 and mu_steps * nu_steps * r_steps
+     * for the whole area, a rank's share after split_astronomy_parameters.
+     * As calculate_integral does (cpu/evaluation_optimized.c:521-527), a
+     * range with max_calculation <= min_calculation still integrates the cell
+     * min_calculation; a negative min_calculation is MWSEP_ERR_ARG. */
+    long min_calculation, max_calculation;
 } mwsep_area_tables;
 
 /* The density constants of one evaluation (init_constants' results). */
@@ -576,8 +585,10 @@ typedef struct
 /* Size of the fixed device array the allocation-free entry point works in. */
 #define MWSEP_NOALLOC_SCRATCH_BYTES (256 * 1024)
 
-/* Plain-FP64 background and stream integrals of one area, written to
- * d_integrals (device, 1 + number_streams doubles), for callers that cannot
+/* Plain-FP64 background and stream integrals of one area (of its cells
+ * [min_calculation, max_calculation)), written to d_integrals (device memory
+ * on the current device, 8-byte aligned, 1 + number_streams doubles), for
+ * callers that cannot
  * let a library allocate device memory: programs that give all device
  * memory to their own pool, hot paths where a cudaMalloc would synchronise
  * the device, loops that must not fail on allocation once running.  No

@@ -82,6 +82,9 @@ struct AreaHost
     int mu_steps, nu_steps, r_steps;
     double mu_min, mu_max, nu_min, nu_max, r_min, r_max;
     double mu_step, nu_step, r_step;
+    /* the cells integrated: [cell_begin, cell_end) of the linearised index,
+     * from INTEGRAL's [min_calculation, max_calculation) (mwsep::effective_slice) */
+    long long cell_begin, cell_end;
 };
 
 struct AreaDev
@@ -226,7 +229,10 @@ int wait_stars(mwsep_ctx* c, cudaStream_t st);
  * (the build after event `after`, if given) and record ev_stars. */
 int launch_star_build(mwsep_ctx* c, cudaEvent_t after);
 void wedge_release(mwsep_ctx* c, Wedge& w);
-void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items);
+/* Integrate the cells [min_calculation, max_calculation) of each area of a
+ * resident wedge (per area; the EvalFunc entries take them from
+ * EVALUATION_STATE as calculate_integral does). */
+int wedge_set_slices(mwsep_ctx* c, Wedge& w, const long* min_calc, const long* max_calc);
 /* r-bins per warp tile that make a tile's points whole lane groups. */
 int warp_tile_kstep(int convolve, int n_streams);
 void default_tune(mwsep_ctx* c, Wedge& w);

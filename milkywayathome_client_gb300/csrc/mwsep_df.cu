@@ -108,13 +108,10 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     constexpr int DFP = mwsep_df_tile_p(S); /* points per lane per group */
     constexpr int NPR = DFP / 2;            /* ... as pairs of points */
     const int lane = threadIdx.x & 31;
-    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
-    const long long rest = wt / nmb;
-    const int mb = (int)(wt - rest * nmb);
-    const int kc = (int)(rest / A.nu_steps);
-    const int nu = (int)(rest - (long long)kc * A.nu_steps);
-    const int mu0 = mb * mwsep::kTileCols;
-    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+    const mwsep::TilePos tp = mwsep::tile_pos(A, wt);
+    const int nu = tp.nu;
+    const int mu0 = tp.mu0;
+    const int ncols = tp.ncols;
 
     /* column constants (FP64); the stream exponents in base 2 */
     mwsep::f64::ColF64<kSP(S)> cc;
@@ -145,8 +142,8 @@ __device__ __forceinline__ void warp_tile_df(const mwsep_area_dev& A, const mwse
     const D::df2 r0 = D::dup(D::from_double(th.r0));
     const D::df2 al = D::dup(D::from_double(th.alpha)), ad3 = D::dup(D::from_double(th.alpha_delta3));
     const int C = A.convolve;
-    const int k0 = kc * A.k_chunk;
-    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int k0 = tp.k0;
+    const int k1 = tp.k1;
     const int nf = (k1 - k0) * C;
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     for (int g0 = 0; g0 < nf; g0 += 32 * DFP)
@@ -566,15 +563,16 @@ int launch_likelihood(const mwsep_stars_dev* St, const float4* pdf, const mwsep_
 
 /* The column-independent background shares of an area integral, summed
  * over the area's cells as cpu/evaluation_optimized.c:498-520 does (times
- * V = irv_k ids_j):
+ * V = irv_k ids_j), box by box (the whole area is one box):
  *  - the aux profile (form 1: alpha = delta = 1 plus qw (a g^2 + b g + c),
  *    :234-239, times reff):
- *      mu_steps * sum_j ids_j * sum_k irv_k reff_k sum_n qw_kn (a g2_kn + b g_kn + c);
+ *      mu_n * sum_j ids_j * sum_k irv_k reff_k sum_n qw_kn (a g2_kn + b g_kn + c);
  *  - q = 0 (form 3: bg = -1 per cell, no reff, :213-216):
- *      mu_steps * sum_j ids_j * sum_k irv_k * (-1).
- * O(R C) work in FP64, added (TwoSum) to block 0's background partial of
- * the area after the double-float kernel has written it.  One block per
- * theta; thetas of the other forms are left alone. */
+ *      mu_n * sum_j ids_j * sum_k irv_k * (-1),
+ * j and k over the box's nu steps and r-bins.  O(R C) work in FP64, added
+ * (TwoSum) to block 0's background partial of the area after the
+ * double-float kernel has written it.  One block per theta; thetas of the
+ * other forms are left alone. */
 __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts* __restrict__ thetas,
                                 double2* __restrict__ partials, long long theta_stride)
 {
@@ -583,28 +581,39 @@ __global__ void aux_area_kernel(const mwsep_area_dev A, const mwsep_theta_consts
     const int form = mwsep_bg_form(th);
     if (form != 1 && form != 3) return; /* uniform per block */
     const double a = th->bg_a, b = th->bg_b, c = th->bg_c;
-    mwsep::comp_sum acc[2];
-    acc[0].zero();
-    acc[1].zero();
     const int C = A.convolve;
-    for (int k = threadIdx.x; k < A.r_steps; k += blockDim.x)
+    double total = 0.0;
+#pragma unroll 1
+    for (int bi = 0; bi < A.n_boxes; ++bi)
     {
-        if (form == 3)
+        mwsep_box bx = A.box[0];
+#pragma unroll
+        for (int i = 1; i < MWSEP_MAX_BOXES; ++i)
+            if (i == bi) bx = A.box[i];
+        mwsep::comp_sum acc[2];
+        acc[0].zero();
+        acc[1].zero();
+        for (int k = bx.r0 + threadIdx.x; k < bx.r0 + bx.r_n; k += blockDim.x)
         {
-            acc[0].add(-A.irv[k]);
-            continue;
+            if (form == 3)
+            {
+                acc[0].add(-A.irv[k]);
+                continue;
+            }
+            const size_t row = (size_t)k * C;
+            double v = 0.0;
+            for (int n = 0; n < C; ++n)
+                v += A.qw[row + n] * (a * A.r_in_mag2[row + n] + b * A.r_in_mag[row + n] + c);
+            acc[0].add(v * A.reff[k] * A.irv[k]);
         }
-        const size_t row = (size_t)k * C;
-        double v = 0.0;
-        for (int n = 0; n < C; ++n)
-            v += A.qw[row + n] * (a * A.r_in_mag2[row + n] + b * A.r_in_mag[row + n] + c);
-        acc[0].add(v * A.reff[k] * A.irv[k]);
+        for (int j = bx.nu0 + threadIdx.x; j < bx.nu0 + bx.nu_n; j += blockDim.x) acc[1].add(A.ids[j]);
+        mwsep::block_reduce<2>(acc, red);
+        if (threadIdx.x == 0) total += (acc[0].s + acc[0].c) * (acc[1].s + acc[1].c) * (double)bx.mu_n;
+        __syncthreads(); /* red is reused by the next box */
     }
-    for (int j = threadIdx.x; j < A.nu_steps; j += blockDim.x) acc[1].add(A.ids[j]);
-    mwsep::block_reduce<2>(acc, red);
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0 && A.n_boxes > 0)
     {
-        const double v = (acc[0].s + acc[0].c) * (acc[1].s + acc[1].c) * (double)A.mu_steps;
+        const double v = total;
         double2* p = partials + (size_t)blockIdx.y * theta_stride;
         const double s = p->x + v;
         const double bb = s - p->x;

@@ -428,10 +428,10 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
                                               const BgConsts& bc, long long item, double (&acc)[1 + S])
 {
     const int C = A.convolve;
-    const int kc = (int)(item / A.n_cols);
-    const int col = (int)(item - (long long)kc * A.n_cols);
-    const int k0 = kc * A.k_chunk;
-    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const mwsep::ItemPos ip = mwsep::item_pos(A, item);
+    const int col = ip.col;
+    const int k0 = ip.k0;
+    const int k1 = ip.k1;
     Col<S> cc;
     int eref[SArr<S>::N];
     item_prologue<S>(A, th, col, k0, k1, cc, eref);
@@ -451,7 +451,7 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
     }
     /* the table weights carry reff*irv; the nu-slab factor ids[j] and the
      * hand-off to FP64 happen once per item */
-    const double idsj = A.ids[MWSEP_IDX(col % A.nu_steps, A.nu_steps, 3)];
+    const double idsj = A.ids[MWSEP_IDX(ip.nu, A.nu_steps, 3)];
     acc[0] += kb.value() * idsj;
 #pragma unroll
     for (int s = 0; s < S; ++s) acc[1 + s] += ks[s].value() * (idsj * exp_scale(eref[s]));
@@ -529,16 +529,13 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
     constexpr int P = mwsep::TileP<S>::P;
     constexpr int CW = ColWords<S>::N;
     const int lane = threadIdx.x & 31;
-    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
-    const long long rest = wt / nmb;
-    const int mb = (int)(wt - rest * nmb);
-    const int kc = (int)(rest / A.nu_steps);
-    const int nu = (int)(rest - (long long)kc * A.nu_steps);
-    const int mu0 = mb * mwsep::kTileCols;
-    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+    const mwsep::TilePos tp = mwsep::tile_pos(A, wt);
+    const int nu = tp.nu;
+    const int mu0 = tp.mu0;
+    const int ncols = tp.ncols;
     const int C = A.convolve;
-    const int k0 = kc * A.k_chunk;
-    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int k0 = tp.k0;
+    const int k1 = tp.k1;
     /* the column constants, each stream's exponent shifted by the tile's
      * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
@@ -779,16 +776,13 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
     constexpr int CW = PackedTile<S>::W;
     static_assert(NP % 2 == 0, "pairs are taken two at a time");
     const int lane = threadIdx.x & 31;
-    const int nmb = (A.mu_steps + mwsep::kTileCols - 1) / mwsep::kTileCols;
-    const long long rest = wt / nmb;
-    const int mb = (int)(wt - rest * nmb);
-    const int kc = (int)(rest / A.nu_steps);
-    const int nu = (int)(rest - (long long)kc * A.nu_steps);
-    const int mu0 = mb * mwsep::kTileCols;
-    const int ncols = min(mwsep::kTileCols, A.mu_steps - mu0);
+    const mwsep::TilePos tp = mwsep::tile_pos(A, wt);
+    const int nu = tp.nu;
+    const int mu0 = tp.mu0;
+    const int ncols = tp.ncols;
     const int C = A.convolve;
-    const int k0 = kc * A.k_chunk;
-    const int k1 = min(k0 + A.k_chunk, A.r_steps);
+    const int k0 = tp.k0;
+    const int k1 = tp.k1;
     /* the column constants, each stream's exponent shifted by the tile's
      * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];

@@ -1,19 +1,21 @@
 /* mwsep_f64.cu -- plain FP64 integral and likelihood kernels (the drop-in
  * form, MWSEP_PLAIN_F64).
  *
- * Arithmetic: every operation of calculate_probabilities
- * (cpu/evaluation_optimized.c:190-299) in the reference's association
- * order, compiled with -fmad=false (no a*b+c contraction), IEEE division and
- * square root.  Per cell the convolution points are summed in the
- * reference's order n = 0..C-1, then multiplied by reff_xr_rp3 and by the
- * cell volume V = irv[k]*ids[j] (:500-504, :513).  Cells are Kahan-summed
- * per thread, then combined error-free across the block; blocks are combined
- * by mwsep_reduce.cu in a fixed order.
+ * Arithmetic: FP64 throughout (mwsep_f64_point.cuh): the likelihood in the
+ * reference's own operation order (convolve_f64), the integral in the
+ * completed-square form (convolve_f64_cs), compiled with -fmad=false.  Per
+ * cell the convolution points are summed in order n = 0..C-1, then
+ * multiplied by reff_xr_rp3 and by the cell volume V = irv[k]*ids[j]
+ * (cpu/evaluation_optimized.c:500-504, :513).  Cells are Kahan-summed per
+ * thread, then combined error-free across the block; blocks are combined by
+ * mwsep_reduce.cu in a fixed order.
  *
  * Mapping: one thread owns a (mu, nu) column and a contiguous run of
- * k_chunk r-bins ("item"); consecutive threads own consecutive columns of
- * the same r-run, so every r-bin table read is warp-uniform.  Grid-stride
- * loop over items; gridDim.y indexes the parameter vector of a batch.
+ * k_chunk r-bins ("item", mwsep::item_pos); consecutive threads own
+ * consecutive columns of the same r-run, so every r-bin table read is
+ * warp-uniform.  Grid-stride loop over the items of the cells the area
+ * integrates (all of them, or a rank's slice); gridDim.y indexes the
+ * parameter vector of a batch.
  */
 #include <cuda_runtime.h>
 #include <math.h>

@@ -1,13 +1,23 @@
 /* mwsep_f64_point.cuh -- the plain-FP64 density evaluation shared by every
  * FP64 kernel (single evaluation, batches, the tiled engine).
  *
- * Every operation of calculate_probabilities
- * (cpu/evaluation_optimized.c:190-299) in the reference's association order;
- * translation units that include this compile with -fmad=false (no a*b+c
- * contraction), with IEEE division and square root.  Per cell the
- * convolution points are summed in the reference's order n = 0..C-1, then
- * multiplied by reff_xr_rp3 and by the cell volume V = irv[k]*ids[j]
- * (:500-504, :513), and cells are Kahan-summed as the reference does.
+ * Two forms of calculate_probabilities (cpu/evaluation_optimized.c:190-299):
+ *  - convolve_f64, used per star by the likelihood and separation kernels:
+ *    every operation in the reference's association order, IEEE division,
+ *    square root and exp;
+ *  - convolve_f64_cs, used per cell by the integral kernels: the same
+ *    densities with the geometry rewritten as completed squares in r
+ *    (column_consts_f64), e^x by Tang's table method (exp_tang) and the
+ *    Hernquist divide as a Newton-Raphson reciprocal (rcp_nr), with explicit
+ *    FMAs.  Its rounding differs from the reference's; measured against the
+ *    reference's own outputs it stays within 4e-15 relative per integral on
+ *    the reference's test fixtures and 6.4e-16 on the full-size wedge
+ *    (1.72e10 points), against the 1e-12 bound of the plain form.
+ * Translation units that include this compile with -fmad=false, so only the
+ * written FMAs are fused.  Per cell the convolution points are summed in
+ * order n = 0..C-1, then multiplied by reff_xr_rp3 and by the cell volume
+ * V = irv[k]*ids[j] (:500-504, :513), and each thread Kahan-sums its cells
+ * as the reference does.
  */
 #ifndef MWSEP_F64_POINT_CUH
 #define MWSEP_F64_POINT_CUH
@@ -254,16 +264,12 @@ __device__ __forceinline__ void integral_item(const mwsep_area_dev& A, const mws
 {
     const int S = th.n_streams;
     const int C = A.convolve;
-    const int kc = (int)(item / A.n_cols);
-    const int col = (int)(item - (long long)kc * A.n_cols);
-    const int j = col % A.nu_steps;
-    const double* g = A.geom + 4 * (size_t)MWSEP_IDX(col, A.n_cols, 1);
+    const mwsep::ItemPos ip = mwsep::item_pos(A, item);
+    const double* g = A.geom + 4 * (size_t)MWSEP_IDX(ip.col, A.n_cols, 1);
     ColF64<SMAX> cc;
     column_consts_f64<SMAX>(g[0], g[1], g[2], g[3], th, cc);
-    const double idsj = A.ids[MWSEP_IDX(j, A.nu_steps, 3)];
-    const int k0 = kc * A.k_chunk;
-    const int k1 = min(k0 + A.k_chunk, A.r_steps);
-    for (int k = k0; k < k1; ++k)
+    const double idsj = A.ids[MWSEP_IDX(ip.nu, A.nu_steps, 3)];
+    for (int k = ip.k0; k < ip.k1; ++k)
     {
         const double V = A.irv[MWSEP_IDX(k, A.r_steps, 4)] * idsj;
         double bg, st[SMAX];

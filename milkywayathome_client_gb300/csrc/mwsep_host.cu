@@ -220,6 +220,7 @@ int check_problem(const ASTRONOMY_PARAMETERS* ap)
         const INTEGRAL* in = ap->integral[i];
         if (!in || in->mu_steps < 1 || in->nu_steps < 1 || in->r_steps < 1) return MWSEP_ERR_ARG;
         if ((long long)in->mu_steps * in->nu_steps > (1LL << 30)) return MWSEP_ERR_UNSUPPORTED;
+        if (in->min_calculation < 0) return MWSEP_ERR_ARG;
     }
     return MWSEP_OK;
 }
@@ -271,6 +272,8 @@ void copy_problem(const ASTRONOMY_PARAMETERS* ap, ProblemHost& p)
         A.mu_step = (A.mu_max - A.mu_min) / A.mu_steps;
         A.nu_step = (A.nu_max - A.nu_min) / A.nu_steps;
         A.r_step = (A.r_max - A.r_min) / A.r_steps;
+        mwsep::effective_slice(in->min_calculation, in->max_calculation,
+                               (long long)A.mu_steps * A.nu_steps * A.r_steps, A.cell_begin, A.cell_end);
     }
     int n = 0;
     for (int i = 0; i < p.n_bg; ++i) n += p.bg_opt[i] ? 1 : 0;
@@ -635,18 +638,30 @@ int build_area(mwsep_ctx* c, Wedge& w, int a)
     v.ids = D.ids.as<double>();
     v.pts = D.pts.as<float4>();
     v.ptsdf = D.ptsdf.as<float4>();
+    set_slice(v, A.cell_begin, A.cell_end);
     return MWSEP_OK;
 }
 
 } // namespace
 
-void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items)
+int wedge_set_slices(mwsep_ctx* c, Wedge& w, const long* min_calc, const long* max_calc)
 {
-    v.k_chunk = std::max(1, std::min(k_chunk, v.r_steps));
-    v.n_kchunks = (v.r_steps + v.k_chunk - 1) / v.k_chunk;
-    v.warp_items = warp_items ? 1 : 0;
-    v.n_items = warp_items ? mwsep::warp_tile_count(v.mu_steps, v.nu_steps, v.n_kchunks)
-                           : (long long)v.n_cols * v.n_kchunks;
+    for (int a = 0; a < w.prob.n_areas; ++a)
+    {
+        AreaHost& A = w.prob.area[a];
+        long long b, e;
+        if (!mwsep::effective_slice(min_calc[a], max_calc[a], (long long)A.mu_steps * A.nu_steps * A.r_steps, b, e))
+            return mwsep_fail(MWSEP_ERR_ARG);
+        A.cell_begin = b;
+        A.cell_end = e;
+        mwsep_area_dev& v = w.areas[a].view;
+        if (v.cell_begin != b || v.cell_end != e)
+        {
+            set_slice(v, b, e);
+            c->eng.desc_dirty = true;
+        }
+    }
+    return MWSEP_OK;
 }
 
 int warp_tile_kstep(int convolve, int n_streams)
@@ -861,6 +876,15 @@ int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap)
         if (same_tables(next, w.prob))
         {
             w.prob = next;
+            for (int a = 0; a < w.prob.n_areas; ++a)
+            {
+                mwsep_area_dev& v = w.areas[a].view;
+                if (v.cell_begin != w.prob.area[a].cell_begin || v.cell_end != w.prob.area[a].cell_end)
+                {
+                    set_slice(v, w.prob.area[a].cell_begin, w.prob.area[a].cell_end);
+                    c->eng.desc_dirty = true;
+                }
+            }
             return MWSEP_OK;
         }
     }
@@ -1484,9 +1508,26 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
         mwsep_fail(MWSEP_ERR_STATE);
         return nan;
     }
+    /* calculate_integral walks each area from the state's min_calculation
+     * (reset_evaluation_state, cpu/evaluation_state.c:197) to its
+     * max_calculation (cpu/evaluation_optimized.c:521-527) */
+    mwsep_ctx* c = g_default;
+    {
+        long mn[MWSEP_MAX_AREAS], mx[MWSEP_MAX_AREAS];
+        for (int a = 0; a < ap->number_integrals; ++a)
+        {
+            if (!es->integral[a])
+            {
+                mwsep_fail(MWSEP_ERR_STATE);
+                return nan;
+            }
+            mn[a] = es->integral[a]->min_calculation;
+            mx[a] = es->integral[a]->max_calculation;
+        }
+        if (wedge_set_slices(c, *c->wedges[0], mn, mx) != MWSEP_OK) return nan;
+    }
     /* the catalogue goes up on the side stream while the integral (which
      * does not read it) runs; the likelihood waits for it */
-    mwsep_ctx* c = g_default;
     if (!sp->stars || sp->number_stars < 1)
     {
         mwsep_fail(MWSEP_ERR_ARG);
@@ -1518,7 +1559,9 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
         INTEGRAL_AREA* ia = es->integral[a];
         ia->background_integral = r.area_integrals[a][0];
         for (int s = 0; s < S; ++s) ia->stream_integrals[s] = r.area_integrals[a][1 + s];
-        ia->current_calculation = ia->max_calculation;
+        /* where calculate_integral's walk stopped: after its last cell */
+        const AreaHost& A = c->wedges[0]->prob.area[a];
+        ia->current_calculation = A.cell_begin < A.cell_end ? (long)A.cell_end : ia->min_calculation;
     }
     es->current_integral = ap->number_integrals;
     es->background_integral = r.background_integral;

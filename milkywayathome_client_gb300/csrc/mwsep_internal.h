@@ -8,8 +8,10 @@
 
 #ifdef __CUDACC__
 #define MWSEP_HD __host__ __device__
+#define MWSEP_HDI __host__ __device__ __forceinline__
 #else
 #define MWSEP_HD
+#define MWSEP_HDI inline
 #endif
 
 /* include/milkyway.h:46-52 (pi is M_PI on glibc; deg = 180/pi) and the
@@ -55,17 +57,37 @@ typedef struct
     float kf[MWSEP_KMAX_STREAMS];
 } mwsep_theta_consts;
 
+/* A rectangular block of an area's cells: mu steps [mu0, mu0 + mu_n), nu
+ * steps [nu0, nu0 + nu_n), r-bins [r0, r0 + r_n).  The cells an area
+ * integrates -- all of them, or the slice [min_calculation, max_calculation)
+ * of the linearised index (mu * nu_steps + nu) * r_steps + r that
+ * calculate_integral walks (cpu/evaluation_optimized.c:461-530,
+ * cpu/evaluation_state.c:129-151) -- are the union of at most
+ * MWSEP_MAX_BOXES boxes, enumerated box after box. */
+typedef struct
+{
+    int mu0, mu_n, nu0, nu_n, r0, r_n;
+    int n_kchunks;       /* ceil(r_n / k_chunk) */
+    int pad0;
+    long long first;     /* the box's first item (or warp tile) in the area's enumeration */
+} mwsep_box;
+#define MWSEP_MAX_BOXES 5
+
 /* One integral area on the device. */
 typedef struct
 {
-    int mu_steps, nu_steps, r_steps, convolve;
+    int mu_steps, nu_steps, r_steps, convolve; /* the grid the tables hold */
     int n_cols;          /* mu_steps * nu_steps */
     int k_chunk;         /* r-bins per item */
     int n_kchunks;       /* ceil(r_steps / k_chunk) */
     int warp_items;      /* 0: an item is (column, r-chunk), one thread;
                             1: an item is a warp tile (32 mu-columns at one nu, r-chunk) */
-    long long n_items;   /* thread items: n_cols * n_kchunks;
-                            warp tiles: n_kchunks * nu_steps * ceil(mu_steps / 32) */
+    long long n_items;   /* items over all boxes; for the whole area, thread items:
+                            n_cols * n_kchunks; warp tiles: n_kchunks * nu_steps * ceil(mu_steps / 32) */
+    long long cell_begin, cell_end; /* the cells integrated, [begin, end) of the linearised index */
+    int n_boxes;         /* 0 (nothing to integrate) .. MWSEP_MAX_BOXES */
+    int pad1;
+    mwsep_box box[MWSEP_MAX_BOXES];
     const double* geom;      /* [mu][nu] x 4: bsin, bcos, lsin, lcos */
     const double* r_point;   /* [R][C] */
     const double* qw;        /* [R][C]  qw_r3_N */
@@ -116,6 +138,174 @@ struct TileP
 MWSEP_HD inline long long warp_tile_count(int mu_steps, int nu_steps, int n_kchunks)
 {
     return (long long)n_kchunks * nu_steps * ((mu_steps + kTileCols - 1) / kTileCols);
+}
+
+/* The cells calculate_integral visits for an INTEGRAL_AREA with
+ * [min_calculation, max_calculation) over a grid of `total` cells
+ * (cpu/evaluation_optimized.c:461-530): it starts at min_calculation
+ * (get_steps, cpu/evaluation_state.c:129-151) and stops after the first cell
+ * that brings the count to max_calculation, so a slice with max <= min still
+ * integrates the one cell min, and a start at or past the end integrates
+ * nothing.  Returns false for a negative start (outside the reference's
+ * domain: its get_steps would index before the grid). */
+inline bool effective_slice(long long min_calc, long long max_calc, long long total, long long& begin,
+                            long long& end)
+{
+    if (min_calc < 0) return false;
+    begin = min_calc < total ? min_calc : total;
+    end = max_calc > begin + 1 ? max_calc : begin + 1;
+    if (end > total) end = total;
+    return true;
+}
+
+/* The cells [begin, end) of the linearised index of an M x NU x R grid as
+ * at most MWSEP_MAX_BOXES boxes in index order: the rest of the first
+ * column, the rest of its mu row, the whole mu rows between, the start of
+ * the last mu row, the start of the last column.  Returns the box count
+ * (0 for an empty range); firsts and chunk counts are set by the caller. */
+inline int slice_boxes(int M, int NU, int R, long long begin, long long end, mwsep_box* out)
+{
+    int n = 0;
+    auto put = [&](int mu0, int mu_n, int nu0, int nu_n, int r0, int r_n) {
+        if (mu_n <= 0 || nu_n <= 0 || r_n <= 0) return;
+        mwsep_box& b = out[n++];
+        b.mu0 = mu0, b.mu_n = mu_n, b.nu0 = nu0, b.nu_n = nu_n, b.r0 = r0, b.r_n = r_n;
+        b.n_kchunks = 0, b.pad0 = 0, b.first = 0;
+    };
+    if (end <= begin) return 0;
+    const long long rowc = (long long)NU * R; /* cells per mu row */
+    const int ib = (int)(begin / rowc), jb = (int)((begin / R) % NU), kb = (int)(begin % R);
+    const long long last = end - 1;
+    const int ie = (int)(last / rowc), je = (int)((last / R) % NU), ke = (int)(last % R) + 1;
+    if (ib == ie && jb == je)
+    {
+        put(ib, 1, jb, 1, kb, ke - kb);
+        return n;
+    }
+    /* first column: [kb, R) unless it starts at 0 (then it joins its row) */
+    int jrow = jb;
+    if (kb > 0)
+    {
+        put(ib, 1, jb, 1, kb, R - kb);
+        jrow = jb + 1;
+    }
+    /* the last column: [0, ke) unless it ends at R (then it joins its row) */
+    int jend = je + 1; /* columns [.., jend) of the last row are whole */
+    const bool last_partial = ke < R;
+    if (last_partial) jend = je;
+    if (ib == ie)
+    {
+        put(ib, 1, jrow, jend - jrow, 0, R);
+    }
+    else
+    {
+        /* the rest of the first row, whole rows between, the start of the last row */
+        if (jrow > 0)
+            put(ib, 1, jrow, NU - jrow, 0, R);
+        const int mu_first_whole = jrow > 0 ? ib + 1 : ib;
+        if (jend == NU)
+            put(mu_first_whole, ie + 1 - mu_first_whole, 0, NU, 0, R);
+        else
+        {
+            put(mu_first_whole, ie - mu_first_whole, 0, NU, 0, R);
+            put(ie, 1, 0, jend, 0, R);
+        }
+    }
+    if (last_partial) put(ie, 1, je, 1, 0, ke);
+    return n;
+}
+
+/* The cells an area view integrates (set_chunking turns them into boxes). */
+inline void set_slice(mwsep_area_dev& v, long long begin, long long end)
+{
+    v.cell_begin = begin;
+    v.cell_end = end;
+}
+
+/* An area view's chunking -- k_chunk r-bins per item, warp tiles or thread
+ * items -- and, from its [cell_begin, cell_end), its boxes, their first
+ * items and the item count. */
+inline void set_chunking(mwsep_area_dev& v, int k_chunk, int warp_items)
+{
+    v.k_chunk = k_chunk < 1 ? 1 : (k_chunk > v.r_steps ? v.r_steps : k_chunk);
+    v.n_kchunks = (v.r_steps + v.k_chunk - 1) / v.k_chunk;
+    v.warp_items = warp_items ? 1 : 0;
+    v.n_boxes = slice_boxes(v.mu_steps, v.nu_steps, v.r_steps, v.cell_begin, v.cell_end, v.box);
+    long long first = 0;
+    for (int b = 0; b < v.n_boxes; ++b)
+    {
+        mwsep_box& x = v.box[b];
+        x.n_kchunks = (x.r_n + v.k_chunk - 1) / v.k_chunk;
+        x.first = first;
+        first += warp_items ? warp_tile_count(x.mu_n, x.nu_n, x.n_kchunks) : (long long)x.mu_n * x.nu_n * x.n_kchunks;
+    }
+    for (int b = v.n_boxes; b < MWSEP_MAX_BOXES; ++b)
+    {
+        v.box[b] = mwsep_box{};
+        v.box[b].first = first; /* past every item: never selected */
+    }
+    v.n_items = first;
+}
+
+/* Where an item or a warp tile of an area lies: its column (mu * nu_steps +
+ * nu), nu step, first mu step and column count (warp tiles), r-bins [k0, k1). */
+struct ItemPos
+{
+    int col, nu, k0, k1;
+};
+struct TilePos
+{
+    int mu0, ncols, nu, k0, k1;
+};
+
+/* The box holding item (or warp tile) idx: the last one starting at or
+ * before it.  Fields are picked with constant indices, so the descriptor is
+ * read where it lives (kernel parameters or shared memory). */
+MWSEP_HDI mwsep_box box_of(const mwsep_area_dev& A, long long idx)
+{
+    mwsep_box b = A.box[0];
+#pragma unroll
+    for (int i = 1; i < MWSEP_MAX_BOXES; ++i)
+        if (i < A.n_boxes && idx >= A.box[i].first) b = A.box[i];
+    return b;
+}
+
+/* A thread item: a column of the box and a run of k_chunk of its r-bins;
+ * consecutive items are consecutive columns of one r-run.  For a whole
+ * area this is item = kc * n_cols + col. */
+MWSEP_HDI ItemPos item_pos(const mwsep_area_dev& A, long long item)
+{
+    const mwsep_box b = box_of(A, item);
+    const long long local = item - b.first;
+    const long long cols = (long long)b.mu_n * b.nu_n;
+    const int kc = (int)(local / cols);
+    const int cl = (int)(local - kc * cols);
+    const int il = cl / b.nu_n;
+    ItemPos p;
+    p.nu = b.nu0 + (cl - il * b.nu_n);
+    p.col = (b.mu0 + il) * A.nu_steps + p.nu;
+    p.k0 = b.r0 + kc * A.k_chunk;
+    p.k1 = p.k0 + A.k_chunk < b.r0 + b.r_n ? p.k0 + A.k_chunk : b.r0 + b.r_n;
+    return p;
+}
+
+/* A warp tile: up to 32 mu-columns of the box at one nu and a run of k_chunk
+ * of its r-bins, mu blocks fastest, then nu, then r-chunks. */
+MWSEP_HDI TilePos tile_pos(const mwsep_area_dev& A, long long wt)
+{
+    const mwsep_box b = box_of(A, wt);
+    const long long local = wt - b.first;
+    const int nmb = (b.mu_n + kTileCols - 1) / kTileCols;
+    const long long rest = local / nmb;
+    const int mb = (int)(local - rest * nmb);
+    const int kc = (int)(rest / b.nu_n);
+    TilePos p;
+    p.nu = b.nu0 + (int)(rest - (long long)kc * b.nu_n);
+    p.mu0 = b.mu0 + mb * kTileCols;
+    p.ncols = kTileCols < b.mu0 + b.mu_n - p.mu0 ? kTileCols : b.mu0 + b.mu_n - p.mu0;
+    p.k0 = b.r0 + kc * A.k_chunk;
+    p.k1 = p.k0 + A.k_chunk < b.r0 + b.r_n ? p.k0 + A.k_chunk : b.r0 + b.r_n;
+    return p;
 }
 } // namespace mwsep
 #endif

@@ -26,6 +26,8 @@
  */
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -44,6 +46,25 @@ constexpr size_t kAreasOffset = 1024;
 constexpr size_t kPartialsOffset = 2048;
 constexpr int kBlock = 256;
 constexpr int kMaxDevices = 64;
+
+/* The layout holds for every accepted request: the constants fit their
+ * slot, one area's 1 + S results fit theirs, and the stream limit the call
+ * accepts is one the kernels are specialised for (blocks_per_sm is indexed
+ * by it). */
+static_assert(sizeof(mwsep_theta_consts) <= kAreasOffset - kThetaOffset, "constants overlap the area results");
+static_assert((1 + MWSEP_MAX_STREAMS) * sizeof(double) <= kPartialsOffset - kAreasOffset,
+              "area results overlap the partial sums");
+static_assert(MWSEP_MAX_STREAMS <= MWSEP_KMAX_STREAMS, "stream limit beyond the kernels' specialisation");
+static_assert(kPartialsOffset + (1 + MWSEP_MAX_STREAMS) * sizeof(double2) <= MWSEP_NOALLOC_SCRATCH_BYTES,
+              "no room for one block's partial sums");
+
+/* A failed launch: its name and CUDA error under MWSEP_DEBUG, then the
+ * status (the CUDA error itself is cleared by cudaGetLastError). */
+int launch_failed(const char* what, cudaError_t e)
+{
+    if (getenv("MWSEP_DEBUG")) fprintf(stderr, "mwsep_area_integrals_noalloc: %s failed: %s\n", what, cudaGetErrorString(e));
+    return mwsep_fail(MWSEP_ERR_CUDA);
+}
 
 struct DeviceSetup
 {
@@ -103,6 +124,10 @@ extern "C" int mwsep_area_integrals_noalloc(const mwsep_area_tables* t, const mw
     if (p->number_streams < 0 || p->number_streams > MWSEP_MAX_STREAMS) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     if (t->convolve > MWSEP_MAX_CONVOLVE) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     if ((long long)t->mu_steps * t->nu_steps > (1LL << 30)) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
+    const long long cols = (long long)t->mu_steps * t->nu_steps;
+    long long cell_begin, cell_end;
+    if (!mwsep::effective_slice(t->min_calculation, t->max_calculation, cols * t->r_steps, cell_begin, cell_end))
+        return mwsep_fail(MWSEP_ERR_ARG);
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
@@ -151,16 +176,11 @@ extern "C" int mwsep_area_integrals_noalloc(const mwsep_area_tables* t, const mw
 
     /* launch shape: a persistent grid that fits the fixed partial-sum area,
      * items of ~48 per thread as the context path picks them */
-    const long long cols = (long long)t->mu_steps * t->nu_steps;
     const int per_sm = d->blocks_per_sm[S];
     long long grid = std::min<long long>((long long)d->sm_count * per_sm, grid_cap);
     const long long want_items = grid * kBlock * 48;
     long long chunks = std::max<long long>(1, std::min<long long>((want_items + cols - 1) / cols, t->r_steps));
     const int k_chunk = (int)((t->r_steps + chunks - 1) / chunks);
-    const long long items = cols * ((t->r_steps + k_chunk - 1) / k_chunk);
-    grid = std::max<long long>(1, std::min<long long>(grid, (items + kBlock - 1) / kBlock));
-    if (kPartialsOffset + (size_t)grid * per_block > MWSEP_NOALLOC_SCRATCH_BYTES)
-        return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
 
     mwsep_area_dev a;
     memset(&a, 0, sizeof(a));
@@ -169,9 +189,11 @@ extern "C" int mwsep_area_integrals_noalloc(const mwsep_area_tables* t, const mw
     a.r_steps = t->r_steps;
     a.convolve = t->convolve;
     a.n_cols = (int)cols;
-    a.k_chunk = k_chunk;
-    a.n_kchunks = (t->r_steps + k_chunk - 1) / k_chunk;
-    a.n_items = items;
+    mwsep::set_slice(a, cell_begin, cell_end);
+    mwsep::set_chunking(a, k_chunk, 0); /* the slice's boxes and item count */
+    grid = std::max<long long>(1, std::min<long long>(grid, (a.n_items + kBlock - 1) / kBlock));
+    if (kPartialsOffset + (size_t)grid * per_block > MWSEP_NOALLOC_SCRATCH_BYTES)
+        return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     a.geom = t->geom;
     a.r_point = t->r_point;
     a.qw = t->qw_r3_N;
@@ -197,10 +219,13 @@ extern "C" int mwsep_area_integrals_noalloc(const mwsep_area_tables* t, const mw
     sh.grid = (int)grid;
 
     store_theta_kernel<<<1, 32, 0, st>>>(th, d_th);
-    if (cudaGetLastError() != cudaSuccess) return mwsep_fail(MWSEP_ERR_CUDA);
-    if (mwsep_launch_integral_f64(&a, d_th, &sh, d_part, st) != 0) return mwsep_fail(MWSEP_ERR_CUDA);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return launch_failed("the constants' store", e);
+    e = (cudaError_t)mwsep_launch_integral_f64(&a, d_th, &sh, d_part, st);
+    if (e != cudaSuccess) return launch_failed("the integral", e);
     /* one area: the reduction's cut-subtracted result is the area result and
      * goes straight to the caller's buffer */
-    if (mwsep_launch_reduce_integrals(d_part, &sh, d_areas, d_integrals, st) != 0) return mwsep_fail(MWSEP_ERR_CUDA);
+    e = (cudaError_t)mwsep_launch_reduce_integrals(d_part, &sh, d_areas, d_integrals, st);
+    if (e != cudaSuccess) return launch_failed("the reduction", e);
     return MWSEP_OK;
 }

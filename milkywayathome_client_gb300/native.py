@@ -30,6 +30,7 @@ MWSEP_ERR_STATE = 10
 
 MWSEP_MAX_STREAMS = 8
 MWSEP_MAX_AREAS = 8
+MWSEP_MAX_CONVOLVE = 512
 
 MWSEP_PLAIN_F64 = 0
 MWSEP_MIXED_F32 = 1
@@ -131,7 +132,8 @@ class mwsep_area_tables(C.Structure):
     _fields_ = [("mu_steps", C.c_int), ("nu_steps", C.c_int), ("r_steps", C.c_int), ("convolve", C.c_int),
                 ("geom", C.c_void_p), ("r_point", C.c_void_p), ("qw_r3_N", C.c_void_p),
                 ("r_in_mag", C.c_void_p), ("r_in_mag2", C.c_void_p), ("reff_xr_rp3", C.c_void_p),
-                ("irv", C.c_void_p), ("ids", C.c_void_p)]
+                ("irv", C.c_void_p), ("ids", C.c_void_p),
+                ("min_calculation", C.c_long), ("max_calculation", C.c_long)]
 
 
 class mwsep_density_params(C.Structure):

@@ -64,6 +64,7 @@ class Oracle:
             L.so_cell_values.argtypes = [C.c_void_p, _D, C.c_int, _D]
             L.so_cell_lb.argtypes = [C.c_void_p, C.c_int, _D]
             L.so_r_tables.argtypes = [C.c_void_p, C.c_int, _D, _D, _D, _D, _D, _D]
+            L.so_r_mag_tables.argtypes = [C.c_void_p, C.c_int, _D, _D]
             L.so_star_densities.argtypes = [C.c_void_p, _D, _D, _D]
             L.so_gauss_legendre.argtypes = [C.c_int, _D, _D]
             L.so_gc_to_lb.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]

@@ -1258,6 +1258,21 @@ int so_r_tables(so_problem* p, int area, double* irv, double* reff, double* r_po
     return 0;
 }
 
+int so_r_mag_tables(so_problem* p, int area, double* r_in_mag, double* r_in_mag2)
+{
+    so_consts k;
+    so_rtab t;
+    if (area < 0 || area >= p->n_areas)
+        return 1;
+    so_init_consts(p, &k);
+    so_build_rtab(p, &k, &p->area[area], &t);
+    memcpy(r_in_mag, t.r_in_mag, sizeof(double) * (size_t)t.R * t.C);
+    memcpy(r_in_mag2, t.r_in_mag2, sizeof(double) * (size_t)t.R * t.C);
+    so_free_rtab(&t);
+    so_free_consts(&k);
+    return 0;
+}
+
 int so_star_densities(so_problem* p, const double* theta, double* bg, double* st)
 {
     so_consts k;

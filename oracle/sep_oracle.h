@@ -69,6 +69,9 @@ int so_cell_lb(so_problem* p, int area, double* out);
  * irv[R], reff_xr_rp3[R], r_point[R][C], qw_r3_N[R][C], ids[Nnu], nus[Nnu]. */
 int so_r_tables(so_problem* p, int area, double* irv, double* reff_xr_rp3,
                 double* r_point, double* qw_r3_N, double* ids, double* nus);
+/* The same area's r_in_mag / r_in_mag2 tables [R][C] (set_probability_constants,
+ * cpu/evaluation_optimized.c:159-188), for the aux profile. */
+int so_r_mag_tables(so_problem* p, int area, double* r_in_mag, double* r_in_mag2);
 
 /* Per-star unnormalised densities (calculate_probabilities on the star):
  * bg[N], st[N][S]. */
