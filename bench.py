@@ -61,8 +61,48 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the population-batch and serving measurements")
+    ap.add_argument("--workload", type=int, default=CONFIG_INDEX, choices=[0, 1, 2],
+                    help="benchmark config of the single-evaluation steps (default 1, the full-size wedge; "
+                         "0 and 2 are smaller wedges, for profiling runs)")
     ap.add_argument("--data-dir", default=os.path.join(tempfile.gettempdir(), "mwsep_bench_data"))
     return ap.parse_args()
+
+
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def workload_files(idx, data_dir):
+    """Parameter and star files of a benchmark config, with the reference's
+    own outputs on them when the repository holds them: configs 1 and 2 from
+    their committed inputs (tests/golden/scale, the reference CPU evaluator's
+    goldens), config 0 from tests/golden/cases/config0.  Returns (files,
+    golden evaluation or None)."""
+    import json as _json
+    import lzma
+    from milkywayathome_client_gb300 import synthetic as syn
+    src = {1: os.path.join(GOLDEN, "scale", "config1"), 2: os.path.join(GOLDEN, "scale", "config2"),
+           0: os.path.join(GOLDEN, "cases", "config0")}[idx]
+    gpath = os.path.join(src, "golden.json")
+    if not os.path.exists(gpath):
+        return [dict(syn.materialise(idx, data_dir)["files"][0])], None
+    os.makedirs(data_dir, exist_ok=True)
+    f = {"problem": syn.config(idx)["problems"][0]}
+    g = _json.load(open(gpath))
+    ev = g["evaluations"][0] if "evaluations" in g else g
+    f["params"] = os.path.join(src, "params.txt")
+    if os.path.exists(os.path.join(src, "stars.txt.xz")):
+        out = os.path.join(data_dir, f"config{idx}_golden_stars.txt")
+        if not os.path.exists(out):
+            with lzma.open(os.path.join(src, "stars.txt.xz"), "rb") as a, open(out + ".part", "wb") as b:
+                shutil.copyfileobj(a, b)
+            os.replace(out + ".part", out)
+        f["stars"] = out
+    else:
+        f["stars"] = os.path.join(src, "stars.txt")
+    f["theta"] = ev["theta"]
+    with open(f["stars"]) as fh:
+        f["n_stars"] = int(fh.readline())
+    return [f], ev
 
 
 def dist_setup():
@@ -163,9 +203,16 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU side
+def cpu_ranks(n_procs, slices=CPU_SLICES):
+    """The slices the CPU baseline times: n_procs ranks of `slices`, spread
+    evenly over the linearised cell index and the catalogue (the cost of a
+    slice depends on where it lies relative to the streams)."""
+    return [(i * slices) // n_procs for i in range(n_procs)]
+
+
 def cpu_sample(files, theta, n_procs, slices=CPU_SLICES):
-    """Run n_procs concurrent slices (ranks 0..n_procs-1 of `slices`) of the
-    evaluation on the host and return (wall seconds, kind, binary)."""
+    """Run n_procs concurrent slices (cpu_ranks) of the evaluation on the
+    host and return (wall seconds, kind, binary)."""
     from oracle import oracle as orc
     ref_bin, port_bin = orc.REF_BIN, orc.ORACLE_BIN
     kind, binary = None, None
@@ -187,7 +234,7 @@ def cpu_sample(files, theta, n_procs, slices=CPU_SLICES):
     t0 = time.perf_counter()
     procs = [subprocess.Popen([binary, "-a", f["params"], "-p", f["stars"], "-r", str(r), "-n", str(slices),
                                *args_theta], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
-             for r in range(n_procs)]
+             for r in cpu_ranks(n_procs, slices)]
     rcs = [p.wait() for p in procs]
     wall = time.perf_counter() - t0
     if any(rcs):
@@ -206,8 +253,7 @@ def run_reference_arm(args, ws, rank):
     """--impl reference: the reference's CPU evaluator on the host cores."""
     if rank != 0:
         return
-    from milkywayathome_client_gb300 import synthetic as syn
-    files = syn.materialise(CONFIG_INDEX, os.path.join(args.data_dir, "rank0"))["files"]
+    files, _ = workload_files(args.workload, os.path.join(args.data_dir, "rank0"))
     theta = files[0]["theta"]
     n = min(host_cores(), 64)
     times = []
@@ -219,7 +265,8 @@ def run_reference_arm(args, ws, rank):
     t = sum(times) / len(times)
     value = (n / CPU_SLICES) / t
     sample = (f"{n} concurrent processes, each 1/{CPU_SLICES} of the evaluation (the reference's own "
-              f"rank slicing of cells and stars), per step")
+              f"rank slicing of cells and stars), ranks {cpu_ranks(n)} of {CPU_SLICES} "
+              f"({n}/{CPU_SLICES} of the evaluation) per step")
     cpu = {"value": value, "unit": "evals/s", "cores": n, "kind": kind, "sample": sample}
     out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -255,7 +302,7 @@ def run_gb300_arm(args, ws, rank, local):
     N.lib(build_if_missing=True)
     device = local
     torch.cuda.set_device(device)
-    files = syn.materialise(CONFIG_INDEX, os.path.join(args.data_dir, f"rank{rank}"))["files"]
+    files, golden = workload_files(args.workload, os.path.join(args.data_dir, f"rank{rank}"))
     f = files[0]
     theta = f["theta"]
     S = len(f["problem"].streams)
@@ -401,6 +448,18 @@ def run_gb300_arm(args, ws, rank, local):
                        "ex2_gops": peaks.ex2_gops, "rsqrt_gops": peaks.rsqrt_gops, "rcp_gops": peaks.rcp_gops},
         "wall_s_timed": wall,
     }
+    if golden is not None:
+        # each form against the reference CPU evaluator's own result on these inputs
+        def err(r):
+            return {"dlogL": r.likelihood - golden["likelihood"],
+                    "max_integral_rel_err": max(abs(a - b) / abs(b) if b else 0.0 for g_area, w_area in
+                                                zip(r.area_integrals, golden["area_integrals"])
+                                                for a, b in zip(g_area, w_area))}
+        out["accuracy_vs_reference"] = {
+            "golden": f"the reference CPU evaluator's own result on these inputs (tests/golden, config "
+                      f"{args.workload})",
+            "mixed_f32": err(r32), "plain_f64": err(r64), "double_float": err(rdf)}
+        out["dlogL_mixed_vs_oracle"] = r32.likelihood - golden["likelihood"]
     if clk:
         out["clocks"] = clk
     if rank == 0 and not args.no_extras:
@@ -416,7 +475,9 @@ def run_gb300_arm(args, ws, rank, local):
         cv = (n / CPU_SLICES) / cw
         out["cpu_baseline"] = {"value": cv, "unit": "evals/s", "cores": n, "kind": kind,
                                "sample": f"{n} concurrent 1/{CPU_SLICES} slices of the evaluation "
-                                         f"(reference rank slicing of cells and stars), {cw:.1f} s wall"}
+                                         f"(reference rank slicing of cells and stars), ranks "
+                                         f"{cpu_ranks(n)} of {CPU_SLICES} spread over the index, "
+                                         f"{cw:.1f} s wall"}
     if ctx is not None:
         ctx.close()
     if rank == 0:

@@ -36,6 +36,7 @@
 #include <mutex>
 
 #include "milkyway_separation_gb300.h"
+#include "milkyway_separation_gb300_test.h"
 #include "mwsep_checks.cuh"
 #include "mwsep_df.cuh"
 #include "mwsep_f64_point.cuh"

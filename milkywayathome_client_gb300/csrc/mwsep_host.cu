@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "milkyway_separation_gb300.h"
+#include "milkyway_separation_gb300_test.h"
 #include "mwsep_ctx.h"
 #include "mwsep_geometry.cuh"
 #include "mwsep_internal.h"

@@ -11,12 +11,27 @@ import pytest
 from conftest import REPO
 
 HEADER = os.path.join(REPO, "include", "milkyway_separation_gb300.h")
+TEST_HEADER = os.path.join(REPO, "include", "milkyway_separation_gb300_test.h")
+
+
+def _functions_in(path):
+    text = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+    return set(re.findall(r"\b(mwsep_\w+)\s*\(", text))
 
 
 def _declared_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mwsep_\w+)\s*\(", text)))
+    """Every function the library's headers declare: the product ABI and the
+    test/diagnostic entry points."""
+    return sorted(_functions_in(HEADER) | _functions_in(TEST_HEADER))
+
+
+def test_public_header_holds_no_test_entry_points():
+    """The product header declares the evaluator ABI only; the debug-build
+    checks, primitive probes and launch-model diagnostics live in the test
+    header."""
+    test_only = _functions_in(TEST_HEADER)
+    assert test_only == {"mwsep_device_checks", "mwsep_df_eval", "mwsep_model_tile_cost", "mwsep_model_kchunk"}
+    assert not (test_only & _functions_in(HEADER))
 
 
 def test_library_exports_every_declared_function(built_library):
@@ -34,7 +49,7 @@ def test_python_binding_covers_header(built_library):
 
 def _prototype_arg_counts():
     """name -> number of parameters, from the header's prototypes."""
-    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read() + open(TEST_HEADER).read(), flags=re.S)
     out = {}
     for m in re.finditer(r"\b(mwsep_\w+)\s*\(([^;{]*?)\)\s*;", text):
         args = m.group(2).strip()
