@@ -598,21 +598,46 @@ def mixed_size_batch(args):
                                                    for a, b in zip(out["double_float"], out["plain_f64"]))}
 
 
+SERVE_RATES = [50.0, 200.0, 300.0, 400.0, 800.0, 1400.0, 2000.0]
+
+
 def serving(args):
-    """Poisson arrivals over the 6 mixed-size wedges: compensated FP32 at 50,
-    200 and 800 requests/s; the plain FP64 form at 1 request/s and the
-    double-float form at 10 requests/s (their throughputs on these wedges
-    are ~2 and ~33 evaluations/s)."""
+    """Poisson arrivals over the 6 mixed-size wedges (all resident; an arrival
+    picks a wedge with probability proportional to its stars), requests
+    admitted against a 160 GB device-memory budget: the compensated form at
+    50 to 2000 requests/s (4 lanes, batches capped at 10 ms of predicted
+    device time, at most 256 requests waiting), the plain FP64 form at 1 and
+    2 requests/s and the double-float form at 10, 20 and 30 requests/s
+    (their throughputs on these wedges are ~3 and ~37 evaluations/s).  The
+    knee is the highest rate served with p99 below 100 ms and nothing
+    refused."""
+    import milkywayathome_client_gb300 as mw
     from milkywayathome_client_gb300 import native as N
     from milkywayathome_client_gb300 import serve_bench
+    from milkywayathome_client_gb300 import synthetic as syn
     d = os.path.join(args.data_dir, "serving")
-    res = serve_bench.run([50.0, 200.0, 800.0], 2.0, N.MWSEP_MIXED_F32, 2, 256, d)
-    plain = serve_bench.run([1.0], 4.0, N.MWSEP_PLAIN_F64, 2, 256, d, autotune=False)
-    dfl = serve_bench.run([10.0], 3.0, N.MWSEP_PLAIN_DF, 2, 256, d, autotune=False)
-    return {"workload": "Poisson arrivals over 6 resident wedges (log-uniform sizes), wedge chosen by star count",
-            "lanes": 2, "precision": "mixed", "results": res,
-            "plain_f64": {"precision": "plain FP64", "results": plain},
-            "double_float": {"precision": "double-float", "results": dfl}}
+    m = syn.materialise(3, d)
+    out = {"workload": "Poisson arrivals over 6 resident wedges (log-uniform sizes), wedge chosen by star count",
+           "hbm_budget_bytes": serve_bench.HBM_BUDGET_BYTES}
+    with mw.Context(0) as ctx:
+        wedges = []
+        for f in m["files"]:
+            wid = ctx.add_wedge(mw.AstronomyParameters.read(f["params"]), mw.StarPoints.read(f["stars"]))
+            wedges.append((wid, f["theta"], f["n_stars"]))
+        for wid, _, _ in wedges:
+            ctx.autotune(wid, N.MWSEP_MIXED_F32)
+        out["resident_bytes"] = sum(ctx.wedge_bytes(w[0]) for w in wedges)
+        arms = (("mixed", N.MWSEP_MIXED_F32, SERVE_RATES, 2.0, 4, 10.0, 256),
+                ("plain_f64", N.MWSEP_PLAIN_F64, [1.0, 2.0], 4.0, 2, 0.0, 64),
+                ("double_float", N.MWSEP_PLAIN_DF, [10.0, 20.0, 30.0], 3.0, 4, 100.0, 256))
+        for name, prec, rates, secs, lanes, cap_ms, max_q in arms:
+            res = serve_bench.run(rates, secs, prec, lanes, 256, d, ctx=ctx, wedges=wedges,
+                                  target_batch_ms=cap_ms, max_queued=max_q)
+            ok = [r["rate_req_s"] for r in res if r["p99_latency_s"] <= 0.1 and r["refused"] == 0]
+            out[name] = {"lanes": lanes, "target_batch_ms": cap_ms, "max_queued": max_q, "seconds_per_rate": secs,
+                         "results": res, "knee_req_s": max(ok) if ok else None,
+                         "peak_evals_per_s": max(r["evals_per_s"] for r in res)}
+    return out
 
 
 def main():

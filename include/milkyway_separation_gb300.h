@@ -153,7 +153,8 @@ enum
     MWSEP_ERR_BUDGET = 7,     /* request exceeds the context HBM budget    */
     MWSEP_ERR_TIMEOUT = 8,    /* a bounded wait ran out                    */
     MWSEP_ERR_CANCELLED = 9,  /* serving request cancelled before launch   */
-    MWSEP_ERR_STATE = 10      /* call out of order (no problem / no stars) */
+    MWSEP_ERR_STATE = 10,     /* call out of order (no problem / no stars) */
+    MWSEP_ERR_BUSY = 11       /* serving: the admission queue is full      */
 };
 
 #define MWSEP_MAX_STREAMS 8
@@ -366,6 +367,10 @@ int mwsep_ctx_add_wedge(mwsep_ctx* ctx, const ASTRONOMY_PARAMETERS* ap, const ST
 int mwsep_ctx_wedge_theta_count(const mwsep_ctx* ctx, int wedge_id);
 /* Device bytes a resident wedge holds (tables + catalogue). */
 int mwsep_ctx_wedge_bytes(const mwsep_ctx* ctx, int wedge_id, size_t* out);
+/* Density points one evaluation of a resident wedge computes: cells x
+ * convolve over the cells its areas integrate, plus stars x convolve (the
+ * work unit of the throughput figures; a scheduler's cost estimate). */
+int mwsep_ctx_wedge_points(const mwsep_ctx* ctx, int wedge_id, double* out);
 /* Cap the context's device memory (0 = no cap). */
 int mwsep_ctx_set_hbm_budget(mwsep_ctx* ctx, size_t bytes);
 
@@ -404,6 +409,11 @@ typedef struct
     int max_batch;         /* requests per engine batch; default 256 */
     size_t lane_hbm_bytes; /* device-memory share of each lane's batch buffers (0 = no cap);
                               a batch that would exceed it is split until it fits */
+    double target_batch_ms; /* a lane stops adding requests to a batch once their predicted
+                               device time passes this (0 = no time cap); predictions are
+                               points per evaluation x the time per point the lanes measure */
+    long long max_queued;   /* admission: submit refuses with MWSEP_ERR_BUSY while this many
+                               requests wait (0 = unbounded) */
 } mwsep_server_config;
 
 typedef struct
@@ -412,6 +422,8 @@ typedef struct
     double mean_batch;
     double p50_latency_s, p99_latency_s, max_latency_s; /* submit -> result */
     double evals_per_s;                                 /* completed / (last result - first submit) */
+    long long refused;                                  /* submits refused by admission (MWSEP_ERR_BUSY) */
+    long long max_queue;                                /* most requests waiting at once */
 } mwsep_server_stats;
 
 /* Start serving the wedges resident in ctx (add them first; the server

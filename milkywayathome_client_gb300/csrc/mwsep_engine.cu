@@ -520,6 +520,18 @@ extern "C" int mwsep_ctx_wedge_bytes(const mwsep_ctx* c, int id, size_t* out)
     return MWSEP_OK;
 }
 
+extern "C" int mwsep_ctx_wedge_points(const mwsep_ctx* c, int id, double* out)
+{
+    if (!c || !out || id < 0 || id >= (int)c->wedges.size()) return mwsep_fail(MWSEP_ERR_ARG);
+    const Wedge& w = *c->wedges[id];
+    if (!w.has_problem) return mwsep_fail(MWSEP_ERR_STATE);
+    double cells = 0.0;
+    for (int a = 0; a < w.prob.n_areas; ++a)
+        cells += (double)(w.prob.area[a].cell_end - w.prob.area[a].cell_begin);
+    *out = (cells + (w.has_stars ? (double)w.n_stars : 0.0)) * (double)w.prob.convolve;
+    return MWSEP_OK;
+}
+
 extern "C" int mwsep_ctx_evaluate_requests(mwsep_ctx* c, int n, const mwsep_request* reqs, int precision,
                                            mwsep_result* out)
 {

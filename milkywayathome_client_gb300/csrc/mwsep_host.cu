@@ -91,6 +91,7 @@ extern "C" const char* mwsep_status_string(int s)
     case MWSEP_ERR_TIMEOUT: return "bounded wait ran out";
     case MWSEP_ERR_CANCELLED: return "request cancelled";
     case MWSEP_ERR_STATE: return "call out of order";
+    case MWSEP_ERR_BUSY: return "admission refused: the serving queue is full";
     default: return "unknown status";
     }
 }

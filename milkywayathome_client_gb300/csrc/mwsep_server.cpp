@@ -4,12 +4,18 @@
  * The server owns `lanes` execution lanes.  A lane is a context sharing the
  * parent's resident wedges (no copy of the tables) with its own CUDA stream,
  * engine buffers and captured graph, driven by one dispatcher thread.  A
- * dispatcher that is free takes every queued request of the oldest
- * request's precision (up to max_batch) and evaluates them as one engine
- * batch; requests that arrive meanwhile wait for the next free lane, so
- * batches on different lanes overlap on the GPU.  A batch that would push
- * the lane past its share of the device-memory budget is split in half until
- * it fits (admission by HBM footprint).
+ * dispatcher that is free takes the queued requests of the oldest request's
+ * precision in arrival order (up to max_batch, and -- with target_batch_ms
+ * set -- until their predicted device time reaches it) and evaluates them as
+ * one engine batch; requests that arrive meanwhile go to the next lane that
+ * frees up, so batches on different lanes overlap on the GPU.  The
+ * prediction is a request's density points (mwsep_ctx_wedge_points) times
+ * the time per point of its precision, which the lanes measure on every
+ * batch they run (a moving average, contention from the other lanes
+ * included).  A batch that would push the lane past its share of the
+ * device-memory budget is split in half until it fits (admission by HBM
+ * footprint), and with max_queued set a submit finding that many requests
+ * waiting is refused with MWSEP_ERR_BUSY.
  *
  * A request's result is the same whichever lane or batch runs it: the
  * reduction order of an evaluation depends only on its wedge's tile shape.
@@ -47,6 +53,7 @@ struct Request
     int precision;
     std::vector<double> theta;
     Clock::time_point submitted;
+    double points = 0.0; /* density points of one evaluation of its wedge */
     bool done = false;
     bool started = false;
     int status = MWSEP_OK;
@@ -70,9 +77,14 @@ struct mwsep_server
     uint64_t next_id = 1;
     bool stop = false;
 
+    /* device time per density point of each precision (plain FP64,
+     * compensated, double-float), seeded with GB300 rates and refreshed from
+     * every batch */
+    double ns_per_point[3] = {120.0, 0.9, 9.6};
+
     /* statistics */
     std::vector<double> latencies;
-    long long batches = 0, evaluated = 0, cancelled = 0, failed = 0;
+    long long batches = 0, evaluated = 0, cancelled = 0, failed = 0, refused = 0, max_queue = 0;
     Clock::time_point first_submit, last_done;
     bool any = false;
 };
@@ -93,10 +105,15 @@ void lane_loop(mwsep_server* s, int lane)
             s->cv_work.wait(lock, [&] { return s->stop || !s->queue.empty(); });
             if (s->stop && s->queue.empty()) return;
             const int precision = s->queue.front()->precision;
+            const double cap_ms = s->cfg.target_batch_ms;
+            double predicted_ms = 0.0;
             for (auto it = s->queue.begin(); it != s->queue.end() && (int)batch.size() < s->cfg.max_batch;)
             {
                 if ((*it)->precision == precision)
                 {
+                    const double ms = (*it)->points * s->ns_per_point[precision] * 1e-6;
+                    if (cap_ms > 0.0 && !batch.empty() && predicted_ms + ms > cap_ms) break;
+                    predicted_ms += ms;
                     (*it)->started = true;
                     batch.push_back(*it);
                     it = s->queue.erase(it);
@@ -106,6 +123,9 @@ void lane_loop(mwsep_server* s, int lane)
             }
         }
         /* evaluate; split in halves while the lane's memory share refuses it */
+        const auto t_batch = Clock::now();
+        double batch_points = 0.0;
+        for (const Request* r : batch) batch_points += r->points;
         size_t done = 0;
         while (done < batch.size())
         {
@@ -147,6 +167,12 @@ void lane_loop(mwsep_server* s, int lane)
             }
             ++s->batches;
             s->last_done = now;
+            if (done + take == batch.size() && rc == MWSEP_OK && batch_points > 0.0)
+            {
+                const int p = batch.front()->precision;
+                const double ns = std::chrono::duration<double>(now - t_batch).count() * 1e9 / batch_points;
+                s->ns_per_point[p] = 0.7 * s->ns_per_point[p] + 0.3 * ns;
+            }
             s->cv_done.notify_all();
             done += take;
         }
@@ -175,8 +201,11 @@ extern "C" int mwsep_server_create(mwsep_ctx* ctx, const mwsep_server_config* cf
     s->cfg.lanes = 2;
     s->cfg.max_batch = 256;
     s->cfg.lane_hbm_bytes = 0;
+    s->cfg.target_batch_ms = 0.0;
+    s->cfg.max_queued = 0;
     if (cfg) s->cfg = *cfg;
-    if (s->cfg.lanes < 1 || s->cfg.lanes > 16 || s->cfg.max_batch < 1)
+    if (s->cfg.lanes < 1 || s->cfg.lanes > 16 || s->cfg.max_batch < 1 || !(s->cfg.target_batch_ms >= 0.0) ||
+        s->cfg.max_queued < 0)
     {
         delete s;
         return mwsep_fail(MWSEP_ERR_ARG);
@@ -206,9 +235,12 @@ extern "C" int mwsep_server_submit(mwsep_server* s, int wedge, const double* the
         return mwsep_fail(MWSEP_ERR_ARG);
     const int n = mwsep_ctx_wedge_theta_count(s->parent, wedge);
     if (n < 0) return mwsep_fail(MWSEP_ERR_ARG);
+    double points = 0.0;
+    if (mwsep_ctx_wedge_points(s->parent, wedge, &points) != MWSEP_OK) return mwsep_fail(MWSEP_ERR_ARG);
     Request* r = new (std::nothrow) Request();
     if (!r) return mwsep_fail(MWSEP_ERR_NOMEM);
     r->wedge = wedge;
+    r->points = points;
     r->precision = precision;
     r->theta.assign(theta, theta + n);
     r->submitted = Clock::now();
@@ -219,6 +251,12 @@ extern "C" int mwsep_server_submit(mwsep_server* s, int wedge, const double* the
             delete r;
             return mwsep_fail(MWSEP_ERR_STATE);
         }
+        if (s->cfg.max_queued > 0 && (long long)s->queue.size() >= s->cfg.max_queued)
+        {
+            ++s->refused;
+            delete r;
+            return mwsep_fail(MWSEP_ERR_BUSY);
+        }
         r->id = s->next_id++;
         if (!s->any)
         {
@@ -226,6 +264,7 @@ extern "C" int mwsep_server_submit(mwsep_server* s, int wedge, const double* the
             s->any = true;
         }
         s->queue.push_back(r);
+        s->max_queue = std::max(s->max_queue, (long long)s->queue.size());
         s->all[r->id] = r;
         *id = r->id;
     }
@@ -282,6 +321,8 @@ extern "C" int mwsep_server_get_stats(mwsep_server* s, mwsep_server_stats* out)
     out->max_latency_s = s->latencies.empty() ? 0.0 : *std::max_element(s->latencies.begin(), s->latencies.end());
     const double span = s->any ? std::chrono::duration<double>(s->last_done - s->first_submit).count() : 0.0;
     out->evals_per_s = span > 0 ? (double)s->evaluated / span : 0.0;
+    out->refused = s->refused;
+    out->max_queue = s->max_queue;
     return MWSEP_OK;
 }
 
@@ -290,7 +331,8 @@ extern "C" int mwsep_server_reset_stats(mwsep_server* s)
     if (!s) return mwsep_fail(MWSEP_ERR_ARG);
     std::lock_guard<std::mutex> lock(s->mu);
     s->latencies.clear();
-    s->batches = s->evaluated = s->cancelled = s->failed = 0;
+    s->batches = s->evaluated = s->cancelled = s->failed = s->refused = 0;
+    s->max_queue = (long long)s->queue.size();
     s->any = false;
     return MWSEP_OK;
 }

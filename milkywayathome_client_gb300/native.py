@@ -27,6 +27,7 @@ MWSEP_ERR_BUDGET = 7
 MWSEP_ERR_TIMEOUT = 8
 MWSEP_ERR_CANCELLED = 9
 MWSEP_ERR_STATE = 10
+MWSEP_ERR_BUSY = 11
 
 MWSEP_MAX_STREAMS = 8
 MWSEP_MAX_AREAS = 8
@@ -148,14 +149,15 @@ MWSEP_NOALLOC_SCRATCH_BYTES = 256 * 1024
 
 
 class mwsep_server_config(C.Structure):
-    _fields_ = [("lanes", C.c_int), ("max_batch", C.c_int), ("lane_hbm_bytes", C.c_size_t)]
+    _fields_ = [("lanes", C.c_int), ("max_batch", C.c_int), ("lane_hbm_bytes", C.c_size_t),
+                ("target_batch_ms", C.c_double), ("max_queued", C.c_longlong)]
 
 
 class mwsep_server_stats(C.Structure):
     _fields_ = [("completed", C.c_longlong), ("failed", C.c_longlong), ("cancelled", C.c_longlong),
                 ("batches", C.c_longlong), ("queued", C.c_longlong), ("mean_batch", C.c_double),
                 ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double),
-                ("evals_per_s", C.c_double)]
+                ("evals_per_s", C.c_double), ("refused", C.c_longlong), ("max_queue", C.c_longlong)]
 
 
 class mwsep_request(C.Structure):
@@ -243,6 +245,7 @@ _SIGS = {
     "mwsep_ctx_add_wedge": (C.c_int, [C.c_void_p, _P(ASTRONOMY_PARAMETERS), _P(STAR_POINTS), _P(C.c_int)]),
     "mwsep_ctx_wedge_theta_count": (C.c_int, [C.c_void_p, C.c_int]),
     "mwsep_ctx_wedge_bytes": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_size_t)]),
+    "mwsep_ctx_wedge_points": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double)]),
     "mwsep_ctx_set_hbm_budget": (C.c_int, [C.c_void_p, C.c_size_t]),
     "mwsep_ctx_evaluate_requests": (C.c_int, [C.c_void_p, C.c_int, _P(mwsep_request), C.c_int,
                                               _P(mwsep_result)]),

@@ -416,6 +416,12 @@ class Context:
     def wedge_theta_count(self, wedge: int) -> int:
         return N.lib().mwsep_ctx_wedge_theta_count(self._h, wedge)
 
+    def wedge_points(self, wedge: int) -> float:
+        """Density points one evaluation of the wedge computes."""
+        v = C.c_double()
+        N.check(N.lib().mwsep_ctx_wedge_points(self._h, wedge, C.byref(v)))
+        return v.value
+
     def wedge_bytes(self, wedge: int) -> int:
         v = C.c_size_t()
         N.check(N.lib().mwsep_ctx_wedge_bytes(self._h, wedge, C.byref(v)))
@@ -590,8 +596,9 @@ class Server:
     """Continuous-batching server over a context's resident wedges
     (mwsep_server_*).  Add the wedges to the context first."""
 
-    def __init__(self, ctx: Context, lanes: int = 2, max_batch: int = 256, lane_hbm_bytes: int = 0):
-        cfg = N.mwsep_server_config(lanes, max_batch, lane_hbm_bytes)
+    def __init__(self, ctx: Context, lanes: int = 2, max_batch: int = 256, lane_hbm_bytes: int = 0,
+                 target_batch_ms: float = 0.0, max_queued: int = 0):
+        cfg = N.mwsep_server_config(lanes, max_batch, lane_hbm_bytes, target_batch_ms, max_queued)
         self._h = C.c_void_p()
         self._ctx = ctx
         N.check(N.lib().mwsep_server_create(ctx._h, C.byref(cfg), C.byref(self._h)), "server_create")

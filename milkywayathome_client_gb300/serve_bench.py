@@ -24,8 +24,15 @@ from . import synthetic as syn
 from .separation import AstronomyParameters, Context, Server, StarPoints
 
 
+HBM_BUDGET_BYTES = 160 * 10 ** 9  # the device-memory budget requests are admitted against
+
+
 def run(rates, seconds, precision, lanes, max_batch, data_dir, autotune=True, star_scale=1.0, seed=0,
-        ctx=None, wedges=None):
+        ctx=None, wedges=None, target_batch_ms=0.0, max_queued=0, hbm_budget=HBM_BUDGET_BYTES):
+    """Feed a server Poisson arrivals at each rate for `seconds`, drain, and
+    report latency, throughput and admission.  The wedges' resident bytes
+    come out of hbm_budget first; the rest is split evenly over the lanes'
+    batch buffers (0: no budget)."""
     own = ctx is None
     if own:
         ctx = Context(0)
@@ -40,7 +47,12 @@ def run(rates, seconds, precision, lanes, max_batch, data_dir, autotune=True, st
     stars = np.array([w[2] for w in wedges], float)
     p = stars / stars.sum()
     out = []
-    with Server(ctx, lanes=lanes, max_batch=max_batch) as srv:
+    lane_bytes = 0
+    if hbm_budget:
+        resident = sum(ctx.wedge_bytes(w[0]) for w in wedges)
+        lane_bytes = max(1, (hbm_budget - resident) // lanes)
+    with Server(ctx, lanes=lanes, max_batch=max_batch, lane_hbm_bytes=lane_bytes, target_batch_ms=target_batch_ms,
+                max_queued=max_queued) as srv:
         # warm-up: one request per wedge (captures the lanes' graphs)
         for wid, th, _ in wedges:
             srv.wait(srv.submit(wid, th, precision), 600)
@@ -60,13 +72,18 @@ def run(rates, seconds, precision, lanes, max_batch, data_dir, autotune=True, st
                 k = rng.choice(len(wedges), p=p)
                 wid, th, _ = wedges[k]
                 theta = np.asarray(th) * (1.0 + 0.001 * rng.standard_normal(len(th)))
-                ids.append(srv.submit(wid, theta, precision))
+                try:
+                    ids.append(srv.submit(wid, theta, precision))
+                except N.MwsepError as e:
+                    if e.status != N.MWSEP_ERR_BUSY:
+                        raise
             for i in ids:
                 srv.wait(i, 3600)
             st = srv.stats()
-            out.append({"rate_req_s": rate, "requests": len(ids), "p50_latency_s": st["p50_latency_s"],
+            out.append({"rate_req_s": rate, "arrivals": len(ids) + st["refused"], "accepted": len(ids),
+                        "refused": st["refused"], "p50_latency_s": st["p50_latency_s"],
                         "p99_latency_s": st["p99_latency_s"], "evals_per_s": st["evals_per_s"],
-                        "mean_batch": st["mean_batch"], "batches": st["batches"]})
+                        "mean_batch": st["mean_batch"], "batches": st["batches"], "max_queue": st["max_queue"]})
     if own:
         ctx.close()
     return out
@@ -80,11 +97,14 @@ def main():
     ap.add_argument("--lanes", type=int, default=2)
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--star-scale", type=float, default=1.0)
+    ap.add_argument("--target-batch-ms", type=float, default=0.0)
+    ap.add_argument("--max-queued", type=int, default=0)
     ap.add_argument("--data-dir", default=os.path.join(tempfile.gettempdir(), "mwsep_serve_data"))
     a = ap.parse_args()
     prec = {"mixed": N.MWSEP_MIXED_F32, "plain": N.MWSEP_PLAIN_F64, "df": N.MWSEP_PLAIN_DF}[a.precision]
     rates = [float(x) for x in a.rates.split(",")]
-    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale)
+    res = run(rates, a.seconds, prec, a.lanes, a.max_batch, a.data_dir, star_scale=a.star_scale,
+              target_batch_ms=a.target_batch_ms, max_queued=a.max_queued)
     print(json.dumps({"precision": a.precision, "lanes": a.lanes, "results": res}))
 
 

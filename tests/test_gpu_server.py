@@ -141,3 +141,45 @@ def test_destroy_with_queued_requests_returns(served):
     # the context still evaluates afterwards
     r = ctx.evaluate_requests([(w, base)], mw.MWSEP_PLAIN_F64)[0]
     assert r.likelihood == r.likelihood
+
+
+def test_admission_queue_bound_refuses_with_busy(served):
+    """With max_queued set, a submit that finds that many requests waiting is
+    refused at once with MWSEP_ERR_BUSY; accepted requests complete with the
+    same bits as alone and the stats count the refusals."""
+    import milkywayathome_client_gb300 as mw
+    from milkywayathome_client_gb300 import native as N
+    ctx, wedges = served
+    w, base = wedges[2]  # config 0 in plain FP64: ~1.5 ms per evaluation
+    want = ctx.evaluate_requests([(w, base)], mw.MWSEP_PLAIN_F64)[0]
+    with mw.Server(ctx, lanes=1, max_batch=1, max_queued=4) as srv:
+        ids, busy = [], 0
+        for _ in range(60):
+            try:
+                ids.append(srv.submit(w, base, mw.MWSEP_PLAIN_F64))
+            except mw.MwsepError as e:
+                assert e.status == N.MWSEP_ERR_BUSY
+                busy += 1
+        for i in ids:
+            assert srv.wait(i, 300).likelihood == want.likelihood
+        st = srv.stats()
+    assert busy > 0 and st["refused"] == busy
+    assert st["completed"] == len(ids) and st["max_queue"] <= 4
+
+
+def test_time_capped_batches(served):
+    """target_batch_ms caps a lane's batch by predicted device time: with a
+    cap far below one evaluation every batch holds one request, and results
+    still equal the requests evaluated alone."""
+    import milkywayathome_client_gb300 as mw
+    ctx, wedges = served
+    work = _workload(wedges, 24, 5)
+    alone = [ctx.evaluate_requests([(w, t)], p)[0] for w, t, p in work]
+    assert all(ctx.wedge_points(w) > 0 for w, _ in wedges)
+    with mw.Server(ctx, lanes=1, max_batch=64, target_batch_ms=1e-6) as srv:
+        ids = [srv.submit(w, t, p) for w, t, p in work]
+        got = [srv.wait(i, timeout=300) for i in ids]
+        st = srv.stats()
+    assert st["batches"] == len(work)
+    for a, b in zip(alone, got):
+        assert a.integrals == b.integrals
