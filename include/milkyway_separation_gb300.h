@@ -290,6 +290,26 @@ double mwsep_evaluate_mixed(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUA
  * coverage are evaluated as mwsep_evaluate does. */
 double mwsep_evaluate_df(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es, STAR_POINTS* sp);
 
+/* The two per-rank steps of the reference's distributed evaluation, which
+ * its MPI worker registers (cpu/mpi_astronomy.c:79-80), same signatures,
+ * plain FP64.  mwsep_integral_f replaces integral_f
+ * (cpu/astronomy_worker.c:33-64): applies parameters to *ap, integrates this
+ * rank's cells of every area (es->integral[i]'s [min_calculation,
+ * max_calculation), after split_astronomy_parameters and initialize_state)
+ * and writes the cut-subtracted background and stream integrals to
+ * results[0..S] and into es.  The ranks' results summed
+ * (integral_compose, :67-92) are the whole evaluation's integrals.
+ * mwsep_likelihood_f replaces likelihood_f (:94-121): calculate_likelihood of
+ * this rank's stars (after split_star_points) at *ap's current parameters
+ * against the given integrals[0..S]; results[0] = prob_sum, results[1] =
+ * bad_jacobians (always 0).  likelihood_compose (:123-143) of every rank's
+ * results is the whole evaluation's log-likelihood.  On failure the results
+ * hold NaN and mwsep_last_error() says why. */
+void mwsep_integral_f(double* parameters, double* results, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                      STAR_POINTS* sp);
+void mwsep_likelihood_f(double* integrals, double* results, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                        STAR_POINTS* sp);
+
 /* ------------------------------------------------------------------ */
 /* Context API: resident wedges and catalogues, batches                 */
 /* ------------------------------------------------------------------ */
@@ -338,6 +358,20 @@ int mwsep_ctx_theta_count(const mwsep_ctx* ctx);
 
 /* One evaluation of theta (mwsep_ctx_theta_count doubles) in `precision`. */
 int mwsep_ctx_evaluate(mwsep_ctx* ctx, const double* theta, int precision, mwsep_result* out);
+
+/* The two phases of one evaluation of wedge 0 separately, for an evaluation
+ * sharded over ranks as the reference's distributed client does it
+ * (integral_f / likelihood_f, cpu/astronomy_worker.c:33-121).
+ * mwsep_ctx_integrals integrates the resident problem's cells (each area's
+ * [min_calculation, max_calculation)) and needs no catalogue; out's
+ * likelihood fields are NaN.  mwsep_ctx_likelihood evaluates the resident
+ * catalogue against given cut-subtracted integrals (1 + S doubles:
+ * background, then streams -- e.g. the sum of every rank's); out carries the
+ * given integrals and zero area integrals.  Each gives the bits of the same
+ * phase of mwsep_ctx_evaluate. */
+int mwsep_ctx_integrals(mwsep_ctx* ctx, const double* theta, int precision, mwsep_result* out);
+int mwsep_ctx_likelihood(mwsep_ctx* ctx, const double* theta, const double* integrals, int precision,
+                         mwsep_result* out);
 
 /* A population: n_theta vectors, row-major [n_theta][theta_count], evaluated
  * together (one batched launch per phase).  out[n_theta].  Each result is

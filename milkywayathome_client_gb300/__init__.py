@@ -7,10 +7,11 @@ interface.
 """
 from .native import (MWSEP_MIXED_F32, MWSEP_PLAIN_DF, MWSEP_PLAIN_F64, MwsepError)  # noqa: F401
 from .separation import (AstronomyParameters, Context, EvaluationState, Result,  # noqa: F401
-                         Server, StarPoints, evaluate, evaluate_df, evaluate_mixed, stripe_transform,
+                         Server, StarPoints, evaluate, evaluate_df, evaluate_mixed, integral_f, likelihood_f,
+                         stripe_transform,
                          write_separation, invert_matrix, errors_from_hessian, write_errors,
                          StarCatalogue)
 
 __all__ = ["AstronomyParameters", "StarPoints", "EvaluationState", "Context", "Result", "Server",
-           "evaluate", "evaluate_df", "evaluate_mixed", "stripe_transform", "write_separation", "invert_matrix", "errors_from_hessian", "write_errors",
+           "evaluate", "evaluate_df", "evaluate_mixed", "integral_f", "likelihood_f", "stripe_transform", "write_separation", "invert_matrix", "errors_from_hessian", "write_errors",
            "StarCatalogue", "MWSEP_PLAIN_F64", "MWSEP_MIXED_F32", "MWSEP_PLAIN_DF", "MwsepError"]

@@ -239,8 +239,21 @@ void default_tune(mwsep_ctx* c, Wedge& w);
 /* One evaluation (or a batch) of wedge 0 through the grid-stride kernels;
  * leaves the integrals in c->d_out after the area block. */
 int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwsep_result* out);
+/* Which phases of an evaluation run: both (the default), the integrals
+ * alone (no catalogue needed; the likelihood fields come back NaN), or the
+ * likelihood alone against given cut-subtracted integrals ([B][1 + S],
+ * host), the two steps of the reference's distributed evaluation
+ * (integral_f / likelihood_f, cpu/astronomy_worker.c:33-121). */
+struct Phases
+{
+    bool integrals = true;
+    bool likelihood = true;
+    const double* given_integrals = nullptr;
+};
+
 /* The same for any resident wedge (wedge 0 is the one set_problem fills). */
-int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out);
+int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out,
+                   const Phases& ph = Phases());
 
 } // namespace mwsep
 

@@ -952,11 +952,14 @@ int evaluate_impl(mwsep_ctx* c, int B, const double* thetas, int precision, mwse
     return evaluate_wedge(c, 0, B, thetas, precision, out);
 }
 
-int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out)
+int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int precision, mwsep_result* out,
+                   const Phases& ph)
 {
     mwsep::Range nvtx_range("mwsep.evaluate");
-    if (wid < 0 || wid >= (int)c->wedges.size() || !c->wedges[wid]->has_problem || !c->wedges[wid]->has_stars)
+    if (wid < 0 || wid >= (int)c->wedges.size() || !c->wedges[wid]->has_problem ||
+        (ph.likelihood && !c->wedges[wid]->has_stars))
         return mwsep_fail(MWSEP_ERR_STATE);
+    if (!ph.integrals && (!ph.likelihood || !ph.given_integrals)) return mwsep_fail(MWSEP_ERR_ARG);
     Wedge& w = *c->wedges[wid];
     if (B < 1 || B > 65535 || !thetas || !out) return mwsep_fail(MWSEP_ERR_ARG);
     if (precision != MWSEP_PLAIN_F64 && precision != MWSEP_MIXED_F32 && precision != MWSEP_PLAIN_DF)
@@ -985,7 +988,7 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
             df_general = df_general || form == 2;
             df_none = df_none || form == 3;
         }
-    const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4;
+    const bool df_likelihood = precision == MWSEP_PLAIN_DF && S <= 4 && ph.likelihood;
     if (precision == MWSEP_PLAIN_DF && mwsep_df_prepare(c->device)) return mwsep_fail(MWSEP_ERR_CUDA);
     const Tune& t = w.tune[precision];
     /* the compensated warp tiles with a tile counter write one slot per tile
@@ -1022,7 +1025,8 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     rc |= c->h_out.ensure(out_doubles * 8);
     /* the compensated likelihood's densities need no integral: computed on
      * the side stream beside the integral kernel */
-    const bool split_lk = precision == MWSEP_MIXED_F32 && env_long("MWSEP_SPLIT_LIKELIHOOD", 1) != 0;
+    const bool split_lk =
+        precision == MWSEP_MIXED_F32 && ph.likelihood && env_long("MWSEP_SPLIT_LIKELIHOOD", 1) != 0;
     if (split_lk) rc |= c->d_dens.ensure((size_t)B * (1 + (S <= 4 ? S : 8)) * w.n_stars * sizeof(double), tot);
     if (dyn)
     {
@@ -1063,7 +1067,14 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     bool forms[4] = {false, false, false, false};
     for (int i = 0; i < B; ++i) forms[mwsep_bg_form(&hth[i])] = true;
     sh.bg_form = 0;
-    for (int a = 0; a < A; ++a)
+    if (!ph.integrals)
+    {
+        /* the likelihood alone: the given (composed) integrals stand in for
+         * the reduction's output; no area results */
+        CU(cudaMemsetAsync(d_areas, 0, sizeof(double) * (size_t)B * A * ncomp, st));
+        CU(h2d(c, d_ints, ph.given_integrals, sizeof(double) * (size_t)B * ncomp, st));
+    }
+    for (int a = 0; a < (ph.integrals ? A : 0); ++a)
     {
         mwsep_area_dev v = w.areas[a].view;
         set_chunking(v, t.k_chunk, t.warp_items);
@@ -1103,7 +1114,7 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
             }
         }
     }
-    if (dyn)
+    if (dyn && ph.integrals)
     {
         for (int b0 = 0; b0 < B; b0 += dyn_chunk)
         {
@@ -1162,8 +1173,11 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
     /* a catalogue uploaded on the side stream: its table build released
      * with the integral (after the parameter upload), so it fills SMs the
      * integral's blocks leave */
-    rc = launch_star_build(c, c->ev[1]);
-    if (rc) return rc;
+    if (ph.likelihood)
+    {
+        rc = launch_star_build(c, c->ev[1]);
+        if (rc) return rc;
+    }
     mwsep_launch_shape lk = sh;
     lk.block = t.lk_block;
     lk.grid = t.lk_grid;
@@ -1179,49 +1193,54 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         ++launches;
     }
     CU(cudaEventRecord(c->ev[2], st));
-    if (!dyn)
+    if (!dyn && ph.integrals)
     {
         CK(mwsep_launch_reduce_integrals(c->d_partials.as<double2>(), &sh, d_areas, d_ints, st));
         ++launches;
     }
     CU(cudaEventRecord(c->ev[3], st));
-    /* from here on the star tables are read */
-    rc = wait_stars(c, st);
-    if (rc) return rc;
-    if (df_likelihood && !w.has_star_df)
+    if (ph.likelihood)
     {
-        CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
-                                      w.s_ptsdf.as<float4>(), st));
-        w.has_star_df = true;
-    }
-    if (df_likelihood)
-    {
-        int n_forms = 0;
-        for (int form : {0, 2, 3})
+        /* from here on the star tables are read */
+        rc = wait_stars(c, st);
+        if (rc) return rc;
+        if (df_likelihood && !w.has_star_df)
         {
-            if (!(form == 0 ? df_hern : form == 2 ? df_general : df_none)) continue;
-            lk.bg_form = form;
-            CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
-                                          &lk, d_ints, c->d_lkpartials.as<double2>(), st));
-            if (n_forms++) ++launches; /* the first one is counted below */
+            CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,
+                                          w.s_ptsdf.as<float4>(), st));
+            w.has_star_df = true;
         }
-    }
-    else if (precision != MWSEP_MIXED_F32)
-        CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
-                                       c->d_lkpartials.as<double2>(), st));
-    else if (split_lk)
-    {
-        CU(cudaStreamWaitEvent(st, c->ev_dens, 0));
-        CK(mwsep_launch_likelihood_f32_finish(w.n_stars, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
-                                              c->d_dens.as<double>(), c->d_lkpartials.as<double2>(), st));
+        if (df_likelihood)
+        {
+            int n_forms = 0;
+            for (int form : {0, 2, 3})
+            {
+                if (!(form == 0 ? df_hern : form == 2 ? df_general : df_none)) continue;
+                lk.bg_form = form;
+                CK(mwsep_launch_likelihood_df(&w.stars_view, w.s_ptsdf.as<float4>(), c->d_theta.as<mwsep_theta_consts>(),
+                                              &lk, d_ints, c->d_lkpartials.as<double2>(), st));
+                if (n_forms++) ++launches; /* the first one is counted below */
+            }
+        }
+        else if (precision != MWSEP_MIXED_F32)
+            CK(mwsep_launch_likelihood_f64(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                           c->d_lkpartials.as<double2>(), st));
+        else if (split_lk)
+        {
+            CU(cudaStreamWaitEvent(st, c->ev_dens, 0));
+            CK(mwsep_launch_likelihood_f32_finish(w.n_stars, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                                  c->d_dens.as<double>(), c->d_lkpartials.as<double2>(), st));
+        }
+        else
+            CK(mwsep_launch_likelihood_f32(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
+                                           c->d_lkpartials.as<double2>(), st));
+        ++launches;
+        CU(cudaEventRecord(c->ev[4], st));
+        CK(mwsep_launch_reduce_likelihood(c->d_lkpartials.as<double2>(), &lk, d_lk, st));
+        ++launches;
     }
     else
-        CK(mwsep_launch_likelihood_f32(&w.stars_view, c->d_theta.as<mwsep_theta_consts>(), &lk, d_ints,
-                                       c->d_lkpartials.as<double2>(), st));
-    ++launches;
-    CU(cudaEventRecord(c->ev[4], st));
-    CK(mwsep_launch_reduce_likelihood(c->d_lkpartials.as<double2>(), &lk, d_lk, st));
-    ++launches;
+        CU(cudaEventRecord(c->ev[4], st));
     CU(d2h(c, c->h_out.p, c->d_out.p, out_doubles * 8));
     CU(cudaEventRecord(c->ev[5], st));
     CU(cudaStreamSynchronize(st));
@@ -1253,6 +1272,13 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
             for (int k = 0; k < ncomp; ++k) r.area_integrals[a][k] = h_areas[((size_t)i * A + a) * ncomp + k];
         r.background_integral = h_ints[(size_t)i * ncomp];
         for (int s = 0; s < S; ++s) r.stream_integrals[s] = h_ints[(size_t)i * ncomp + 1 + s];
+        r.status = MWSEP_OK;
+        if (!ph.likelihood)
+        {
+            r.prob_sum = r.likelihood = r.background_only_likelihood = NAN;
+            for (int s = 0; s < S; ++s) r.stream_only_likelihood[s] = NAN;
+            continue;
+        }
         const double* lkv = h_lk + (size_t)i * nslots;
         r.prob_sum = lkv[0];
         r.num_zero = (int)llround(lkv[1]);
@@ -1261,7 +1287,6 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         r.likelihood = lkv[0] / N - 3.0;
         r.background_only_likelihood = lkv[2] / N - 3.0;
         for (int s = 0; s < S; ++s) r.stream_only_likelihood[s] = lkv[3 + s] / N - 3.0;
-        r.status = MWSEP_OK;
     }
     return MWSEP_OK;
 }
@@ -1414,6 +1439,26 @@ extern "C" int mwsep_ctx_evaluate(mwsep_ctx* c, const double* theta, int precisi
     if (!c) return mwsep_fail(MWSEP_ERR_ARG);
     CU(cudaSetDevice(c->device));
     return evaluate_impl(c, 1, theta, precision, out);
+}
+
+extern "C" int mwsep_ctx_integrals(mwsep_ctx* c, const double* theta, int precision, mwsep_result* out)
+{
+    if (!c) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    Phases ph;
+    ph.likelihood = false;
+    return evaluate_wedge(c, 0, 1, theta, precision, out, ph);
+}
+
+extern "C" int mwsep_ctx_likelihood(mwsep_ctx* c, const double* theta, const double* integrals, int precision,
+                                    mwsep_result* out)
+{
+    if (!c || !integrals) return mwsep_fail(MWSEP_ERR_ARG);
+    CU(cudaSetDevice(c->device));
+    Phases ph;
+    ph.integrals = false;
+    ph.given_integrals = integrals;
+    return evaluate_wedge(c, 0, 1, theta, precision, out, ph);
 }
 
 extern "C" int mwsep_ctx_evaluate_batch(mwsep_ctx* c, int n_theta, const double* thetas, int precision,
@@ -1576,7 +1621,122 @@ double evalfunc_impl(double* parameters, ASTRONOMY_PARAMETERS* ap, EVALUATION_ST
     return es->prob_sum / (sp->number_stars - es->bad_jacobians);
 }
 
+/* The library's default context for the process-wide entries (created on
+ * first use; the caller holds g_default_mu). */
+mwsep_ctx* default_ctx()
+{
+    if (!g_default)
+    {
+        int dev = 0;
+        if (const char* e = getenv("MWSEP_DEVICE")) dev = atoi(e);
+        if (mwsep_ctx_create(dev, &g_default) != MWSEP_OK) return nullptr;
+    }
+    return g_default;
+}
+
+/* Writes NaN into the n results of a failed worker step. */
+void worker_fail(double* results, int n)
+{
+    if (results)
+        for (int i = 0; i < n; ++i) results[i] = NAN;
+}
+
 } // namespace
+
+/* integral_f (cpu/astronomy_worker.c:33-64): theta applied to *ap, this
+ * rank's cells of every area integrated (es->integral[i]'s
+ * [min_calculation, max_calculation), as calculate_integral walks them),
+ * the cut-subtracted background and stream integrals into results[0..S]
+ * and into es, as the reference leaves them. */
+extern "C" void mwsep_integral_f(double* parameters, double* results, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                                 STAR_POINTS* sp)
+{
+    (void)sp; /* the integrals read no catalogue */
+    const int S = ap ? ap->number_streams : 0;
+    if (!parameters || !results || !ap || !es || S < 0 || S > MWSEP_MAX_STREAMS)
+    {
+        mwsep_fail(MWSEP_ERR_ARG);
+        worker_fail(results, S >= 0 && S <= MWSEP_MAX_STREAMS ? 1 + S : 0);
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    mwsep_ctx* c = default_ctx();
+    if (!c || mwsep_set_astronomy_parameters(ap, parameters) != MWSEP_OK || mwsep_ctx_set_problem(c, ap) != MWSEP_OK)
+        return worker_fail(results, 1 + S);
+    if (es->number_integrals != ap->number_integrals || es->number_streams != S || !es->integral)
+    {
+        mwsep_fail(MWSEP_ERR_STATE);
+        return worker_fail(results, 1 + S);
+    }
+    long mn[MWSEP_MAX_AREAS], mx[MWSEP_MAX_AREAS];
+    for (int a = 0; a < ap->number_integrals; ++a)
+    {
+        if (!es->integral[a])
+        {
+            mwsep_fail(MWSEP_ERR_STATE);
+            return worker_fail(results, 1 + S);
+        }
+        mn[a] = es->integral[a]->min_calculation;
+        mx[a] = es->integral[a]->max_calculation;
+    }
+    mwsep_result r;
+    if (wedge_set_slices(c, *c->wedges[0], mn, mx) != MWSEP_OK ||
+        mwsep_ctx_integrals(c, parameters, MWSEP_PLAIN_F64, &r) != MWSEP_OK)
+        return worker_fail(results, 1 + S);
+    for (int a = 0; a < ap->number_integrals; ++a)
+    {
+        INTEGRAL_AREA* ia = es->integral[a];
+        ia->background_integral = r.area_integrals[a][0];
+        for (int s = 0; s < S; ++s) ia->stream_integrals[s] = r.area_integrals[a][1 + s];
+        const AreaHost& A = c->wedges[0]->prob.area[a];
+        ia->current_calculation = A.cell_begin < A.cell_end ? (long)A.cell_end : ia->min_calculation;
+    }
+    es->current_integral = ap->number_integrals;
+    es->background_integral = results[0] = r.background_integral;
+    for (int s = 0; s < S; ++s) es->stream_integrals[s] = results[1 + s] = r.stream_integrals[s];
+}
+
+/* likelihood_f (cpu/astronomy_worker.c:94-121): calculate_likelihood of
+ * this rank's stars at *ap's current parameters against the given
+ * (composed) integrals[0..S]; results[0] = prob_sum, results[1] =
+ * bad_jacobians (always 0), and es as the reference leaves it. */
+extern "C" void mwsep_likelihood_f(double* integrals, double* results, ASTRONOMY_PARAMETERS* ap, EVALUATION_STATE* es,
+                                   STAR_POINTS* sp)
+{
+    if (!integrals || !results || !ap || !es || !sp || ap->number_streams < 0 ||
+        ap->number_streams > MWSEP_MAX_STREAMS)
+    {
+        mwsep_fail(MWSEP_ERR_ARG);
+        return worker_fail(results, 2);
+    }
+    const int S = ap->number_streams;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    mwsep_ctx* c = default_ctx();
+    const int P = mwsep_get_optimized_parameter_count(ap);
+    if (!c || P < 0) return worker_fail(results, 2);
+    std::vector<double> theta((size_t)std::max(P, 1));
+    if (mwsep_get_search_parameters(ap, theta.data()) != MWSEP_OK || mwsep_ctx_set_problem(c, ap) != MWSEP_OK)
+        return worker_fail(results, 2);
+    if (cudaSetDevice(c->device) != cudaSuccess)
+    {
+        mwsep_fail(MWSEP_ERR_CUDA);
+        return worker_fail(results, 2);
+    }
+    if (wedge_set_stars_rows(c, *c->wedges[0], sp, false) != MWSEP_OK) return worker_fail(results, 2);
+    c->eng.desc_dirty = true;
+    mwsep_result r;
+    if (mwsep_ctx_likelihood(c, theta.data(), integrals, MWSEP_PLAIN_F64, &r) != MWSEP_OK)
+        return worker_fail(results, 2);
+    es->background_integral = integrals[0];
+    if (es->stream_integrals)
+        for (int s = 0; s < S && s < es->number_streams; ++s) es->stream_integrals[s] = integrals[1 + s];
+    es->current_star_point = sp->number_stars;
+    es->num_zero = r.num_zero;
+    es->bad_jacobians = 0;
+    es->prob_sum = r.prob_sum;
+    results[0] = r.prob_sum;
+    results[1] = 0.0;
+}
 
 extern "C" int mwsep_evalfunc_transfer_bytes(size_t* h2d_out, size_t* d2h_out)
 {

@@ -212,6 +212,12 @@ _SIGS = {
                                           _P(C.c_double)]),
     "mwsep_ctx_theta_count": (C.c_int, [C.c_void_p]),
     "mwsep_ctx_evaluate": (C.c_int, [C.c_void_p, _P(C.c_double), C.c_int, _P(mwsep_result)]),
+    "mwsep_ctx_integrals": (C.c_int, [C.c_void_p, _P(C.c_double), C.c_int, _P(mwsep_result)]),
+    "mwsep_ctx_likelihood": (C.c_int, [C.c_void_p, _P(C.c_double), _P(C.c_double), C.c_int, _P(mwsep_result)]),
+    "mwsep_integral_f": (None, [_P(C.c_double), _P(C.c_double), _P(ASTRONOMY_PARAMETERS), _P(EVALUATION_STATE),
+                                _P(STAR_POINTS)]),
+    "mwsep_likelihood_f": (None, [_P(C.c_double), _P(C.c_double), _P(ASTRONOMY_PARAMETERS), _P(EVALUATION_STATE),
+                                  _P(STAR_POINTS)]),
     "mwsep_ctx_evaluate_batch": (C.c_int, [C.c_void_p, C.c_int, _P(C.c_double), C.c_int,
                                            _P(mwsep_result)]),
     "mwsep_ctx_device_bytes": (C.c_int, [C.c_void_p, _P(C.c_size_t)]),

@@ -277,6 +277,28 @@ def evaluate(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints
     return _evalfunc(N.lib().mwsep_evaluate, theta, ap, es, sp)
 
 
+def integral_f(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> List[float]:
+    """integral_f (cpu/astronomy_worker.c:33-64) on the GPU: this rank's
+    cut-subtracted background and stream integrals."""
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    out = np.zeros(1 + ap.number_streams)
+    N.lib().mwsep_integral_f(_dptr(t), _dptr(out), C.byref(ap.struct), C.byref(es.struct), C.byref(sp.struct))
+    if np.isnan(out).any():
+        raise N.MwsepError(N.lib().mwsep_last_error(), "integral_f")
+    return out.tolist()
+
+
+def likelihood_f(integrals, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> List[float]:
+    """likelihood_f (cpu/astronomy_worker.c:94-121) on the GPU: [prob_sum,
+    bad_jacobians] of this rank's stars against the given integrals."""
+    i = np.ascontiguousarray(integrals, dtype=np.float64)
+    out = np.zeros(2)
+    N.lib().mwsep_likelihood_f(_dptr(i), _dptr(out), C.byref(ap.struct), C.byref(es.struct), C.byref(sp.struct))
+    if np.isnan(out).any():
+        raise N.MwsepError(N.lib().mwsep_last_error(), "likelihood_f")
+    return out.tolist()
+
+
 def evaluate_mixed(theta, ap: AstronomyParameters, es: EvaluationState, sp: StarPoints) -> float:
     """Compensated-FP32 GPU evaluation with the same contract as evaluate."""
     return _evalfunc(N.lib().mwsep_evaluate_mixed, theta, ap, es, sp)
@@ -383,6 +405,23 @@ class Context:
             raise N.MwsepError(N.MWSEP_ERR_PARAM_COUNT, "evaluate")
         r = N.mwsep_result()
         N.check(N.lib().mwsep_ctx_evaluate(self._h, _dptr(t), precision, C.byref(r)), "evaluate")
+        return Result.from_c(r)
+
+    def integrals(self, theta, precision: int = N.MWSEP_PLAIN_F64) -> Result:
+        """The integrals alone of the resident problem's cells
+        (mwsep_ctx_integrals): a rank's integral_f."""
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        r = N.mwsep_result()
+        N.check(N.lib().mwsep_ctx_integrals(self._h, _dptr(t), precision, C.byref(r)), "integrals")
+        return Result.from_c(r)
+
+    def likelihood(self, theta, integrals, precision: int = N.MWSEP_PLAIN_F64) -> Result:
+        """The resident catalogue's likelihood against given cut-subtracted
+        integrals (mwsep_ctx_likelihood): a rank's likelihood_f."""
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        i = np.ascontiguousarray(integrals, dtype=np.float64)
+        r = N.mwsep_result()
+        N.check(N.lib().mwsep_ctx_likelihood(self._h, _dptr(t), _dptr(i), precision, C.byref(r)), "likelihood")
         return Result.from_c(r)
 
     def evaluate_batch(self, thetas, precision: int = N.MWSEP_PLAIN_F64) -> List[Result]:

@@ -76,3 +76,43 @@ def likelihood_compose(rank_results: Sequence[Sequence[float]], total_stars: int
     sum prob_sum / (N - sum bad_jacobians) - 3."""
     s = compensated_sum(np.asarray(rank_results, dtype=np.float64).reshape(-1, 2))
     return float(s[0] / (float(total_stars) - s[1]) - 3.0)
+
+
+def evaluate_sharded(params_path: str, stars_path: str, theta, precision: int = 0, group=None, device: int = 0):
+    """One evaluation sharded over the ranks of the process group, as the
+    reference's distributed client runs it (cpu/astronomy_worker.c,
+    cpu/mpi_astronomy.c), on this rank's GPU through the library:
+
+      1. this rank's cells of every area (split_astronomy_parameters) are
+         integrated (mwsep_ctx_integrals, integral_f);
+      2. the ranks' cut-subtracted integrals are summed (integral_compose,
+         allreduce_sum);
+      3. this rank's stars (split_star_points) are evaluated against the sum
+         (mwsep_ctx_likelihood, likelihood_f);
+      4. the ranks' (prob_sum, bad_jacobians) are summed and composed
+         (likelihood_compose).
+
+    The only exchanges are the two host-side sums.  Without an initialised
+    process group it is one rank's whole evaluation.  Returns
+    (integrals [1 + S], log-likelihood)."""
+    import torch.distributed as dist
+    from .separation import AstronomyParameters, Context, StarPoints
+    world = dist.get_world_size(group) if dist.is_available() and dist.is_initialized() else 1
+    rank = dist.get_rank(group) if world > 1 else 0
+    ap = AstronomyParameters.read(params_path)
+    sp = StarPoints.read(stars_path)
+    total_stars = sp.number_stars
+    if world > 1:
+        ap.split(rank, world)
+        sp.split(rank, world)
+    with Context(device) as ctx:
+        ctx.set_problem(ap)
+        mine = ctx.integrals(theta, precision)
+        integrals = allreduce_sum(mine.integrals, group)
+        lk = np.zeros(2)
+        if sp.number_stars > 0:
+            ctx.set_stars(sp)
+            r = ctx.likelihood(theta, integrals, precision)
+            lk[0] = r.prob_sum
+    lk = allreduce_sum(lk, group)
+    return integrals, likelihood_compose([lk], total_stars)
