@@ -157,3 +157,34 @@ def test_negative_slice_start_refused(gpu_ctx):
     ap.struct.integral[0].contents.min_calculation = -1
     with pytest.raises(mw.MwsepError):
         gpu_ctx.set_problem(ap)
+
+
+@pytest.mark.parametrize("name", ["aux_profile", "general_alpha_delta", "sgr_coordinates", "six_streams"])
+def test_slices_other_forms_against_oracle(gpu_ctx, oracle_built, name):
+    """Rank slices of the background forms and coordinate frames the two
+    reference-sliced cases do not cover (the aux profile and general
+    alpha/delta, whose column-independent shares the double-float form sums
+    box by box; Sagittarius coordinates; eight-stream kernels), against the
+    oracle's sliced integrals (the oracle equals the reference's own sliced
+    runs on config0 and cut_area); and q = 0, whose background the
+    double-float form also sums box by box."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = load_case(name)
+    o = oracle_built.Oracle(pf, sf)
+    theta_q0 = list(g["theta"])
+    ap0 = mw.AstronomyParameters.read(pf)
+    q_index = 1 if ap0.struct.background_optimize[0] else 0  # q follows alpha when alpha is optimised
+    theta_q0[q_index] = 0.0
+    for rank in range(3):
+        ap, sp = _split_inputs(pf, sf, rank, 3)
+        gpu_ctx.set_problem(ap)
+        gpu_ctx.set_stars(sp)
+        _, want = o.integrals(g["theta"], rank=rank, nranks=3)
+        for prec, rel in ((mw.MWSEP_PLAIN_F64, REL_INT), (mw.MWSEP_PLAIN_DF, REL_INT), (mw.MWSEP_MIXED_F32, 2e-6)):
+            r = gpu_ctx.evaluate(g["theta"], prec)
+            _check(r.area_integrals, None, {"area_integrals": want.tolist()}, rel, None,
+                   f"{name} rank {rank} form {prec}")
+        _, want0 = o.integrals(theta_q0, rank=rank, nranks=3)
+        for prec in (mw.MWSEP_PLAIN_F64, mw.MWSEP_PLAIN_DF):
+            r = gpu_ctx.evaluate(theta_q0, prec)
+            assert _rel(r.area_integrals[0][0], want0[0][0]) <= REL_INT, (name, rank, prec)
