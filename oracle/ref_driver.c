@@ -14,9 +14,14 @@
  * product.  Output is one "key value" pair per line, values printed %.17g.
  *
  * Usage:  mw_ref -a params.txt -p stars.txt [-r rank -n nranks] [-k repeats]
- *                [-t] theta0 theta1 ...
+ *                [-t] [-I i0,i1,...] theta0 theta1 ...
  *   -t : print wall seconds of the evaluation(s) (integral+likelihood)
  *   -k : evaluate k times (θ reapplied, constants re-initialised each time)
+ *   -I : no integrals: the likelihood alone against the given background
+ *        and stream integrals (1 + S values), as the distributed client's
+ *        likelihood_f does with the composed integrals
+ *        (cpu/astronomy_worker.c:94-121): set_astronomy_parameters,
+ *        init_constants, then the reference's calculate_likelihood
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -40,6 +45,49 @@ static double now_seconds(void)
 
 /* One evaluation of the reference path on files.  Returns 0 on success.
  * area_out receives (1+S) doubles per integral area, in area order. */
+/* The likelihood alone of a whole catalogue against given integrals
+ * (likelihood_f, cpu/astronomy_worker.c:94-121, with the reference's own
+ * calculate_likelihood).  Returns 0 on success. */
+int mwref_likelihood_files(const char* param_path, const char* star_path, const double* theta, int n_theta,
+                           const double* integrals, double* prob_sum, int* num_zero, double* likelihood)
+{
+    ASTRONOMY_PARAMETERS ap;
+    STAR_POINTS sp;
+    EVALUATION_STATE es;
+    double* params;
+    int i;
+
+    memset(&ap, 0, sizeof(ap));
+    memset(&sp, 0, sizeof(sp));
+    memset(&es, 0, sizeof(es));
+    if (read_astronomy_parameters(param_path, &ap))
+        return 1;
+    if (read_star_points(star_path, &sp))
+        return 2;
+    initialize_state(&ap, &sp, &es);
+    if (n_theta < 1 || n_theta != get_optimized_parameter_count(&ap))
+        return 3;
+    params = (double*)malloc(sizeof(double) * (size_t)n_theta);
+    memcpy(params, theta, sizeof(double) * (size_t)n_theta);
+    set_astronomy_parameters(&ap, params);
+    init_constants(&ap);
+    es.background_integral = integrals[0];
+    for (i = 0; i < ap.number_streams; ++i)
+        es.stream_integrals[i] = integrals[1 + i];
+    if (calculate_likelihood(&ap, &es, &sp))
+        return 4;
+    free_constants(&ap);
+    *prob_sum = es.prob_sum;
+    *num_zero = es.num_zero;
+    /* likelihood_compose (:123-143) over one rank: prob_sum / N - 3 */
+    *likelihood = es.prob_sum / (sp.number_stars - es.bad_jacobians) - 3.0;
+    free(params);
+    free_state(&es);
+    free_star_points(&sp);
+    free_parameters(&ap);
+    return 0;
+}
+
 int mwref_evaluate_files(const char* param_path, const char* star_path,
                          const double* theta, int n_theta,
                          int rank, int nranks, int repeats,
@@ -127,6 +175,8 @@ int main(int argc, char** argv)
     double theta[256];
     int n_theta = 0;
     double bg = 0.0, st[64], areas[64 * 65], psum = 0.0, logl = 0.0, secs = 0.0;
+    double given[65];
+    int n_given = 0;
     int nz = 0, i, rc;
     ASTRONOMY_PARAMETERS probe;
 
@@ -138,6 +188,17 @@ int main(int argc, char** argv)
         else if (!strcmp(argv[i], "-n") && i + 1 < argc) nranks = atoi(argv[++i]);
         else if (!strcmp(argv[i], "-k") && i + 1 < argc) repeats = atoi(argv[++i]);
         else if (!strcmp(argv[i], "-t")) timing = 1;
+        else if (!strcmp(argv[i], "-I") && i + 1 < argc)
+        {
+            char* p = argv[++i];
+            while (*p && n_given < 65)
+            {
+                char* end;
+                given[n_given++] = strtod(p, &end);
+                p = (*end == ',') ? end + 1 : end;
+                if (end == p && *p) break;
+            }
+        }
         else if (n_theta < 256) theta[n_theta++] = strtod(argv[i], NULL);
     }
     if (!pfile || !sfile)
@@ -151,6 +212,17 @@ int main(int argc, char** argv)
     if (probe.number_streams > 64 || probe.number_integrals > 64)
         return 1;
 
+    if (n_given)
+    {
+        if (n_given != 1 + probe.number_streams)
+            return 2;
+        rc = mwref_likelihood_files(pfile, sfile, theta, n_theta, given, &psum, &nz, &logl);
+        if (rc)
+            return rc;
+        printf("prob_sum %.17g\nnum_zero %d\nsearch_likelihood %.17g\n", psum, nz, logl);
+        free_parameters(&probe);
+        return 0;
+    }
     rc = mwref_evaluate_files(pfile, sfile, theta, n_theta, rank, nranks, repeats,
                               &bg, st, areas, &psum, &nz, &logl, &secs);
     if (rc)

@@ -40,6 +40,15 @@ def reference_fixture_ids():
         return list(json.load(f))
 
 
+def large_fixture_ids():
+    """The reference's large test fixtures (1600 x 640 x 1400 cells) that have
+    goldens."""
+    d = os.path.join(GOLDEN, "reference_large")
+    if not os.path.isdir(d):
+        return []
+    return sorted(x for x in os.listdir(d) if os.path.exists(os.path.join(d, x, "golden.json")))
+
+
 def _unpacked(xz_path, tmp_root):
     """The decompressed star file of a committed .xz fixture (once per session)."""
     import lzma
@@ -55,13 +64,14 @@ def _unpacked(xz_path, tmp_root):
 @pytest.fixture(scope="session")
 def golden_inputs(tmp_path_factory):
     """Paths of the committed large fixtures: fn(kind, name) -> (params,
-    stars, golden) with kind "reference" (a reference test fixture) or
-    "scale" (a benchmark config, name "config1" / "config2")."""
+    stars, golden) with kind "reference" (a reference test fixture),
+    "reference_large" (one of its large fixtures) or "scale" (a benchmark
+    config, name "config1" / "config2")."""
     root = str(tmp_path_factory.mktemp("golden_stars"))
 
     def get(kind, name):
-        if kind == "reference":
-            d = os.path.join(REF_FIXTURES, name)
+        if kind in ("reference", "reference_large"):
+            d = os.path.join(GOLDEN, kind, name)
             with open(os.path.join(d, "golden.json")) as f:
                 g = json.load(f)
             xz = os.path.join(GOLDEN, g["stars_xz"])

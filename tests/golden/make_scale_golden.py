@@ -21,6 +21,14 @@ writes travels with the repository:
                cpu/star_points.c:105-131) over 8 ranks.
   --slices     golden_slices.json beside the small synthetic cases config0
                and cut_area: every rank of a 3-way split.
+  --large ID   tests/golden/reference_large/<ID>/ for the reference's large
+               fixture tests/astronomy_parameters-<ID>.txt (1600 x 640 x 1400
+               cells, ~1.7e11 points; the star file is the small fixture's):
+               the reference's distributed evaluation over 8 ranks -- each
+               rank's slice integrated by the reference, the slices summed in
+               rank order as integral_compose does (cpu/astronomy_worker.c:
+               67-92), then the reference's calculate_likelihood over the whole
+               catalogue against that sum (likelihood_f, :94-121).
 
     python tests/golden/make_scale_golden.py --fixtures --slices --config 2 --config 1
 """
@@ -174,6 +182,67 @@ def make_config(k, work):
         print(f"config{k}", r["likelihood"], r["wall_s"], "s", flush=True)
 
 
+LARGE = {"86": ("86", "86", TEST_86), "12": ("12", "12", PARAM_SET1), "79": ("79", "79", TEST_79)}
+
+
+def make_large(fid, nranks=8):
+    import subprocess
+    pname, sname, theta = LARGE[fid]
+    d = os.path.join(HERE, "reference_large", fid)
+    os.makedirs(d, exist_ok=True)
+    pf = os.path.join(d, "params.txt")
+    shutil.copyfile(os.path.join(REF_TESTS, f"astronomy_parameters-{pname}.txt"), pf)
+    sf = os.path.join(REF_TESTS, f"stars-{sname}.txt")
+    t0 = time.time()
+    ranks = _run([(pf, sf, theta, r, nranks) for r in range(nranks)])
+    S = len(ranks[0]["stream_integrals"])
+    # integral_compose: plain sums in rank order
+    ints = [0.0] * (1 + S)
+    areas = [[0.0] * (1 + S) for _ in ranks[0]["area_integrals"]]
+    for r in ranks:
+        row = [r["background_integral"]] + r["stream_integrals"]
+        for k in range(1 + S):
+            ints[k] += row[k]
+        for a, ar in enumerate(r["area_integrals"]):
+            for k in range(1 + S):
+                areas[a][k] += ar[k]
+    ints = [float(x) for x in ints]
+    areas = [[float(x) for x in a] for a in areas]
+    out = subprocess.run([orc.REF_BIN, "-a", pf, "-p", sf, "-I", ",".join(repr(x) for x in ints),
+                          *[repr(float(x)) for x in theta]], capture_output=True, text=True, check=True).stdout
+    kv = dict(l.split(" ", 1) for l in out.strip().splitlines())
+    g = {"background_integral": ints[0], "stream_integrals": ints[1:], "area_integrals": areas,
+         "prob_sum": float(kv["prob_sum"]), "num_zero": int(kv["num_zero"]),
+         "likelihood": float(kv["search_likelihood"]), "theta": [float(x) for x in theta],
+         "method": f"the reference's distributed evaluation over {nranks} ranks (integral_compose, then "
+                   f"calculate_likelihood over the whole catalogue)",
+         "params_file": f"tests/astronomy_parameters-{pname}.txt", "stars_file": f"tests/stars-{sname}.txt",
+         "stars_xz": f"reference/{sname}/stars.txt.xz", "rank_wall_s": [r["wall_s"] for r in ranks],
+         "wall_s": round(time.time() - t0, 1)}
+    with open(os.path.join(d, "golden.json"), "w") as f:
+        json.dump(g, f, indent=1)
+    print("large", fid, g["likelihood"], g["wall_s"], "s", flush=True)
+
+
+def relikelihood(fid):
+    """Recompute a large fixture's likelihood step from its stored composed
+    integrals (the reference's calculate_likelihood against them)."""
+    import subprocess
+    pname, sname, theta = LARGE[fid]
+    d = os.path.join(HERE, "reference_large", fid)
+    g = json.load(open(os.path.join(d, "golden.json")))
+    ints = [float(g["background_integral"])] + [float(x) for x in g["stream_integrals"]]
+    out = subprocess.run([orc.REF_BIN, "-a", os.path.join(d, "params.txt"), "-p",
+                          os.path.join(REF_TESTS, f"stars-{sname}.txt"), "-I", ",".join(repr(x) for x in ints),
+                          *[repr(float(x)) for x in theta]], capture_output=True, text=True, check=True).stdout
+    kv = dict(l.split(" ", 1) for l in out.strip().splitlines())
+    g["prob_sum"], g["num_zero"] = float(kv["prob_sum"]), int(kv["num_zero"])
+    g["likelihood"] = float(kv["search_likelihood"])
+    with open(os.path.join(d, "golden.json"), "w") as f:
+        json.dump(g, f, indent=1)
+    print("large", fid, g["likelihood"], flush=True)
+
+
 def make_slices():
     jobs, where = [], []
     for name in ("config0", "cut_area"):
@@ -203,6 +272,10 @@ def main():
     for i, a in enumerate(args):
         if a == "--config":
             make_config(int(args[i + 1]), work)
+        if a == "--large":
+            make_large(args[i + 1])
+        if a == "--relikelihood":
+            relikelihood(args[i + 1])
 
 
 if __name__ == "__main__":

@@ -9,7 +9,11 @@ sources; tests/golden/make_scale_golden.py):
   * benchmark config 2 (400 x 160 x 140 cells, convolve 60, 3 streams, 50k
     stars) at its base theta and four population members;
   * benchmark config 1 (1600 x 640 x 140 cells, convolve 120, 3 streams, 100k
-    stars: 1.72e10 density points) at its base theta.
+    stars: 1.72e10 density points) at its base theta;
+  * the reference's large fixtures tests/astronomy_parameters-{86,12}.txt
+    (1600 x 640 x 1400 cells, convolve 120; 86 with an 800 x 320 x 700 cut:
+    1.7e11 to 1.9e11 points), the golden being the reference's own
+    distributed evaluation over 8 ranks.
 
 Bounds, per form:
   MWSEP_PLAIN_F64, MWSEP_PLAIN_DF  1e-12 relative on every area integral,
@@ -22,7 +26,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import reference_fixture_ids
+from conftest import large_fixture_ids, reference_fixture_ids
 
 pytestmark = pytest.mark.gpu
 
@@ -112,3 +116,15 @@ def test_config1_all_forms(gpu_ctx, golden_inputs):
     _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64), g, REL_INT, ABS_LOGL, "config1 plain")
     _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF), g, REL_INT, ABS_LOGL, "config1 double-float")
     _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32), g, MIXED_REL_INT, ABS_LOGL_MIXED, "config1 mixed")
+
+
+@pytest.mark.parametrize("fid", large_fixture_ids())
+def test_reference_large_fixture_all_forms(gpu_ctx, golden_inputs, fid):
+    """The reference's largest test inputs, ten times the full-size benchmark
+    wedge: the plain FP64 form takes ~10-20 s here."""
+    import milkywayathome_client_gb300 as mw
+    pf, sf, g = golden_inputs("reference_large", fid)
+    _ctx_for(gpu_ctx, pf, sf)
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_F64), g, REL_INT, ABS_LOGL, f"{fid} large plain")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_PLAIN_DF), g, REL_INT, ABS_LOGL, f"{fid} large double-float")
+    _check(gpu_ctx.evaluate(g["theta"], mw.MWSEP_MIXED_F32), g, MIXED_REL_INT, ABS_LOGL_MIXED, f"{fid} large mixed")
