@@ -104,15 +104,14 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
 
 template <int S>
 __device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                      const LkScale<S>& ks, const mwsep_ltile& t, double* red, double2* out)
+                                      const LkScale<S>& ks, const mwsep_ltile& t, Log10Sum* red, double2* out)
 {
-    double acc[3 + S];
-#pragma unroll
-    for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
+    LkAcc<S> acc;
+    acc.init();
     const BgConsts bc = bg_consts(th);
     for (int s0 = t.star_begin + threadIdx.x; s0 < t.star_end; s0 += blockDim.x)
         likelihood_star<S>(St, th, bc, ks, s0, acc);
-    reduce_and_store<3 + S>(acc, 3 + th.n_streams, red, out);
+    lk_block_store<S>(acc, 3 + th.n_streams, red, out);
 }
 
 template <int G>
@@ -120,7 +119,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
 {
     constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (3 + S) * 32];
+    __shared__ Log10Sum red[LkSmem<S, kBlock>::N];
     __shared__ LkScale<S> ks;
     __shared__ int s_tile;
     const int n_tiles = a.counters[4 * G + 3];

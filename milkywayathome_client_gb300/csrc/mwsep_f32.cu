@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
                                                                 long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (3 + S) * 32];
+    __shared__ Log10Sum red[LkSmem<S, kBlock>::N];
     __shared__ LkScale<S> ks;
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
@@ -146,15 +146,13 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
     __syncthreads();
     const BgConsts bc = bg_consts(th);
 
-    double acc[3 + S];
-#pragma unroll
-    for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
-
+    LkAcc<S> acc;
+    acc.init();
     const int N = St.n_stars;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
         likelihood_star<S>(St, th, bc, ks, s0, acc);
-    reduce_and_store<3 + S>(acc, 3 + NS, red,
-                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
+    lk_block_store<S>(acc, 3 + NS, red,
+                      partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }
 
 /* The likelihood in two launches: the per-star densities, which need no
@@ -192,7 +190,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_finish_kernel(int N,
                                                                        long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
-    __shared__ double red[2 * (3 + S) * 32];
+    __shared__ Log10Sum red[LkSmem<S, kBlock>::N];
     __shared__ LkScale<S> ks;
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
@@ -200,9 +198,8 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_finish_kernel(int N,
     if (threadIdx.x == 0) lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
     __syncthreads();
 
-    double acc[3 + S];
-#pragma unroll
-    for (int k = 0; k < 3 + S; ++k) acc[k] = 0.0;
+    LkAcc<S> acc;
+    acc.init();
     const double* d = dens + (size_t)blockIdx.y * (1 + S) * N;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
     {
@@ -211,8 +208,8 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_finish_kernel(int N,
         for (int s = 0; s < S; ++s) st[s] = (s < NS) ? d[(size_t)(1 + s) * N + s0] : 0.0;
         star_epilogue<S>(th, ks, d[s0], st, acc);
     }
-    reduce_and_store<3 + S>(acc, 3 + NS, red,
-                            partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
+    lk_block_store<S>(acc, 3 + NS, red,
+                      partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }
 
 template <int S>

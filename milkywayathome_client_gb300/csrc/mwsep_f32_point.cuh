@@ -897,47 +897,195 @@ __device__ __forceinline__ void star_density(const mwsep_stars_dev& St, const mw
     for (int s = 0; s < S; ++s) st[s] = (double)stf[s] * exp_scale(eref[s]);
 }
 
+/* A sum of log10 terms without a log10 per term.  A positive normal term
+ * x = m 2^e (m in [1, 2)) adds e to an integer sum and multiplies m into a
+ * running FP64 product kept in [1, 2) the same way; log10 is taken once, of
+ * the product, plus e log10(2).  Each factor rounds by at most 2^-53
+ * relative, 2^-53 / ln 10 ~ 5e-17 in the sum per term -- below the rounding
+ * of the per-term log10 sum it replaces -- while the FP64 work per term is
+ * one multiply.  Terms follow log10: 0 gives -inf, a negative or NaN term
+ * NaN, +inf +inf.  The -238 of a zero star probability
+ * (cpu/evaluation_optimized.c:700-716) is counted apart (sentinels). */
+struct Log10Sum
+{
+    double m;      /* product of the mantissas, in [1, 2) */
+    long long e;   /* sum of the binary exponents */
+    int sentinels; /* -238 terms */
+    int special;   /* 1: NaN, 2: +inf, 4: -inf */
+};
+
+/* One thread's sum: the same with a 32-bit exponent sum (a thread adds at
+ * most a few thousand terms of |e| <= 1128; the block's merge widens it). */
+struct Log10Acc
+{
+    double m;
+    int e;
+    int sentinels;
+    int special;
+};
+
+constexpr double kLog10Two_hi = 0.3010299956639812;     /* log10(2) rounded to double */
+constexpr double kLog10Two_lo = -2.8037281277851704e-18; /* log10(2) - kLog10Two_hi */
+constexpr long long kMantissa = 0x000fffffffffffffLL, kOne = 0x3ff0000000000000LL;
+
+__device__ __forceinline__ void lsum_init(Log10Acc& a)
+{
+    a.m = 1.0;
+    a.e = 0;
+    a.sentinels = 0;
+    a.special = 0;
+}
+
+/* a *= m 2^e for m in [1, 2), renormalised into [1, 2) */
+template <typename T, typename E>
+__device__ __forceinline__ void lsum_mul(T& a, double m, E e)
+{
+    const long long b = __double_as_longlong(a.m * m);
+    const int k = (int)(b >> 52) - 1023; /* 0 or 1 */
+    a.m = __longlong_as_double(b - ((long long)k << 52));
+    a.e += e + k;
+}
+
+__device__ __forceinline__ void lsum_add(Log10Acc& a, double x)
+{
+    const long long b = __double_as_longlong(x);
+    if (b >= 0x0010000000000000LL && b < 0x7ff0000000000000LL) /* positive normal */
+        lsum_mul(a, __longlong_as_double((b & kMantissa) | kOne), (int)(b >> 52) - 1023);
+    else if (x == 0.0)
+        a.special |= 4;
+    else if (!(x > 0.0))
+        a.special |= 1;
+    else if (x == INFINITY)
+        a.special |= 2;
+    else /* positive subnormal */
+    {
+        const long long s = __double_as_longlong(x * 0x1p54);
+        lsum_mul(a, __longlong_as_double((s & kMantissa) | kOne), (int)(s >> 52) - 1023 - 54);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void lsum_merge(Log10Sum& a, const T& b)
+{
+    lsum_mul(a, b.m, (long long)b.e);
+    a.sentinels += b.sentinels;
+    a.special |= b.special;
+}
+
+/* the sum: NaN if a term was NaN (or both infinities occurred) */
+__device__ __forceinline__ double lsum_value(const Log10Sum& a)
+{
+    if ((a.special & 1) || (a.special & 6) == 6) return NAN;
+    if (a.special & 2) return INFINITY;
+    if (a.special & 4) return -INFINITY;
+    const double e = (double)a.e;
+    const double hi = e * kLog10Two_hi;
+    const double lo = fma(e, kLog10Two_hi, -hi) + fma(e, kLog10Two_lo, log10(a.m));
+    return (hi + -238.0 * (double)a.sentinels) + lo;
+}
+
+/* The likelihood's log10 sums of one thread: [0] the star probabilities,
+ * [1] the background alone, [2 + s] stream s alone. */
+template <int S>
+struct LkAcc
+{
+    Log10Acc c[2 + S];
+    __device__ __forceinline__ void init()
+    {
+#pragma unroll
+        for (int k = 0; k < 2 + S; ++k) lsum_init(c[k]);
+    }
+};
+
 /* The rest of calculate_likelihood for one star (cpu/evaluation_optimized.c:
- * 692-717), in FP64: the mixture weights over the integrals, log10 sums.
- * acc slots: [0] log10 p, [1] zero count, [2] bg-only, [3+s] stream-only. */
+ * 692-717), in FP64: the mixture weights over the integrals, the log10
+ * terms. */
 template <int S>
 __device__ __forceinline__ void star_epilogue(const mwsep_theta_consts& th, const LkScale<S>& ks, double bg,
-                                              const double (&st)[SArr<S>::N], double (&acc)[3 + S])
+                                              const double (&st)[SArr<S>::N], LkAcc<S>& acc)
 {
     const int NS = th.n_streams;
-    double bg_only = bg * ks.bg;
+    const double bg_only = bg * ks.bg;
     double star_prob = bg_only;
-    acc[2] += (bg_only == 0.0) ? -238.0 : log10(bg_only * ks.inv_sw);
+    if (bg_only == 0.0)
+        ++acc.c[1].sentinels;
+    else
+        lsum_add(acc.c[1], bg_only * ks.inv_sw);
 #pragma unroll
     for (int s = 0; s < S; ++s)
     {
         if (s < NS)
         {
-            double st_only = st[s] * ks.st[s];
+            const double st_only = st[s] * ks.st[s];
             star_prob += st_only;
-            acc[3 + s] += (st_only == 0.0) ? -238.0 : log10(st_only * ks.inv_sw);
+            if (st_only == 0.0)
+                ++acc.c[2 + s].sentinels;
+            else
+                lsum_add(acc.c[2 + s], st_only * ks.inv_sw);
         }
     }
     star_prob *= ks.inv_sw;
     if (star_prob != 0.0)
-        acc[0] += log10(star_prob);
+        lsum_add(acc.c[0], star_prob);
     else
-    {
-        acc[0] += -238.0;
-        acc[1] += 1.0;
-    }
+        ++acc.c[0].sentinels;
 }
 
 /* calculate_likelihood for one star (cpu/evaluation_optimized.c:665-717):
  * the density sums in FP32, everything after them in FP64. */
 template <int S>
 __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                                const BgConsts& bc, const LkScale<S>& ks, int s0,
-                                                double (&acc)[3 + S])
+                                                const BgConsts& bc, const LkScale<S>& ks, int s0, LkAcc<S>& acc)
 {
     double bg, st[SArr<S>::N];
     star_density<S>(St, th, bc, s0, bg, st);
     star_epilogue<S>(th, ks, bg, st, acc);
+}
+
+/* Shared memory of lk_block_store: one Log10Sum per warp and sum. */
+template <int S, int BLOCK>
+struct LkSmem
+{
+    static constexpr int N = (BLOCK / 32) * (2 + S);
+};
+
+/* The block's sums, combined in a fixed order (warps by butterfly, then
+ * warp after warp), as the likelihood partial slots: [0] log10 p, [1] the
+ * zero-probability count, [2] background alone, [3 + s] stream s alone,
+ * each (value, 0); n_out = 3 + streams. */
+template <int S>
+__device__ __forceinline__ void lk_block_store(LkAcc<S>& acc, int n_out, Log10Sum* smem, double2* out)
+{
+    constexpr int NC = 2 + S;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+    {
+        Log10Sum a;
+        a.m = acc.c[k].m;
+        a.e = acc.c[k].e;
+        a.sentinels = acc.c[k].sentinels;
+        a.special = acc.c[k].special;
+        for (int off = 16; off > 0; off >>= 1)
+        {
+            Log10Sum b;
+            b.m = __shfl_xor_sync(0xffffffffu, a.m, off);
+            b.e = __shfl_xor_sync(0xffffffffu, a.e, off);
+            b.sentinels = __shfl_xor_sync(0xffffffffu, a.sentinels, off);
+            b.special = __shfl_xor_sync(0xffffffffu, a.special, off);
+            lsum_merge(a, b);
+        }
+        if (lane == 0) smem[warp * NC + k] = a;
+    }
+    __syncthreads();
+    if (warp == 0 && lane < NC)
+    {
+        Log10Sum t = smem[lane];
+        for (int w = 1; w < nw; ++w) lsum_merge(t, smem[w * NC + lane]);
+        const int slot = lane == 0 ? 0 : lane + 1;
+        if (slot < n_out) out[slot] = make_double2(lsum_value(t), 0.0);
+        if (lane == 0) out[1] = make_double2((double)t.sentinels, 0.0);
+    }
 }
 
 } // namespace f32
