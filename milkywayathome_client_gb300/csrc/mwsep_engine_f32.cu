@@ -30,8 +30,8 @@ __device__ __forceinline__ void load_area(mwsep_area_dev& dst, const mwsep_area_
 /* cs: the block's column-constant scratch, kTileCols * ColWords<S>::N floats
  * per warp (used by warp-tile items). */
 template <int S, int FORM>
-__device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const mwsep_itile& t,
-                                      double* red, float* cs, double2* out)
+__device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const ThetaDF<S>& td,
+                                      const mwsep_itile& t, double* red, float* cs, double2* out)
 {
     double acc[1 + S];
 #pragma unroll
@@ -44,9 +44,9 @@ __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta
         for (long long wt = t.item_begin + warp; wt < t.item_end; wt += blockDim.x >> 5)
         {
             if constexpr (PackedTile<S>::ok)
-                warp_tile2<S, FORM>(A, th, bc, wt, mine, acc);
+                warp_tile2<S, FORM>(A, th, td, bc, wt, mine, acc);
             else
-                warp_tile<S, FORM>(A, th, bc, wt, mine, acc);
+                warp_tile<S, FORM>(A, th, td, bc, wt, mine, acc);
         }
     }
     else
@@ -57,14 +57,15 @@ __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta
 
 template <int S>
 __device__ __forceinline__ void itile_form(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                           const mwsep_itile& t, double* red, float* cs, double2* out)
+                                           const ThetaDF<S>& td, const mwsep_itile& t, double* red, float* cs,
+                                           double2* out)
 {
     switch (mwsep_bg_form(&th))
     {
-    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, t, red, cs, out); break;
-    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, t, red, cs, out); break;
-    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, t, red, cs, out); break;
-    default: itile<S, BG_NONE>(A, th, t, red, cs, out); break;
+    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, td, t, red, cs, out); break;
+    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, td, t, red, cs, out); break;
+    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, td, t, red, cs, out); break;
+    default: itile<S, BG_NONE>(A, th, td, t, red, cs, out); break;
     }
 }
 
@@ -81,6 +82,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
 {
     constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     __shared__ mwsep_area_dev A;
     __shared__ double red[2 * (1 + S) * 32];
     __shared__ __align__(16) float cs[(kBlock / 32) * TileSmem<S>::N];
@@ -96,21 +98,24 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
         load_theta(th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10));
         load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
         __syncthreads();
+        if (threadIdx.x == 0) theta_df<S>(th, td);
+        __syncthreads();
         double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
-        itile_form<S>(A, th, tile, red, cs, out);
+        itile_form<S>(A, th, td, tile, red, cs, out);
         __syncthreads();
     }
 }
 
 template <int S>
 __device__ __forceinline__ void ltile(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                      const LkScale<S>& ks, const mwsep_ltile& t, Log10Sum* red, double2* out)
+                                      const ThetaDF<S>& td, const LkScale<S>& ks, const mwsep_ltile& t,
+                                      Log10Sum* red, double2* out)
 {
     LkAcc<S> acc;
     acc.init();
     const BgConsts bc = bg_consts(th);
     for (int s0 = t.star_begin + threadIdx.x; s0 < t.star_end; s0 += blockDim.x)
-        likelihood_star<S>(St, th, bc, ks, s0, acc);
+        likelihood_star<S>(St, th, td, bc, ks, s0, acc);
     lk_block_store<S>(acc, 3 + th.n_streams, red, out);
 }
 
@@ -119,6 +124,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
 {
     constexpr int S = GroupS<G>::S;
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     __shared__ Log10Sum red[LkSmem<S, kBlock>::N];
     __shared__ LkScale<S> ks;
     __shared__ int s_tile;
@@ -135,10 +141,14 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
         const mwsep_stars_dev St =
             a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
-        if (threadIdx.x == 0) lk_scale<S>(th, I, ks);
+        if (threadIdx.x == 0)
+        {
+            lk_scale<S>(th, I, ks);
+            theta_df<S>(th, td);
+        }
         __syncthreads();
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
-        ltile<S>(St, th, ks, tile, red, out);
+        ltile<S>(St, th, td, ks, tile, red, out);
         __syncthreads();
     }
 }

@@ -55,11 +55,14 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
                                                                   long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     __shared__ double red[2 * (1 + S) * 32];
     __shared__ __align__(16) float cs[kBlock / 32][TileSmem<S>::N];
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     if (mwsep_bg_form(&th) != FORM) return;
+    if (threadIdx.x == 0) theta_df<S>(th, td);
+    __syncthreads();
 
     double acc[1 + S];
 #pragma unroll
@@ -71,9 +74,9 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
     {
         if constexpr (PackedTile<S>::ok)
-            warp_tile2<S, FORM>(A, th, bc, wt, cs[warp], acc);
+            warp_tile2<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
         else
-            warp_tile<S, FORM>(A, th, bc, wt, cs[warp], acc);
+            warp_tile<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
     }
     reduce_and_store<1 + S>(acc, 1 + th.n_streams, red,
                             partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (1 + th.n_streams));
@@ -92,10 +95,13 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_dyn_kern
     long long theta_stride, int* __restrict__ counters, int counter_stride)
 {
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     __shared__ __align__(16) float cs[kBlock / 32][TileSmem<S>::N];
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     if (mwsep_bg_form(&th) != FORM) return;
+    if (threadIdx.x == 0) theta_df<S>(th, td);
+    __syncthreads();
     const BgConsts bc = bg_consts(th);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int NC = 1 + th.n_streams;
@@ -111,9 +117,9 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_dyn_kern
 #pragma unroll
         for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
         if constexpr (PackedTile<S>::ok)
-            warp_tile2<S, FORM>(A, th, bc, wt, cs[warp], acc);
+            warp_tile2<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
         else
-            warp_tile<S, FORM>(A, th, bc, wt, cs[warp], acc);
+            warp_tile<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
 #pragma unroll
         for (int k = 0; k < 1 + S; ++k)
 #pragma unroll
@@ -137,12 +143,17 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
                                                                 long long theta_stride)
 {
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     __shared__ Log10Sum red[LkSmem<S, kBlock>::N];
     __shared__ LkScale<S> ks;
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     const int NS = th.n_streams;
-    if (threadIdx.x == 0) lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
+    if (threadIdx.x == 0)
+    {
+        lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
+        theta_df<S>(th, td);
+    }
     __syncthreads();
     const BgConsts bc = bg_consts(th);
 
@@ -150,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
     acc.init();
     const int N = St.n_stars;
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
-        likelihood_star<S>(St, th, bc, ks, s0, acc);
+        likelihood_star<S>(St, th, td, bc, ks, s0, acc);
     lk_block_store<S>(acc, 3 + NS, red,
                       partials + (size_t)blockIdx.y * theta_stride + (size_t)blockIdx.x * (3 + NS));
 }
@@ -165,7 +176,10 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_density_kernel(const mw
                                                                         double* __restrict__ dens)
 {
     __shared__ mwsep_theta_consts th;
+    __shared__ ThetaDF<S> td;
     load_theta(th, thetas + blockIdx.y);
+    __syncthreads();
+    if (threadIdx.x == 0) theta_df<S>(th, td);
     __syncthreads();
     const BgConsts bc = bg_consts(th);
     const int N = St.n_stars, NS = th.n_streams;
@@ -173,7 +187,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_density_kernel(const mw
     for (int s0 = blockIdx.x * blockDim.x + threadIdx.x; s0 < N; s0 += gridDim.x * blockDim.x)
     {
         double bg, st[SArr<S>::N];
-        star_density<S>(St, th, bc, s0, bg, st);
+        star_density<S>(St, th, td, bc, s0, bg, st);
         d[s0] = bg;
 #pragma unroll
         for (int s = 0; s < S; ++s)

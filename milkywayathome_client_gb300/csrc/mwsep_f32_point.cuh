@@ -30,6 +30,7 @@
 #include "mwsep_internal.h"
 #include "mwsep_reduce.cuh"
 #include "mwsep_checks.cuh"
+#include "mwsep_df.cuh"
 
 namespace mwsep {
 namespace f32 {
@@ -294,6 +295,143 @@ __device__ __forceinline__ void column_consts(const double* g, const mwsep_theta
     }
 }
 
+/* ---- the column (or star) prologue in double-float ----
+ * The same constants as column_consts, formed in pairs of floats (about 2^-44
+ * relative, mwsep_df.cuh) on the FP32 pipe: GB300 runs FP64 at ~1/70 of
+ * FP32, so the ~190 FP64 operations of a column prologue held a warp for as
+ * long as thousands of FP32 ones.  Each constant is rounded to float as
+ * before; the exponent constants k2 (r - rs)^2 + k0 need rs and Ds to ~1e-9
+ * absolute, which the pairs give with margin under the cancellation of
+ * e = q - rs p (|q| / |e| up to ~1e4). */
+
+/* theta-only constants, formed once per block in FP64 and split into pairs:
+ * 1/q^2 (0 when q = 0: no background is evaluated then, and the streams do
+ * not depend on rb), each stream's axis a, its centre's offset from the
+ * axis q = c' - (a.c') a with c' = c + (8.5, 0, 0), and
+ * f = -log2(e) / (2 sigma^2) (0 for a switched-off stream). */
+template <int S>
+struct ThetaDF
+{
+    dfl::df iq2;
+    dfl::df a[SArr<S>::N][3], q[SArr<S>::N][3], f[SArr<S>::N];
+};
+
+template <int S>
+__device__ __forceinline__ void theta_df(const mwsep_theta_consts& th, ThetaDF<S>& td)
+{
+    td.iq2 = dfl::from_double(th.q != 0.0 ? 1.0 / (th.q * th.q) : 0.0);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        const bool on = s < th.n_streams && th.stream_on[s];
+        const double a0 = th.a[s][0], a1 = th.a[s][1], a2 = th.a[s][2];
+        const double c0 = th.c[s][0] + MW_LBR_R, c1 = th.c[s][1], c2 = th.c[s][2];
+        const double ac = a0 * c0 + a1 * c1 + a2 * c2;
+        td.a[s][0] = dfl::from_double(on ? a0 : 0.0);
+        td.a[s][1] = dfl::from_double(on ? a1 : 0.0);
+        td.a[s][2] = dfl::from_double(on ? a2 : 0.0);
+        td.q[s][0] = dfl::from_double(on ? c0 - ac * a0 : 0.0);
+        td.q[s][1] = dfl::from_double(on ? c1 - ac * a1 : 0.0);
+        td.q[s][2] = dfl::from_double(on ? c2 - ac * a2 : 0.0);
+        td.f[s] = dfl::from_double(on ? -kLog2e / th.sigma_sq2[s] : 0.0);
+    }
+}
+
+/* The block's theta and its pair constants: thread 0 forms them after the
+ * theta is loaded (callers sync before and after). */
+__device__ __forceinline__ dfl::df df_norm(dfl::df x)
+{
+    float h, l;
+    dfl::fast_two_sum(x.hi, x.lo, h, l);
+    return dfl::mk(h, l);
+}
+
+__device__ __forceinline__ dfl::df df_sub(dfl::df x, dfl::df y) { return dfl::add_fast(x, dfl::neg(y)); }
+
+__device__ __forceinline__ dfl::df df_dot3(const dfl::df (&x)[3], const dfl::df (&y)[3])
+{
+    return dfl::add_fast(dfl::add_fast(dfl::mul(x[0], y[0]), dfl::mul(x[1], y[1])), dfl::mul(x[2], y[2]));
+}
+
+/* floor of a pair, clamped at kErefFloor (also for NaN) */
+__device__ __forceinline__ int df_floor(dfl::df x)
+{
+    if (!(x.hi > (float)kErefFloor)) return kErefFloor;
+    float f = floorf(x.hi);
+    if (f == x.hi && x.lo < 0.f) f -= 1.f;
+    return (int)f;
+}
+
+/* column_consts from pairs.  FROM_HI as there.  STAR: eref is computed here
+ * (each stream's largest exponent over [r_lo, r_hi], floored) instead of
+ * given; either way each stream's k0c comes out shifted by it. */
+template <int S, bool FROM_HI, bool STAR>
+__device__ __forceinline__ void column_consts_df(const double* g, const mwsep_theta_consts& th, const ThetaDF<S>& td,
+                                                 Col<S>& cc, int (&eref)[SArr<S>::N], double r_lo = 0.0,
+                                                 double r_hi = 0.0)
+{
+    using namespace dfl;
+    df u[3];
+    u[0] = from_double(g[1] * g[3]);
+    u[1] = from_double(g[1] * g[2]);
+    u[2] = from_double(g[0]);
+    const df perp = add_fast(sqr(u[1]), mul(sqr(u[2]), td.iq2));
+    const df B2 = add_fast(sqr(u[0]), perp);
+    df rb = df_norm(div(mul(mk((float)MW_LBR_R, 0.f), u[0]), B2));
+    const df Db = df_norm(div(mul(mk((float)(MW_LBR_R * MW_LBR_R), 0.f), perp), B2));
+    cc.B2 = B2.hi;
+    cc.rb_hi = rb.hi;
+    if (FROM_HI)
+    {
+        /* t' = r - rb_hi; the pair's low part is rb - rb_hi */
+        const float dl = rb.lo;
+        cc.rb_lo = -2.f * B2.hi * dl;
+        cc.Db = add_fast(Db, mk(B2.hi * dl * dl, 0.f)).hi;
+        rb = mk(rb.hi, 0.f);
+    }
+    else
+    {
+        cc.rb_lo = rb.lo;
+        cc.Db = Db.hi;
+    }
+    const df rlo = from_double(r_lo), rhi = from_double(r_hi);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        cc.k2[s] = 0.f;
+        cc.k2dl[s] = 0.f;
+        cc.k0c[s] = -1.0e30f; /* far below the FTZ range: a stream that is off or absent */
+        cc.d_hi[s] = 0.f;
+        if (STAR) eref[s] = kErefFloor;
+        if (s < th.n_streams && th.stream_on[s])
+        {
+            const df au = df_dot3(td.a[s], u);
+            df p[3], e[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) p[i] = df_sub(u[i], mul(au, td.a[s][i]));
+            const df A2 = add_fast(add_fast(sqr(p[0]), sqr(p[1])), sqr(p[2]));
+            const df rs = (A2.hi > 1e-30f) ? df_norm(div(df_dot3(p, td.q[s]), A2)) : mk(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) e[i] = df_sub(td.q[s][i], mul(rs, p[i]));
+            const df Dsf = mul(add_fast(add_fast(sqr(e[0]), sqr(e[1])), sqr(e[2])), td.f[s]);
+            const df k2 = mul(A2, td.f[s]);
+            const df d = df_sub(rb, rs);
+            cc.d_hi[s] = d.hi;
+            cc.k2[s] = k2.hi;
+            cc.k2dl[s] = 2.f * k2.hi * d.lo;
+            const df k0c = add_fast(Dsf, mk(k2.hi * d.lo * d.lo, 0.f));
+            if (STAR)
+            {
+                /* the largest exponent over the star's points: at rs clamped
+                 * into [r_lo, r_hi] */
+                const df rc = (rs.hi < rlo.hi) ? df_sub(rlo, rs) : (rs.hi > rhi.hi) ? df_sub(rhi, rs) : mk(0.f, 0.f);
+                eref[s] = df_floor(add_fast(mul(k2, sqr(rc)), Dsf));
+            }
+            cc.k0c[s] = fmaxf(add_fast(k0c, mk(-(float)eref[s], 0.f)).hi, -1.0e30f);
+        }
+    }
+}
+
 struct BgConsts
 {
     float r0, aux_a, aux_b, aux_c, alpha, ad3;
@@ -523,8 +661,8 @@ __device__ __forceinline__ void load_col(const float* src, Col<S>& cc)
  * acc. */
 template <int S, int FORM>
 __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                          const BgConsts& bc, long long wt, float* __restrict__ cs,
-                                          double (&acc)[1 + S])
+                                          const ThetaDF<S>& td, const BgConsts& bc, long long wt,
+                                          float* __restrict__ cs, double (&acc)[1 + S])
 {
     constexpr int P = mwsep::TileP<S>::P;
     constexpr int CW = ColWords<S>::N;
@@ -549,7 +687,7 @@ __device__ __forceinline__ void warp_tile(const mwsep_area_dev& A, const mwsep_t
         if (live)
         {
             Col<S> cc;
-            column_consts<S>(g, th, cc, nullptr, 0.0, 0.0, eref);
+            column_consts_df<S, false, false>(g, th, td, cc, eref);
             store_col<S>(cs + lane * CW, cc);
         }
     }
@@ -751,9 +889,9 @@ __device__ __forceinline__ void points4(const f2 XA, const f2 YA, const f2 WA, c
  * factors (inline: out of line, the call's register saves cost 1.5% of the
  * full-size integral). */
 template <int S>
-__device__ __forceinline__ void tile_prologue2(const mwsep_area_dev& A, const mwsep_theta_consts& th, int k0, int k1,
-                                            int mu0, int nu, int ncols, int lane, double idsv, float* cs,
-                                            double* tscale)
+__device__ __forceinline__ void tile_prologue2(const mwsep_area_dev& A, const mwsep_theta_consts& th,
+                                            const ThetaDF<S>& td, int k0, int k1, int mu0, int nu, int ncols,
+                                            int lane, double idsv, float* cs, double* tscale)
 {
     constexpr int CW = PackedTile<S>::W;
     const bool live = lane < ncols;
@@ -764,7 +902,7 @@ __device__ __forceinline__ void tile_prologue2(const mwsep_area_dev& A, const mw
     if (live)
     {
         Col<S> cc;
-        column_consts<S, true>(g, th, cc, nullptr, 0.0, 0.0, eref);
+        column_consts_df<S, true, false>(g, th, td, cc, eref);
         store_col2<S>(cs + lane * CW, cc);
     }
 }
@@ -773,8 +911,8 @@ __device__ __forceinline__ void tile_prologue2(const mwsep_area_dev& A, const mw
  * this warp. */
 template <int S, int FORM>
 __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                           const BgConsts& bc, long long wt, float* __restrict__ cs,
-                                           double (&acc)[1 + S])
+                                           const ThetaDF<S>& td, const BgConsts& bc, long long wt,
+                                           float* __restrict__ cs, double (&acc)[1 + S])
 {
     constexpr int P = PackedTile<S>::P;
     constexpr int NP = P / 2;
@@ -792,7 +930,7 @@ __device__ __forceinline__ void warp_tile2(const mwsep_area_dev& A, const mwsep_
      * eref; ids_nu 2^eref goes after the constants in shared memory */
     const double idsv = A.ids[MWSEP_IDX(nu, A.nu_steps, 3)];
     double* const tscale = reinterpret_cast<double*>(cs + mwsep::kTileCols * CW);
-    tile_prologue2<S>(A, th, k0, k1, mu0, nu, ncols, lane, idsv, cs, tscale);
+    tile_prologue2<S>(A, th, td, k0, k1, mu0, nu, ncols, lane, idsv, cs, tscale);
     __syncwarp();
     const int nf = (k1 - k0) * C;
     for (int g0 = 0; g0 < nf; g0 += 32 * P)
@@ -871,19 +1009,16 @@ __device__ __forceinline__ void lk_scale(const mwsep_theta_consts& th, const dou
  * shift undone (the star weights carry its reff_xr_rp3). */
 template <int S>
 __device__ __forceinline__ void star_density(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                             const BgConsts& bc, int s0, double& bg, double (&st)[SArr<S>::N])
+                                             const ThetaDF<S>& td, const BgConsts& bc, int s0, double& bg,
+                                             double (&st)[SArr<S>::N])
 {
     const int N = St.n_stars;
     Col<S> cc;
     s0 = (int)MWSEP_IDX(s0, N, 7);
     /* the star's convolution points span [r_point[0], r_point[C-1]] */
-    StreamExp<S> se;
     const double ra = St.r_point[s0], rb = St.r_point[(size_t)(St.convolve - 1) * N + s0];
-    column_consts<S>(St.geom + 4 * (size_t)s0, th, cc, &se, fmin(ra, rb), fmax(ra, rb));
     int eref[SArr<S>::N];
-#pragma unroll
-    for (int s = 0; s < S; ++s) eref[s] = exp_ref(se.amax[s]);
-    shift_exponents<S>(th, se, eref, cc);
+    column_consts_df<S, false, true>(St.geom + 4 * (size_t)s0, th, td, cc, eref, fmin(ra, rb), fmax(ra, rb));
     float bgf = 0.f, stf[SArr<S>::N];
     switch (mwsep_bg_form(&th))
     {
@@ -1035,10 +1170,11 @@ __device__ __forceinline__ void star_epilogue(const mwsep_theta_consts& th, cons
  * the density sums in FP32, everything after them in FP64. */
 template <int S>
 __device__ __forceinline__ void likelihood_star(const mwsep_stars_dev& St, const mwsep_theta_consts& th,
-                                                const BgConsts& bc, const LkScale<S>& ks, int s0, LkAcc<S>& acc)
+                                                const ThetaDF<S>& td, const BgConsts& bc, const LkScale<S>& ks,
+                                                int s0, LkAcc<S>& acc)
 {
     double bg, st[SArr<S>::N];
-    star_density<S>(St, th, bc, s0, bg, st);
+    star_density<S>(St, th, td, bc, s0, bg, st);
     star_epilogue<S>(th, ks, bg, st, acc);
 }
 
