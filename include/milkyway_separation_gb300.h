@@ -59,6 +59,9 @@ typedef struct
 
     int number_background_parameters;
     double background_weight;
+    /* number_background_parameters values; at least 7 when aux_bg_profile
+     * is 1, whose a, b, c are values 4..6 whatever
+     * number_background_parameters says (as init_constants reads them) */
     double* background_parameters;
     double* background_step;
     double* background_min;

@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "milkyway_separation_gb300.h"
+#include "mwsep_params.h"
 #include "mwsep_status.h"
 
 namespace {
@@ -44,6 +45,10 @@ namespace {
 const char kCatMagic[8] = {'M', 'W', 'S', 'E', 'P', 'C', 'A', 'T'};
 const char kParMagic[8] = {'M', 'W', 'S', 'E', 'P', 'P', 'A', 'R'};
 constexpr uint32_t kVersion = 1;
+/* parameter files: 1 stored number_background_parameters values of each
+ * background array; 2 also the count of background values (the aux
+ * profile's 4..6 kept where number_parameters counts fewer) */
+constexpr uint32_t kParVersion = 2;
 constexpr uint64_t kAlign = 64;
 
 struct CatHeader
@@ -287,11 +292,13 @@ extern "C" int mwsep_write_astronomy_parameters_binary(const char* path, const A
     if (!little_endian()) return mwsep_fail(MWSEP_ERR_UNSUPPORTED);
     const int nb = ap->number_background_parameters, S = ap->number_streams, P = ap->number_stream_parameters;
     if (nb < 0 || S < 0 || P < 0 || ap->number_integrals < 0) return mwsep_fail(MWSEP_ERR_ARG);
+    const int nv = mwsep_background_values(ap);
     Out o;
     o.put(ap->parameters_version);
     o.put(nb);
+    o.put(nv);
     o.put(ap->background_weight);
-    o.put_n(ap->background_parameters, nb);
+    o.put_n(ap->background_parameters, nv);
     o.put_n(ap->background_step, nb);
     o.put_n(ap->background_min, nb);
     o.put_n(ap->background_max, nb);
@@ -329,7 +336,7 @@ extern "C" int mwsep_write_astronomy_parameters_binary(const char* path, const A
     const uint64_t sum = fnv1a(o.b.data(), o.b.size());
     FILE* f = fopen(path, "wb");
     if (!f) return mwsep_fail(MWSEP_ERR_IO);
-    bool ok = write_all(f, kParMagic, 8) && write_all(f, &kVersion, 4) && write_all(f, &body, 4) &&
+    bool ok = write_all(f, kParMagic, 8) && write_all(f, &kParVersion, 4) && write_all(f, &body, 4) &&
               write_all(f, o.b.data(), o.b.size()) && write_all(f, &sum, 8);
     if (fclose(f) != 0) ok = false;
     return ok ? MWSEP_OK : mwsep_fail(MWSEP_ERR_IO);
@@ -345,7 +352,7 @@ extern "C" int mwsep_read_astronomy_parameters_binary(const char* path, ASTRONOM
     char magic[8];
     uint32_t version = 0, body = 0;
     bool ok = fread(magic, 1, 8, f) == 8 && fread(&version, 4, 1, f) == 1 && fread(&body, 4, 1, f) == 1 &&
-              memcmp(magic, kParMagic, 8) == 0 && version == kVersion && body <= (1u << 26);
+              memcmp(magic, kParMagic, 8) == 0 && (version == 1 || version == kParVersion) && body <= (1u << 26);
     std::vector<unsigned char> buf;
     uint64_t sum = 0;
     if (ok)
@@ -360,9 +367,10 @@ extern "C" int mwsep_read_astronomy_parameters_binary(const char* path, ASTRONOM
     In in{buf.data(), buf.size()};
     ap->parameters_version = in.get<double>();
     const int nb = in.get<int>();
+    const int nv = version >= 2 ? in.get<int>() : nb;
     ap->background_weight = in.get<double>();
-    if (nb < 0 || nb > 1024) in.ok = false;
-    ap->background_parameters = in.get_n<double>(nb);
+    if (nb < 0 || nb > 1024 || nv < nb || nv > 1024) in.ok = false;
+    ap->background_parameters = in.get_n<double>(nv);
     ap->background_step = in.get_n<double>(nb);
     ap->background_min = in.get_n<double>(nb);
     ap->background_max = in.get_n<double>(nb);
@@ -407,6 +415,7 @@ extern "C" int mwsep_read_astronomy_parameters_binary(const char* path, ASTRONOM
     ap->convolve = in.get<int>();
     ap->sgr_coordinates = in.get<int>();
     ap->aux_bg_profile = in.get<int>();
+    if (ap->aux_bg_profile == 1 && nv < 7) in.ok = false;
     ap->wedge = in.get<int>();
     const int ni = in.get<int>();
     if (ni < 0 || ni > 1025) in.ok = false;

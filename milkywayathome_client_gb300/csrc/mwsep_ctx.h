@@ -142,6 +142,10 @@ struct Wedge
      * of this catalogue */
     DevBuf s_ptsdf;
     bool has_star_df = false;
+    /* the plain forms' FP64 star tables (r_point, qw, r_in_mag, r_in_mag2):
+     * built with the catalogue, or on the first plain-form read after an
+     * EvalFunc call's upload, which builds only what every form reads */
+    bool has_star_f64 = false;
     mwsep_stars_dev stars_view{};
     HostPinned h_stars;
 
@@ -213,10 +217,12 @@ void theta_consts(const ProblemHost& base, const double* theta, mwsep_theta_cons
 long env_long(const char* name, long dflt);
 /* (Re)build a wedge's problem tables from *ap. */
 int wedge_set_problem(mwsep_ctx* c, Wedge& w, const ASTRONOMY_PARAMETERS* ap);
-/* Upload a catalogue (SoA, host) and build its per-star tables. */
-/* Upload a catalogue and build its star tables on stream st. */
+/* Upload a catalogue (SoA, host) and build all its star tables on stream st. */
 int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double* b, const double* r,
                     cudaStream_t st);
+/* The plain forms' FP64 star tables on stream st, unless built (after the
+ * catalogue's upload in stream order). */
+int ensure_star_f64(mwsep_ctx* c, Wedge& w, cudaStream_t st);
 /* From STAR_POINTS rows: synchronously on the context's stream, or (on_side)
  * deferred to launch_star_build with stars_pending set (sp must stay valid
  * until then). */

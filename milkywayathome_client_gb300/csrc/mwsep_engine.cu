@@ -542,6 +542,13 @@ extern "C" int mwsep_ctx_evaluate_requests(mwsep_ctx* c, int n, const mwsep_requ
     if (rc) return mwsep_fail(rc);
     CU(cudaSetDevice(c->device));
     if (precision == MWSEP_PLAIN_DF) return evaluate_requests_df(c, n, reqs, out);
+    if (precision == MWSEP_PLAIN_F64)
+    {
+        /* the plain likelihood reads the FP64 star tables */
+        rc = wait_stars(c, c->stream);
+        for (int i = 0; i < n && !rc; ++i) rc = ensure_star_f64(c, *c->wedges[reqs[i].wedge], c->stream);
+        if (rc) return rc;
+    }
     rc = ensure_descriptors(c);
     if (rc) return rc;
     BatchShape shape;

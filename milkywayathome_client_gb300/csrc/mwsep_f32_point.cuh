@@ -1015,8 +1015,9 @@ __device__ __forceinline__ void star_density(const mwsep_stars_dev& St, const mw
     const int N = St.n_stars;
     Col<S> cc;
     s0 = (int)MWSEP_IDX(s0, N, 7);
-    /* the star's convolution points span [r_point[0], r_point[C-1]] */
-    const double ra = St.r_point[s0], rb = St.r_point[(size_t)(St.convolve - 1) * N + s0];
+    /* the star's convolution points span [r_0, r_{C-1}] (their float parts
+     * suffice: the range only places each stream's exponent shift) */
+    const double ra = St.pts[s0].x, rb = St.pts[(size_t)(St.convolve - 1) * N + s0].x;
     int eref[SArr<S>::N];
     column_consts_df<S, false, true>(St.geom + 4 * (size_t)s0, th, td, cc, eref, fmin(ra, rb), fmax(ra, rb));
     float bgf = 0.f, stf[SArr<S>::N];

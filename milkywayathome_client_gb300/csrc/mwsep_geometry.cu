@@ -12,6 +12,7 @@
 #include <math.h>
 #include "mwsep_internal.h"
 #include "mwsep_geometry.cuh"
+#include "mwsep_df.cuh"
 
 namespace {
 
@@ -66,28 +67,57 @@ __global__ void star_head_kernel(int n, const double* __restrict__ l, const doub
     }
 }
 
-/* Per (convolution point i = blockIdx.y, star): the tables at [i][s], one
- * thread each, so the launch is as wide as the table (the per-star loop over
- * the points left ~20 warps per SM on FP64 latency). */
-__global__ void star_points_kernel(int n, const double* __restrict__ dx, const double* __restrict__ nfac,
-                                   const double* __restrict__ head, const double* __restrict__ reff,
-                                   double* __restrict__ r_point, double* __restrict__ qw,
-                                   double* __restrict__ r_in_mag, double* __restrict__ r_in_mag2,
-                                   float4* __restrict__ pts)
+/* The plain forms' FP64 tables at [i][s] (convolution point i =
+ * blockIdx.y, one thread per star): r_point, qw_r3_N, r_in_mag,
+ * r_in_mag2.  Built when a plain form first reads them. */
+__global__ void star_f64_kernel(int n, const double* __restrict__ dx, const double* __restrict__ nfac,
+                                const double* __restrict__ head, double* __restrict__ r_point,
+                                double* __restrict__ qw, double* __restrict__ r_in_mag,
+                                double* __restrict__ r_in_mag2)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int i = blockIdx.y, C = gridDim.y;
     const double g = head[s] + dx[i];
     const double rp = head[(size_t)n + s] * nfac[i];
-    const double q = nfac[C + i] * (rp * rp * rp);
     const size_t o = (size_t)i * n + s;
     r_in_mag[o] = g;
     r_in_mag2[o] = g * g;
     r_point[o] = rp;
-    qw[o] = q;
-    const float hi = (float)rp;
-    pts[o] = make_float4(hi, (float)(rp - (double)hi), (float)(q * reff[s]), (float)g);
+    qw[o] = nfac[C + i] * (rp * rp * rp);
+}
+
+/* The compensated form's table pts[i][s] = {r_hi, r_lo, qw * reff, g}, one
+ * thread per star over its C points, in float pairs on the FP32 pipe (the
+ * FP64 tables took ~0.25 ms of FP64 work per 100k x 120 points): the same
+ * factors r = r' F_i, qw = wq_i r^3, g = g' + dx_i (r', g' per star from
+ * star_head_kernel; F_i = nfac[i], wq_i = nfac[C + i]), each rounded to
+ * float once from its pair (~2^-44 relative before the rounding).  kc holds
+ * the per-point pairs F_i, wq_i and dx_i, built by the block. */
+__global__ void star_pts_kernel(int n, int C, const double* __restrict__ dx, const double* __restrict__ nfac,
+                                const double* __restrict__ head, const double* __restrict__ reff,
+                                float4* __restrict__ pts)
+{
+    using namespace mwsep::dfl;
+    extern __shared__ float2 kc[]; /* [C] x {F, wq, dx} pairs */
+    for (int i = threadIdx.x; i < C; i += blockDim.x)
+    {
+        const df f = from_double(nfac[i]), w = from_double(nfac[C + i]), d = from_double(dx[i]);
+        kc[3 * i] = make_float2(f.hi, f.lo);
+        kc[3 * i + 1] = make_float2(w.hi, w.lo);
+        kc[3 * i + 2] = make_float2(d.hi, d.lo);
+    }
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const df rs = from_double(head[(size_t)n + s]), gs = from_double(head[s]), rf = from_double(reff[s]);
+    for (int i = 0; i < C; ++i)
+    {
+        const float2 f = kc[3 * i], w = kc[3 * i + 1], d = kc[3 * i + 2];
+        const df r = mul(rs, mk(f.x, f.y));
+        const df q = mul(mk(w.x, w.y), mul(sqr(r), r));
+        pts[(size_t)i * n + s] = make_float4(r.hi, r.lo, mul(q, rf).hi, add_fast(gs, mk(d.x, d.y)).hi);
+    }
 }
 
 } // namespace
@@ -105,17 +135,26 @@ extern "C" int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps
 }
 
 extern "C" int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
-                                        const double* dx, const double* nfac, double* geom, double* r_point,
-                                        double* qw, double* r_in_mag, double* r_in_mag2, double* reff, float4* pts,
-                                        double* head, void* stream)
+                                        const double* dx, const double* nfac, double* geom, double* reff,
+                                        float4* pts, double* head, void* stream)
 {
     if (n <= 0) return 0;
-    if (convolve < 1 || convolve > 65535) return (int)cudaErrorInvalidValue;
+    if (convolve < 1 || convolve > MWSEP_MAX_CONVOLVE) return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     int grid = (n + 127) / 128;
     if (grid > 152 * 32) grid = 152 * 32;
     star_head_kernel<<<grid, 128, 0, st>>>(n, l, b, r, geom, reff, head);
-    star_points_kernel<<<dim3((n + 255) / 256, convolve), 256, 0, st>>>(n, dx, nfac, head, reff, r_point, qw,
-                                                                         r_in_mag, r_in_mag2, pts);
+    star_pts_kernel<<<(n + 127) / 128, 128, (size_t)convolve * 3 * sizeof(float2), st>>>(n, convolve, dx, nfac, head,
+                                                                                        reff, pts);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mwsep_launch_star_f64(int n, int convolve, const double* dx, const double* nfac, const double* head,
+                                     double* r_point, double* qw, double* r_in_mag, double* r_in_mag2, void* stream)
+{
+    if (n <= 0) return 0;
+    if (convolve < 1 || convolve > MWSEP_MAX_CONVOLVE) return (int)cudaErrorInvalidValue;
+    star_f64_kernel<<<dim3((n + 255) / 256, convolve), 256, 0, (cudaStream_t)stream>>>(n, dx, nfac, head, r_point, qw,
+                                                                                      r_in_mag, r_in_mag2);
     return (int)cudaGetLastError();
 }

@@ -31,6 +31,7 @@
 #include "mwsep_ctx.h"
 #include "mwsep_geometry.cuh"
 #include "mwsep_internal.h"
+#include "mwsep_params.h"
 #include "mwsep_checks.cuh"
 #include "mwsep_status.h"
 
@@ -212,7 +213,6 @@ int check_problem(const ASTRONOMY_PARAMETERS* ap)
     if (ap->number_background_parameters < 4 || ap->number_background_parameters > MWSEP_MAX_BG_PARAMS)
         return MWSEP_ERR_UNSUPPORTED;
     if (ap->aux_bg_profile != 0 && ap->aux_bg_profile != 1) return MWSEP_ERR_UNSUPPORTED;
-    if (ap->aux_bg_profile == 1 && ap->number_background_parameters < 7) return MWSEP_ERR_UNSUPPORTED;
     if (ap->sgr_coordinates != 0 && ap->sgr_coordinates != 1) return MWSEP_ERR_UNSUPPORTED;
     if (ap->number_streams > 0 &&
         (ap->number_stream_parameters < 5 || ap->number_stream_parameters > MWSEP_MAX_STREAM_PARAMS))
@@ -242,6 +242,8 @@ void copy_problem(const ASTRONOMY_PARAMETERS* ap, ProblemHost& p)
         p.bg[i] = ap->background_parameters[i];
         p.bg_opt[i] = ap->background_optimize[i];
     }
+    /* the aux profile's a, b, c beyond the searched values */
+    for (int i = p.n_bg; i < mwsep_background_values(ap); ++i) p.bg[i] = ap->background_parameters[i];
     for (int s = 0; s < p.n_streams; ++s)
     {
         p.st_weight[s] = ap->stream_weights[s];
@@ -719,15 +721,17 @@ int prepare_stars(mwsep_ctx* c, Wedge& w, int n)
     w.n_stars = n;
     w.has_stars = true;
     w.has_star_df = false; /* rebuilt from these tables when first needed */
+    w.has_star_f64 = false;
     for (int prec = 0; prec < 3; ++prec)
         w.tune[prec].lk_grid = occupancy_grid(c, w.tune[prec].lk_block, n);
     return MWSEP_OK;
 }
 
 /* The catalogue's columns to the device and the star tables built from
- * them, on stream st (the build after event `after`, if given). */
+ * them, on stream st (the build after event `after`, if given); the plain
+ * forms' FP64 tables too when with_f64. */
 int upload_stars(mwsep_ctx* c, Wedge& w, const double* l, const double* b, const double* r, cudaStream_t st,
-                 cudaEvent_t after)
+                 cudaEvent_t after, bool with_f64)
 {
     const size_t bytes = (size_t)w.n_stars * 8;
     CU(h2d(c, w.s_l.p, l, bytes, st));
@@ -736,9 +740,19 @@ int upload_stars(mwsep_ctx* c, Wedge& w, const double* l, const double* b, const
     if (after) CU(cudaStreamWaitEvent(st, after, 0));
     CK(mwsep_launch_star_tables(w.n_stars, w.s_l.as<double>(), w.s_b.as<double>(), w.s_r.as<double>(),
                                 w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(), w.s_geom.as<double>(),
-                                w.s_r_point.as<double>(), w.s_qw.as<double>(), w.s_r_in_mag.as<double>(),
-                                w.s_r_in_mag2.as<double>(), w.s_reff.as<double>(), w.s_pts.as<float4>(),
-                                w.s_head.as<double>(), st));
+                                w.s_reff.as<double>(), w.s_pts.as<float4>(), w.s_head.as<double>(), st));
+    w.has_star_f64 = false;
+    return with_f64 ? ensure_star_f64(c, w, st) : MWSEP_OK;
+}
+
+int ensure_star_f64(mwsep_ctx* c, Wedge& w, cudaStream_t st)
+{
+    (void)c;
+    if (w.has_star_f64 || !w.has_stars) return MWSEP_OK;
+    CK(mwsep_launch_star_f64(w.n_stars, w.prob.convolve, w.d_dx.as<double>(), w.d_nfac.as<double>(),
+                             w.s_head.as<double>(), w.s_r_point.as<double>(), w.s_qw.as<double>(),
+                             w.s_r_in_mag.as<double>(), w.s_r_in_mag2.as<double>(), st));
+    w.has_star_f64 = true;
     return MWSEP_OK;
 }
 
@@ -748,7 +762,7 @@ int wedge_set_stars(mwsep_ctx* c, Wedge& w, int n, const double* l, const double
     mwsep::Range nvtx_range("mwsep.set_stars");
     int rc = prepare_stars(c, w, n);
     if (rc) return rc;
-    return upload_stars(c, w, l, b, r, st, nullptr);
+    return upload_stars(c, w, l, b, r, st, nullptr, true);
 }
 
 /* STAR_POINTS rows (l, b, r) into the wedge's pinned staging columns. */
@@ -824,7 +838,9 @@ int launch_star_build(mwsep_ctx* c, cudaEvent_t after)
     gather_rows(w, sp);
     const double* l = w.h_stars.as<double>();
     const size_t n = (size_t)w.n_stars;
-    int rc = upload_stars(c, w, l, l + n, l + 2 * n, c->side, after);
+    /* the tables every form reads; a plain form builds its FP64 ones on
+     * its first read (ensure_star_f64) */
+    int rc = upload_stars(c, w, l, l + n, l + 2 * n, c->side, after, false);
     if (rc) return rc;
     CU(cudaEventRecord(c->ev_stars, c->side));
     return MWSEP_OK;
@@ -942,6 +958,7 @@ void wedge_release(mwsep_ctx* c, Wedge& w)
                       &w.s_r_in_mag, &w.s_r_in_mag2, &w.s_reff, &w.s_pts, &w.s_ptsdf, &w.s_head};
     for (DevBuf* b : bufs) b->release(t);
     w.has_star_df = false;
+    w.has_star_f64 = false;
     w.h_stars.release();
     w.bytes = 0;
     w.has_problem = w.has_stars = false;
@@ -1204,6 +1221,11 @@ int evaluate_wedge(mwsep_ctx* c, int wid, int B, const double* thetas, int preci
         /* from here on the star tables are read */
         rc = wait_stars(c, st);
         if (rc) return rc;
+        if (precision != MWSEP_MIXED_F32)
+        {
+            rc = ensure_star_f64(c, w, st);
+            if (rc) return rc;
+        }
         if (df_likelihood && !w.has_star_df)
         {
             CK(mwsep_launch_star_df_table(w.n_stars, p.convolve, w.stars_view.r_point, w.stars_view.qw,

@@ -423,12 +423,15 @@ int mwsep_engine_reduce(int phase, const mwsep_engine_args* a, int grid, void* s
 /* Launchers (defined in the .cu files).  All return cudaError_t as int. */
 int mwsep_launch_geometry(double mu_min, double mu_step, int mu_steps, const double* nus, int nu_steps,
                           int sgr, int wedge, double* geom_out, void* stream);
-/* nfac: [C] 10^(dx_n/5), then [C] gl_w_n coeff e^{-dx_n^2 / 2 sigma^2};
- * head: 2n doubles of scratch (per-star values between the two launches) */
+/* The star tables every form reads (geom, reff, the compensated form's
+ * pts) and head, 2n doubles per star (g', the distance factor) from which
+ * mwsep_launch_star_f64 later builds the plain forms' FP64 tables.  nfac:
+ * [C] 10^(dx_n/5), then [C] gl_w_n coeff e^{-dx_n^2 / 2 sigma^2}. */
 int mwsep_launch_star_tables(int n, const double* l, const double* b, const double* r, int convolve,
-                             const double* dx, const double* nfac, double* geom, double* r_point, double* qw,
-                             double* r_in_mag, double* r_in_mag2, double* reff, float4* pts, double* head,
-                             void* stream);
+                             const double* dx, const double* nfac, double* geom, double* reff, float4* pts,
+                             double* head, void* stream);
+int mwsep_launch_star_f64(int n, int convolve, const double* dx, const double* nfac, const double* head,
+                          double* r_point, double* qw, double* r_in_mag, double* r_in_mag2, void* stream);
 int mwsep_launch_integral_f64(const mwsep_area_dev* area, const mwsep_theta_consts* th_dev,
                               const mwsep_launch_shape* shape, double2* partials, void* stream);
 int mwsep_launch_likelihood_f64(const mwsep_stars_dev* st, const mwsep_theta_consts* th_dev,

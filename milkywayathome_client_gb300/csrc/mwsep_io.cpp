@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "milkyway_separation_gb300.h"
+#include "mwsep_params.h"
 #include "mwsep_status.h"
 
 namespace {
@@ -192,6 +193,7 @@ extern "C" int mwsep_read_astronomy_parameters(const char* path, ASTRONOMY_PARAM
     std::vector<double> v;
     const char* s;
     int rc = MWSEP_ERR_IO;
+    size_t n_bg_values = 0;
 
     s = L.take("parameters_version");
     ap->parameters_version = s ? strtod(s, nullptr) : 0.01;
@@ -201,16 +203,23 @@ extern "C" int mwsep_read_astronomy_parameters(const char* path, ASTRONOMY_PARAM
     if (!(s = L.take("background_weight"))) goto fail;
     ap->background_weight = strtod(s, nullptr);
 
+    /* Each array is as long as its own bracket says (util/io_util.c:55-71);
+     * number_parameters counts the leading values the search maps.  One of
+     * the reference's test files (astronomy_parameters-79-aux.txt) lists
+     * seven background values, the aux profile's three among them, under
+     * number_parameters 4. */
+    if (ap->number_background_parameters < 0) goto fail;
     if (!L.take_array("background_parameters", v)) goto fail;
-    if ((int)v.size() != ap->number_background_parameters) goto fail;
+    if (v.size() < (size_t)ap->number_background_parameters) goto fail;
+    n_bg_values = v.size();
     ap->background_parameters = dup_array<double>(v);
-    if (!L.take_array("background_step", v)) goto fail;
+    if (!L.take_array("background_step", v) || v.size() < (size_t)ap->number_background_parameters) goto fail;
     ap->background_step = dup_array<double>(v);
-    if (!L.take_array("background_min", v)) goto fail;
+    if (!L.take_array("background_min", v) || v.size() < (size_t)ap->number_background_parameters) goto fail;
     ap->background_min = dup_array<double>(v);
-    if (!L.take_array("background_max", v)) goto fail;
+    if (!L.take_array("background_max", v) || v.size() < (size_t)ap->number_background_parameters) goto fail;
     ap->background_max = dup_array<double>(v);
-    if (!L.take_array("optimize_parameter", v)) goto fail;
+    if (!L.take_array("optimize_parameter", v) || v.size() < (size_t)ap->number_background_parameters) goto fail;
     ap->background_optimize = dup_array<int>(v);
 
     {
@@ -267,6 +276,9 @@ extern "C" int mwsep_read_astronomy_parameters(const char* path, ASTRONOMY_PARAM
         if (!(s = L.take("aux_bg_profile"))) goto fail;
         ap->aux_bg_profile = atoi(s);
     }
+    /* the aux profile reads background values 4..6 (init_constants,
+     * cpu/evaluation_optimized.c:72-77) */
+    if (ap->aux_bg_profile == 1 && n_bg_values < 7) goto fail;
     if (!(s = L.take("wedge"))) goto fail;
     ap->wedge = atoi(s);
 
@@ -312,7 +324,9 @@ extern "C" int mwsep_write_astronomy_parameters(const char* path, const ASTRONOM
     fprintf(f, "parameters_version: %lf\n", ap->parameters_version);
     fprintf(f, "number_parameters: %d\n", ap->number_background_parameters);
     fprintf(f, "background_weight: %lf\n", ap->background_weight);
-    fwrite_doubles(f, "background_parameters", ap->number_background_parameters, ap->background_parameters);
+    /* the aux profile's values 4..6 are written even where
+     * number_parameters counts fewer (the reader's file form) */
+    fwrite_doubles(f, "background_parameters", mwsep_background_values(ap), ap->background_parameters);
     fwrite_doubles(f, "background_step", ap->number_background_parameters, ap->background_step);
     fwrite_doubles(f, "background_min", ap->number_background_parameters, ap->background_min);
     fwrite_doubles(f, "background_max", ap->number_background_parameters, ap->background_max);

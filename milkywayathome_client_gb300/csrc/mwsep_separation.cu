@@ -263,6 +263,9 @@ extern "C" int mwsep_ctx_separation(mwsep_ctx* c, const double* theta, unsigned 
     int* d_as = c->d_assign.as<int>();
     double* d_xyz = xyz ? c->d_xyz.as<double>() : nullptr;
     cudaStream_t st = c->stream;
+    int rc3 = wait_stars(c, st);
+    if (!rc3) rc3 = ensure_star_f64(c, w, st);
+    if (rc3) return rc3;
     if (S <= 1)
         separation_kernel<1><<<grid, 256, 0, st>>>(w.stars_view, d_th, d_ints, sc, d_sp, d_as, d_xyz);
     else if (S <= 2)

@@ -22,7 +22,10 @@ writes travels with the repository:
   --slices     golden_slices.json beside the small synthetic cases config0
                and cut_area: every rank of a 3-way split.
   --large ID   tests/golden/reference_large/<ID>/ for the reference's large
-               fixture tests/astronomy_parameters-<ID>.txt (1600 x 640 x 1400
+               fixture tests/astronomy_parameters-<ID>.txt (ID 86, 12, 79 and
+               the -aux files of 79, 86, 11, 12, with the theta of the small
+               ones -- but 79-aux, whose number_parameters 4 leaves its aux
+               values out of the search, takes test 79's; 1600 x 640 x 1400
                cells, ~1.7e11 points; the star file is the small fixture's):
                the reference's distributed evaluation over 8 ranks -- each
                rank's slice integrated by the reference, the slices summed in
@@ -182,7 +185,13 @@ def make_config(k, work):
         print(f"config{k}", r["likelihood"], r["wall_s"], "s", flush=True)
 
 
-LARGE = {"86": ("86", "86", TEST_86), "12": ("12", "12", PARAM_SET1), "79": ("79", "79", TEST_79)}
+LARGE = {"86": ("86", "86", TEST_86), "12": ("12", "12", PARAM_SET1), "79": ("79", "79", TEST_79),
+         # number_parameters 4 over seven background values: the aux a, b, c
+         # are read from the file, the theta is the plain test's
+         "79-aux": ("79-aux", "79", TEST_79),
+         "86-aux": ("86-aux", "86", TEST_86[:2] + AUX_ABC + TEST_86[2:]),
+         "11-aux": ("11-aux", "11", PARAM_SET1[:2] + AUX_ABC + PARAM_SET1[2:]),
+         "12-aux": ("12-aux", "12", PARAM_SET1[:2] + AUX_ABC + PARAM_SET1[2:])}
 
 
 def make_large(fid, nranks=8):

@@ -10,7 +10,7 @@ import pytest
 
 import milkywayathome_client_gb300 as mw
 from milkywayathome_client_gb300 import native as N
-from conftest import REFERENCE_DIR, golden_cases, load_case
+from conftest import CASES, GOLDEN, REFERENCE_DIR, golden_cases, load_case
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -56,6 +56,42 @@ def test_reads_reference_fixtures(built_library, fname, count, areas):
     ap = mw.AstronomyParameters.read(os.path.join(REFERENCE_DIR, "tests", fname))
     assert ap.optimized_parameter_count == count
     assert ap.number_integrals == areas
+
+
+def _background(ap, n):
+    return [ap.struct.background_parameters[i] for i in range(n)]
+
+
+def test_aux_values_beyond_number_parameters(built_library, oracle_built, tmp_path):
+    """The reference's astronomy_parameters-79-aux.txt lists seven background
+    values under number_parameters 4: the search maps four of them (8
+    parameters in all) and the aux profile reads values 4..6, as
+    init_constants does; both writers keep the seven."""
+    pf = os.path.join(GOLDEN, "reference_large", "79-aux", "params.txt")
+    ap = mw.AstronomyParameters.read(pf)
+    assert ap.struct.number_background_parameters == 4 and ap.struct.aux_bg_profile == 1
+    assert ap.optimized_parameter_count == 8
+    assert _background(ap, 7)[4:] == [100.0, 50.0, 25.0]
+    assert oracle_built.Oracle(pf, os.path.join(CASES, "config0", "stars.txt")).n_theta == 8
+    t = tmp_path / "p.txt"
+    ap.write(str(t))
+    back = mw.AstronomyParameters.read(str(t))
+    assert back.struct.number_background_parameters == 4 and _background(back, 7) == _background(ap, 7)
+    b = tmp_path / "p.mwsp"
+    ap.write_binary(str(b))
+    back = mw.AstronomyParameters.read_binary(str(b))
+    assert back.struct.number_background_parameters == 4 and _background(back, 7) == _background(ap, 7)
+    # an aux profile without its three values is refused
+    lines = []
+    for line in open(pf).read().splitlines():
+        key, _, vals = line.partition(": ")
+        if key.endswith("[7]") and not lines[-1].startswith("number_streams"):
+            line = key.replace("[7]", "[4]") + ": " + ", ".join(vals.split(", ")[:4])
+        lines.append(line)
+    bad = tmp_path / "short.txt"
+    bad.write_text("\n".join(lines) + "\n")
+    with pytest.raises(mw.MwsepError):
+        mw.AstronomyParameters.read(str(bad))
 
 
 def test_theta_layout(built_library):
