@@ -10,10 +10,10 @@ sources; tests/golden/make_scale_golden.py):
     stars) at its base theta and four population members;
   * benchmark config 1 (1600 x 640 x 140 cells, convolve 120, 3 streams, 100k
     stars: 1.72e10 density points) at its base theta;
-  * the reference's large fixtures tests/astronomy_parameters-{86,12}.txt
-    (1600 x 640 x 1400 cells, convolve 120; 86 with an 800 x 320 x 700 cut:
-    1.7e11 to 1.9e11 points), the golden being the reference's own
-    distributed evaluation over 8 ranks.
+  * the reference's large fixtures tests/astronomy_parameters-{79,86,12}.txt
+    and the -aux files of 79, 86, 11, 12 (1600 x 640 x 1400 cells, convolve
+    120; 86 with an 800 x 320 x 700 cut: 1.7e11 to 1.9e11 points), the
+    golden being the reference's own distributed evaluation over 8 ranks.
 
 Bounds, per form:
   MWSEP_PLAIN_F64, MWSEP_PLAIN_DF  1e-12 relative on every area integral,
