@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the population-batch and serving measurements")
+    ap.add_argument("--extras", default="population,mixed,serving,catalogue",
+                    help="comma list of the extra measurements to run (population, mixed, serving, catalogue)")
     ap.add_argument("--workload", type=int, default=CONFIG_INDEX, choices=[0, 1, 2],
                     help="benchmark config of the single-evaluation steps (default 1, the full-size wedge; "
                          "0 and 2 are smaller wedges, for profiling runs)")
@@ -462,13 +464,18 @@ def run_gb300_arm(args, ws, rank, local):
         out["dlogL_mixed_vs_oracle"] = r32.likelihood - golden["likelihood"]
     if clk:
         out["clocks"] = clk
-    if rank == 0 and not args.no_extras:
+    extras = set() if args.no_extras else {e.strip() for e in args.extras.split(",") if e.strip()}
+    if rank == 0 and extras:
         ctx.close()
         ctx = None
-        out["population_batch"] = population_batch(args)
-        out["mixed_size_batch"] = mixed_size_batch(args)
-        out["serving"] = serving(args)
-        out["catalogue_load"] = catalogue_load(args, files)
+        if "population" in extras:
+            out["population_batch"] = population_batch(args)
+        if "mixed" in extras:
+            out["mixed_size_batch"] = mixed_size_batch(args)
+        if "serving" in extras:
+            out["serving"] = serving(args)
+        if "catalogue" in extras:
+            out["catalogue_load"] = catalogue_load(args, files)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         n = min(host_cores(), 64)
         cw, kind, _ = cpu_sample(files, theta, n)
