@@ -697,7 +697,10 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
     const Tune saved = w.tune[precision];
     const int cls = stream_group(w.prob.n_streams);
     const int waves = 6;
-    const long long resident = (long long)c->sm_count * blocks_per_sm(precision, 0, cls);
+    /* concurrent takers of integral tiles: warps for the compensated engine,
+     * blocks for the plain one */
+    const long long resident = (long long)c->sm_count * blocks_per_sm(precision, 0, cls) *
+                               (precision == MWSEP_MIXED_F32 ? saved.block / 32 : 1);
     std::vector<int> kcs;
     if (saved.warp_items)
     {
@@ -717,10 +720,12 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
             if (kcs.empty() || kcs.back() != kc) kcs.push_back(kc);
             if (kc == 1) break;
         }
-    /* items per engine tile: thread items per block thread, or warp tiles
-     * per warp of a block */
+    /* items per engine tile: the compensated engine gives a tile to one
+     * warp (warp tiles, or thread items per lane), the plain engine to a
+     * block (thread items per thread) */
     const int tile_mult[3] = {2, 8, 32};
-    const int warp_mult[3] = {1, 4, 16};
+    const int warp_tiles[3] = {2, 4, 8};
+    const int tile_threads = precision == MWSEP_MIXED_F32 ? 32 : saved.block;
     double best = 1e300;
     Tune best_t = saved;
     for (int kc : kcs)
@@ -730,7 +735,7 @@ extern "C" int mwsep_ctx_autotune(mwsep_ctx* c, int id, int precision, double* p
             Tune& t = w.tune[precision];
             t = saved;
             t.k_chunk = kc;
-            t.tile_items = saved.warp_items ? (t.block / 32) * warp_mult[mi] : t.block * tile_mult[mi];
+            t.tile_items = saved.warp_items ? warp_tiles[mi] : tile_threads * tile_mult[mi];
             ++w.tune_gen;
             c->eng.desc_dirty = true;
             int rc = ensure_descriptors(c);

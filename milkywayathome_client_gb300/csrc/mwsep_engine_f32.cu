@@ -1,10 +1,11 @@
 /* mwsep_engine_f32.cu -- compensated-FP32 kernels of the tiled engine.
  *
  * One persistent launch evaluates every request of a batch, whatever wedge
- * each names: blocks take (request, area, item-run) tiles from a global
- * counter, so uneven wedges balance themselves, and each tile writes its own
- * partial slot, so a request's result does not depend on which block ran
- * which tile or what else was in the batch.  Per tile the block dispatches on
+ * each names: warps (integrals) and blocks (likelihood) take (request, area,
+ * item-run) tiles from a global counter, so uneven wedges balance
+ * themselves, and each tile writes its own partial slot, so a request's
+ * result does not depend on which warp ran which tile or what else was in
+ * the batch.  Per tile the block dispatches on
  * the request's stream count and background form to the same specialised
  * density code as the single-wedge kernels (mwsep_f32_point.cuh).
  */
@@ -19,19 +20,33 @@ using namespace mwsep::f32;
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ void load_area(mwsep_area_dev& dst, const mwsep_area_dev* src)
+/* 8-byte words from src to dst by the 32 lanes of a warp */
+__device__ __forceinline__ void warp_copy(void* dst, const void* src, int bytes)
 {
-    static_assert(sizeof(mwsep_area_dev) % 8 == 0, "area descriptor must be 8-byte sized");
+    static_assert(sizeof(mwsep_area_dev) % 8 == 0 && sizeof(mwsep_theta_consts) % 8 == 0,
+                  "descriptors are copied in 8-byte words");
     const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
-    unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(mwsep_area_dev) / 8); i += blockDim.x) d[i] = s[i];
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+    for (int i = threadIdx.x & 31; i < bytes / 8; i += 32) d[i] = s[i];
 }
 
-/* cs: the block's column-constant scratch, kTileCols * ColWords<S>::N floats
- * per warp (used by warp-tile items). */
+/* A warp's shared memory in the integral kernel: the column constants of its
+ * current warp tile, and its integral tile's theta, area and theta pairs. */
+template <int S>
+struct WarpSlot
+{
+    __align__(16) float cs[TileSmem<S>::N];
+    mwsep_theta_consts th;
+    mwsep_area_dev A;
+    ThetaDF<S> td;
+};
+
+/* One integral tile by one warp: its warp tiles in order (or its thread
+ * items, the lanes striding), then the lanes' sums added across the warp in
+ * a fixed order into the tile's slot. */
 template <int S, int FORM>
 __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta_consts& th, const ThetaDF<S>& td,
-                                      const mwsep_itile& t, double* red, float* cs, double2* out)
+                                      const mwsep_itile& t, float* cs, double2* out)
 {
     double acc[1 + S];
 #pragma unroll
@@ -39,33 +54,38 @@ __device__ __forceinline__ void itile(const mwsep_area_dev& A, const mwsep_theta
     const BgConsts bc = bg_consts(th);
     if (A.warp_items)
     {
-        const int warp = threadIdx.x >> 5;
-        float* mine = cs + warp * TileSmem<S>::N;
-        for (long long wt = t.item_begin + warp; wt < t.item_end; wt += blockDim.x >> 5)
+        for (long long wt = t.item_begin; wt < t.item_end; ++wt)
         {
             if constexpr (PackedTile<S>::ok)
-                warp_tile2<S, FORM>(A, th, td, bc, wt, mine, acc);
+                warp_tile2<S, FORM>(A, th, td, bc, wt, cs, acc);
             else
-                warp_tile<S, FORM>(A, th, td, bc, wt, mine, acc);
+                warp_tile<S, FORM>(A, th, td, bc, wt, cs, acc);
         }
     }
     else
-        for (long long item = t.item_begin + threadIdx.x; item < t.item_end; item += blockDim.x)
+        for (long long item = t.item_begin + (threadIdx.x & 31); item < t.item_end; item += 32)
             integral_item<S, FORM>(A, th, bc, item, acc);
-    reduce_and_store<1 + S>(acc, 1 + th.n_streams, red, out);
+#pragma unroll
+    for (int k = 0; k < 1 + S; ++k)
+        for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+    if ((threadIdx.x & 31) == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 1 + S; ++k)
+            if (k < 1 + th.n_streams) out[k] = make_double2(acc[k], 0.0);
+    }
 }
 
 template <int S>
 __device__ __forceinline__ void itile_form(const mwsep_area_dev& A, const mwsep_theta_consts& th,
-                                           const ThetaDF<S>& td, const mwsep_itile& t, double* red, float* cs,
-                                           double2* out)
+                                           const ThetaDF<S>& td, const mwsep_itile& t, float* cs, double2* out)
 {
     switch (mwsep_bg_form(&th))
     {
-    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, td, t, red, cs, out); break;
-    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, td, t, red, cs, out); break;
-    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, td, t, red, cs, out); break;
-    default: itile<S, BG_NONE>(A, th, td, t, red, cs, out); break;
+    case BG_HERNQUIST: itile<S, BG_HERNQUIST>(A, th, td, t, cs, out); break;
+    case BG_HERNQUIST_AUX: itile<S, BG_HERNQUIST_AUX>(A, th, td, t, cs, out); break;
+    case BG_GENERAL: itile<S, BG_GENERAL>(A, th, td, t, cs, out); break;
+    default: itile<S, BG_NONE>(A, th, td, t, cs, out); break;
     }
 }
 
@@ -78,31 +98,38 @@ struct GroupS
 };
 
 template <int G>
+constexpr size_t integral_smem()
+{
+    return sizeof(WarpSlot<GroupS<G>::S>) * (kBlock / 32);
+}
+
+/* Each warp takes integral tiles from the group's counter on its own (a
+ * block-wide tile waited at its end for its slowest warp: a half-width
+ * warp tile at a wedge's mu edge left the other seven warps of the block
+ * idle for half a tile), with its tile's theta and area in its own slot of
+ * shared memory. */
+template <int G>
 __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mwsep_engine_args a)
 {
     constexpr int S = GroupS<G>::S;
-    __shared__ mwsep_theta_consts th;
-    __shared__ ThetaDF<S> td;
-    __shared__ mwsep_area_dev A;
-    __shared__ double red[2 * (1 + S) * 32];
-    __shared__ __align__(16) float cs[(kBlock / 32) * TileSmem<S>::N];
-    __shared__ int s_tile;
+    extern __shared__ __align__(16) unsigned char smem[];
+    WarpSlot<S>& ws = reinterpret_cast<WarpSlot<S>*>(smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
     const int n_tiles = a.counters[4 * G + 2];
     for (;;)
     {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.counters[4 * G + 0], 1);
-        __syncthreads();
-        const int t = s_tile;
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&a.counters[4 * G + 0], 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n_tiles) break;
         const mwsep_itile tile = a.itiles[t];
-        load_theta(th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10));
-        load_area(A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11));
-        __syncthreads();
-        if (threadIdx.x == 0) theta_df<S>(th, td);
-        __syncthreads();
-        double2* out = a.ipart + (size_t)t * MWSEP_ENG_ICOMP;
-        itile_form<S>(A, th, td, tile, red, cs, out);
-        __syncthreads();
+        warp_copy(&ws.th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10), sizeof(mwsep_theta_consts));
+        warp_copy(&ws.A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11), sizeof(mwsep_area_dev));
+        __syncwarp();
+        if (lane == 0) theta_df<S>(ws.th, ws.td);
+        __syncwarp();
+        itile_form<S>(ws.A, ws.th, ws.td, tile, ws.cs, a.ipart + (size_t)t * MWSEP_ENG_ICOMP);
+        __syncwarp();
     }
 }
 
@@ -157,11 +184,24 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
 
 namespace {
 
+/* the integral kernel's per-warp slots can pass the 48 KB of a default
+ * launch (four streams: ~53 KB per block) */
+template <int G>
+cudaError_t integral_smem_attr()
+{
+    static_assert(integral_smem<G>() <= 100 * 1024, "two blocks per SM must fit in shared memory");
+    return cudaFuncSetAttribute(engine_integral_f32_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)integral_smem<G>());
+}
+
 template <int G>
 void launch_group(int phase, const mwsep_engine_args* a, int grid, cudaStream_t st)
 {
     if (phase == 0)
-        engine_integral_f32_kernel<G><<<grid, kBlock, 0, st>>>(*a);
+    {
+        if (integral_smem_attr<G>() != cudaSuccess) return;
+        engine_integral_f32_kernel<G><<<grid, kBlock, integral_smem<G>(), st>>>(*a);
+    }
     else
         engine_likelihood_f32_kernel<G><<<grid, kBlock, 0, st>>>(*a);
 }
@@ -169,8 +209,11 @@ void launch_group(int phase, const mwsep_engine_args* a, int grid, cudaStream_t 
 template <int G>
 cudaError_t group_occupancy(int* b, int phase)
 {
-    return phase == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_integral_f32_kernel<G>, kBlock, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_likelihood_f32_kernel<G>, kBlock, 0);
+    if (phase != 0)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_likelihood_f32_kernel<G>, kBlock, 0);
+    const cudaError_t e = integral_smem_attr<G>();
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(b, engine_integral_f32_kernel<G>, kBlock, integral_smem<G>());
 }
 
 } // namespace

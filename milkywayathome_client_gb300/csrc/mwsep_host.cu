@@ -526,7 +526,9 @@ void default_tune(mwsep_ctx* c, Wedge& w)
             t.grid = (int)std::max<long long>(1, g);
             t.lk_block = 256;
             t.lk_grid = occupancy_grid(c, t.lk_block, std::max(w.n_stars, 1));
-            t.tile_items = 8 * 4; /* engine: 4 warp tiles per warp of a block */
+            /* engine: warp tiles per integral tile (the compensated engine
+             * hands a tile to one warp) */
+            t.tile_items = prec == MWSEP_MIXED_F32 ? 4 : 8 * 4;
             t.tile_stars = 1024;
             t.tuned = false;
             continue;
@@ -542,7 +544,9 @@ void default_tune(mwsep_ctx* c, Wedge& w)
         t.grid = (int)std::max<long long>(1, g);
         t.lk_block = 256;
         t.lk_grid = occupancy_grid(c, t.lk_block, std::max(w.n_stars, 1));
-        t.tile_items = t.block * 8;
+        /* engine: thread items per integral tile (the compensated engine's
+         * tiles go to one warp, the plain engine's to a block) */
+        t.tile_items = (prec == MWSEP_MIXED_F32 ? 32 : t.block) * 8;
         t.tile_stars = 1024;
         t.tuned = false;
     }
