@@ -35,6 +35,12 @@ int mwsep_device_checks(int device, int* enabled, unsigned long long* failures, 
  * FP64 integral kernel's own table-driven exponential and Newton-Raphson
  * reciprocal, in plain FP64. */
 int mwsep_df_eval(int device, int op, int n, const double* x, const double* y, const double* z, double* out);
+/* The compensated likelihood's log10 sum (a mantissa product and an exponent
+ * sum, log10 taken once) over host values x[0..n) on `device`, in one block
+ * with the likelihood kernels' fixed-order combination: *out = sum of
+ * log10(x[i]) with log10's semantics per term (0 gives -inf, a negative or
+ * NaN term NaN, +inf +inf).  Synchronous. */
+int mwsep_log10_sum_eval(int device, int n, const double* x, double* out);
 
 /* The launch model behind the compensated form's default r-chunk (host only,
  * no device needed; no reference counterpart).  mwsep_model_tile_cost: the

@@ -8,6 +8,7 @@
  */
 #include <cuda_runtime.h>
 #include <math.h>
+#include "milkyway_separation_gb300_test.h"
 #include "mwsep_internal.h"
 #include "mwsep_reduce.cuh"
 #include "mwsep_f32_point.cuh"
@@ -314,7 +315,43 @@ int launch_finish(int n_stars, const mwsep_theta_consts* th, const mwsep_launch_
     return (int)cudaGetLastError();
 }
 
+/* mwsep_log10_sum_eval's kernel: one block, each thread a strided share */
+__global__ void __launch_bounds__(kBlock) log10_sum_kernel(int n, const double* __restrict__ x,
+                                                           double2* __restrict__ out)
+{
+    __shared__ Log10Sum red[LkSmem<0, kBlock>::N];
+    LkAcc<0> acc;
+    acc.init();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lsum_add(acc.c[0], x[i]);
+    lk_block_store<0>(acc, 3, red, out);
+}
+
 } // namespace
+
+extern "C" int mwsep_log10_sum_eval(int device, int n, const double* x, double* out)
+{
+    if (n < 0 || !out || (n > 0 && !x)) return MWSEP_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return MWSEP_ERR_CUDA;
+    double* d = nullptr;
+    if (cudaMalloc(&d, ((size_t)n + 8) * sizeof(double)) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return MWSEP_ERR_NOMEM;
+    }
+    double2* o = reinterpret_cast<double2*>(d + n + (n & 1)); /* 16-byte aligned after x */
+    cudaError_t e = n > 0 ? cudaMemcpy(d, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) : cudaSuccess;
+    if (e == cudaSuccess)
+    {
+        log10_sum_kernel<<<1, kBlock>>>(n, d, o);
+        e = cudaGetLastError();
+    }
+    double2 h[1];
+    if (e == cudaSuccess) e = cudaMemcpy(h, o, sizeof(double2), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MWSEP_ERR_CUDA;
+    *out = h[0].x;
+    return MWSEP_OK;
+}
 
 namespace {
 

@@ -185,6 +185,7 @@ _SIGS = {
     "mwsep_device_checks": (C.c_int, [C.c_int, _P(C.c_int), _P(C.c_ulonglong), _P(C.c_ulonglong)]),
     "mwsep_df_eval": (C.c_int, [C.c_int, C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double),
                                 _P(C.c_double)]),
+    "mwsep_log10_sum_eval": (C.c_int, [C.c_int, C.c_int, _P(C.c_double), _P(C.c_double)]),
     "mwsep_read_astronomy_parameters": (C.c_int, [C.c_char_p, _P(ASTRONOMY_PARAMETERS)]),
     "mwsep_write_astronomy_parameters": (C.c_int, [C.c_char_p, _P(ASTRONOMY_PARAMETERS)]),
     "mwsep_free_parameters": (None, [_P(ASTRONOMY_PARAMETERS)]),
