@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kBlock, 2) engine_integral_f32_kernel(const mw
         warp_copy(&ws.th, a.thetas + MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10), sizeof(mwsep_theta_consts));
         warp_copy(&ws.A, a.areas + MWSEP_IDX(tile.area_desc, a.n_area_desc, 11), sizeof(mwsep_area_dev));
         __syncwarp();
-        if (lane == 0) theta_df<S>(ws.th, ws.td);
+        theta_df_part<S>(ws.th, ws.td, lane);
         __syncwarp();
         itile_form<S>(ws.A, ws.th, ws.td, tile, ws.cs, a.ipart + (size_t)t * MWSEP_ENG_ICOMP);
         __syncwarp();
@@ -168,11 +168,8 @@ __global__ void __launch_bounds__(kBlock, 2) engine_likelihood_f32_kernel(const 
         const mwsep_stars_dev St =
             a.stars[MWSEP_IDX(a.reqs[MWSEP_IDX(tile.req, a.counters[MWSEP_ENG_NREQ], 10)].stars, a.n_star_desc, 12)];
         const double* I = a.out + (size_t)tile.req * MWSEP_ENG_OUT_STRIDE + MWSEP_ENG_OUT_INTS;
-        if (threadIdx.x == 0)
-        {
-            lk_scale<S>(th, I, ks);
-            theta_df<S>(th, td);
-        }
+        if (threadIdx.x == 0) lk_scale<S>(th, I, ks);
+        theta_df_part<S>(th, td, (int)threadIdx.x - 32);
         __syncthreads();
         double2* out = a.lpart + (size_t)t * MWSEP_ENG_LCOMP;
         ltile<S>(St, th, td, ks, tile, red, out);

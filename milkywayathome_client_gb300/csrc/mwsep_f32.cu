@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     if (mwsep_bg_form(&th) != FORM) return;
-    if (threadIdx.x == 0) theta_df<S>(th, td);
+    theta_df_part<S>(th, td, (int)threadIdx.x);
     __syncthreads();
 
     double acc[1 + S];
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_dyn_kern
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     if (mwsep_bg_form(&th) != FORM) return;
-    if (threadIdx.x == 0) theta_df<S>(th, td);
+    theta_df_part<S>(th, td, (int)threadIdx.x);
     __syncthreads();
     const BgConsts bc = bg_consts(th);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -150,11 +150,8 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_kernel(const mwsep_star
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
     const int NS = th.n_streams;
-    if (threadIdx.x == 0)
-    {
-        lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
-        theta_df<S>(th, td);
-    }
+    if (threadIdx.x == 0) lk_scale<S>(th, integrals + (size_t)blockIdx.y * (1 + NS), ks);
+    theta_df_part<S>(th, td, (int)threadIdx.x - 32);
     __syncthreads();
     const BgConsts bc = bg_consts(th);
 
@@ -180,7 +177,7 @@ __global__ void __launch_bounds__(kBlock) likelihood_f32_density_kernel(const mw
     __shared__ ThetaDF<S> td;
     load_theta(th, thetas + blockIdx.y);
     __syncthreads();
-    if (threadIdx.x == 0) theta_df<S>(th, td);
+    theta_df_part<S>(th, td, (int)threadIdx.x);
     __syncthreads();
     const BgConsts bc = bg_consts(th);
     const int N = St.n_stars, NS = th.n_streams;

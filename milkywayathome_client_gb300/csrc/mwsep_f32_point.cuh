@@ -316,29 +316,31 @@ struct ThetaDF
     dfl::df a[SArr<S>::N][3], q[SArr<S>::N][3], f[SArr<S>::N];
 };
 
+/* Part i of the theta pairs: stream i's for i < S, 1/q^2 for i == S (parts
+ * are independent, so S + 1 threads form them at once; callers sync after). */
 template <int S>
-__device__ __forceinline__ void theta_df(const mwsep_theta_consts& th, ThetaDF<S>& td)
+__device__ __forceinline__ void theta_df_part(const mwsep_theta_consts& th, ThetaDF<S>& td, int i)
 {
-    td.iq2 = dfl::from_double(th.q != 0.0 ? 1.0 / (th.q * th.q) : 0.0);
-#pragma unroll
-    for (int s = 0; s < S; ++s)
+    if (i == S)
     {
-        const bool on = s < th.n_streams && th.stream_on[s];
-        const double a0 = th.a[s][0], a1 = th.a[s][1], a2 = th.a[s][2];
-        const double c0 = th.c[s][0] + MW_LBR_R, c1 = th.c[s][1], c2 = th.c[s][2];
-        const double ac = a0 * c0 + a1 * c1 + a2 * c2;
-        td.a[s][0] = dfl::from_double(on ? a0 : 0.0);
-        td.a[s][1] = dfl::from_double(on ? a1 : 0.0);
-        td.a[s][2] = dfl::from_double(on ? a2 : 0.0);
-        td.q[s][0] = dfl::from_double(on ? c0 - ac * a0 : 0.0);
-        td.q[s][1] = dfl::from_double(on ? c1 - ac * a1 : 0.0);
-        td.q[s][2] = dfl::from_double(on ? c2 - ac * a2 : 0.0);
-        td.f[s] = dfl::from_double(on ? -kLog2e / th.sigma_sq2[s] : 0.0);
+        td.iq2 = dfl::from_double(th.q != 0.0 ? 1.0 / (th.q * th.q) : 0.0);
+        return;
     }
+    if (i < 0 || i >= S) return;
+    const int s = i;
+    const bool on = s < th.n_streams && th.stream_on[s];
+    const double a0 = th.a[s][0], a1 = th.a[s][1], a2 = th.a[s][2];
+    const double c0 = th.c[s][0] + MW_LBR_R, c1 = th.c[s][1], c2 = th.c[s][2];
+    const double ac = a0 * c0 + a1 * c1 + a2 * c2;
+    td.a[s][0] = dfl::from_double(on ? a0 : 0.0);
+    td.a[s][1] = dfl::from_double(on ? a1 : 0.0);
+    td.a[s][2] = dfl::from_double(on ? a2 : 0.0);
+    td.q[s][0] = dfl::from_double(on ? c0 - ac * a0 : 0.0);
+    td.q[s][1] = dfl::from_double(on ? c1 - ac * a1 : 0.0);
+    td.q[s][2] = dfl::from_double(on ? c2 - ac * a2 : 0.0);
+    td.f[s] = dfl::from_double(on ? -kLog2e / th.sigma_sq2[s] : 0.0);
 }
 
-/* The block's theta and its pair constants: thread 0 forms them after the
- * theta is loaded (callers sync before and after). */
 __device__ __forceinline__ dfl::df df_norm(dfl::df x)
 {
     float h, l;
