@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_kernel(c
     for (long long wt = (long long)blockIdx.x * (kBlock / 32) + warp; wt < A.n_items; wt += warps)
     {
         if constexpr (PackedTile<S>::ok)
-            warp_tile2<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
+            warp_tile2<S, FORM, true>(A, th, td, bc, wt, cs[warp], acc);
         else
             warp_tile<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
     }
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kBlock, MWSEP_F32_MINB) integral_f32w_dyn_kern
 #pragma unroll
         for (int k = 0; k < 1 + S; ++k) acc[k] = 0.0;
         if constexpr (PackedTile<S>::ok)
-            warp_tile2<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
+            warp_tile2<S, FORM, true>(A, th, td, bc, wt, cs[warp], acc);
         else
             warp_tile<S, FORM>(A, th, td, bc, wt, cs[warp], acc);
 #pragma unroll
