@@ -2,9 +2,11 @@
  * every compensated kernel (single evaluation, batches, the tiled engine).
  *
  * Split of precision:
- *   FP64: the per-column (or per-star) coordinate transform with the Sun
- *         offset, the r-bin volume and convolution weight tables (built in
- *         FP64, rounded to FP32 once), the per-item and cross-block sums, the
+ *   FP64 or float pairs (~2^-44): the per-column (or per-star) coordinate
+ *         transform with the Sun offset -- in pairs on the FP32 pipe for warp
+ *         tiles and stars (column_consts_df), in FP64 for thread items -- the
+ *         r-bin volume and convolution weight tables (built in FP64, rounded
+ *         to FP32 once), the per-item and cross-block sums, the
  *         normalisation and the log-likelihood;
  *   FP32: the density at each convolution point, on the FMA pipe and the
  *         SFU (ex2 / rsqrt / rcp approximations), with Kahan-compensated
@@ -15,11 +17,11 @@
  * x = r u - (8.5, 0, 0) (cpu/evaluation_optimized.c:224-227).  Then
  *   background: x0^2 + x1^2 + x2^2/q^2 = B2 (r - rb)^2 + Db
  *   stream s:   |x - c - ((x - c).a) a|^2 = A2 (r - rs)^2 + Ds
- * with B2, rb, Db, A2, rs, Ds >= 0 computed per column in FP64.  Both forms
+ * with B2, rb, Db, A2, rs, Ds >= 0 computed per column (FP64 or pairs).  Both forms
  * are sums of non-negative terms, so FP32 evaluation has no cancellation.
  * t = r - rb is formed from (hi, lo) float pairs, so it keeps full relative
  * accuracy even where r and rb are close, and each stream reuses it:
- * r - rs = t + (rb - rs) with the FP64 offset split into (hi, lo) too.
+ * r - rs = t + (rb - rs) with the offset split into (hi, lo) too.
  * The stream exponent -|.|^2/(2 sigma^2) becomes k2 ts^2 + k0 in base 2.
  */
 #ifndef MWSEP_F32_POINT_CUH
