@@ -127,3 +127,34 @@ def test_corrupt_parameter_file_is_rejected(built_library, tmp_path):
     open(bad, "wb").write(bytes(raw[:-9]))
     with pytest.raises(mw.MwsepError):
         mw.AstronomyParameters.read_binary(bad)
+
+
+def _fnv1a(data):
+    h = 1469598103934665603
+    for b in data:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def test_parameter_format_1_still_loads(built_library, tmp_path):
+    """Format 1 stored number_background_parameters values of each background
+    array and no separate count; a file in it (the format-2 file of a problem
+    without the aux quirk, its count removed) still loads to the same struct."""
+    import struct
+    import milkywayathome_client_gb300 as mw
+    pf, _, _ = load_case("aux_profile")
+    ap = mw.AstronomyParameters.read(pf)
+    p2 = str(tmp_path / "p2.mwsp")
+    ap.write_binary(p2)
+    raw = open(p2, "rb").read()
+    magic, version, body_len = raw[:8], struct.unpack("<I", raw[8:12])[0], struct.unpack("<I", raw[12:16])[0]
+    assert version == 2
+    body = raw[16:16 + body_len]
+    nb, nv = struct.unpack("<ii", body[8:16])
+    assert nb == nv
+    body1 = body[:12] + body[16:]  # drop the stored count after number_background_parameters
+    p1 = str(tmp_path / "p1.mwsp")
+    with open(p1, "wb") as f:
+        f.write(magic + struct.pack("<II", 1, len(body1)) + body1 + struct.pack("<Q", _fnv1a(body1)))
+    back = mw.AstronomyParameters.read_binary(p1)
+    assert _fields(back) == _fields(ap)
